@@ -1,0 +1,90 @@
+// FFT plans: radix sequences and double-precision twiddle tables, cached per
+// (device, length).  The tables are allocated once per length and live until
+// process exit.
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <utility>
+#include <vector>
+
+#include "kernels.h"
+
+namespace simrecon {
+
+namespace {
+std::mutex g_mu;
+std::map<std::pair<int, int>, FFTPlan> g_plans;
+
+bool factor(int n, std::vector<int>& radix)
+{
+  radix.clear();
+  if (n < 1) return false;
+  int m = n;
+  int p2 = 0;
+  while (m % 2 == 0) {
+    m /= 2;
+    ++p2;
+  }
+  // powers of two as radix 8 / 4 (a lone factor 2 only when n is 2)
+  int k8 = p2 / 3, rem = p2 % 3;
+  if (rem == 1 && k8 >= 1) {
+    --k8;
+    radix.push_back(4);
+    radix.push_back(4);
+  } else if (rem == 1) {
+    radix.push_back(2);
+  } else if (rem == 2) {
+    radix.push_back(4);
+  }
+  for (int i = 0; i < k8; ++i) radix.push_back(8);
+  for (int r : {3, 5, 7})
+    while (m % r == 0) {
+      m /= r;
+      radix.push_back(r);
+    }
+  if (m != 1) return false;
+  if ((int)radix.size() > kMaxStages) return false;
+  return true;
+}
+}  // namespace
+
+bool fft_length_ok(int n)
+{
+  std::vector<int> r;
+  return factor(n, r);
+}
+
+bool get_fft_plan(int n, FFTPlan* plan)
+{
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_plans.find({dev, n});
+  if (it != g_plans.end()) {
+    *plan = it->second;
+    return true;
+  }
+  std::vector<int> radix;
+  if (!factor(n, radix)) return false;
+  FFTPlan p{};
+  p.n = n;
+  p.nstages = (int)radix.size();
+  for (int i = 0; i < p.nstages; ++i) p.radix[i] = radix[i];
+  std::vector<float2> tw(n);
+  for (int k = 0; k < n; ++k) {
+    double a = -2.0 * M_PI * (double)k / (double)n;
+    tw[k] = make_float2((float)cos(a), (float)sin(a));
+  }
+  float2* d = nullptr;
+  if (cudaMalloc(&d, sizeof(float2) * n) != cudaSuccess) return false;
+  if (cudaMemcpy(d, tw.data(), sizeof(float2) * n, cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(d);
+    return false;
+  }
+  p.tw = d;
+  g_plans[{dev, n}] = p;
+  *plan = p;
+  return true;
+}
+
+}  // namespace simrecon

@@ -1,0 +1,479 @@
+// Wiener filtering and band assembly.
+//
+// k_filter applies the generalized Wiener filter of filterbands
+// (gpuFunctionsImpl.cu:1222-1675) element by element.  The reference runs
+// filterbands_kernel1 twice per order over the same half-spectrum arrays:
+// the first pass treats stored column jin in [1, nx/2] as the kx = +jin
+// pixel, the second treats column 0 (kx = 0) and columns jin in
+// [1, nx/2-1] again, now as the conjugate pixel kx = -jin, ky = -y, kz = -z.
+// Here one thread owns one stored element and applies both updates in the
+// same order, so every element is read and written once.  Planes outside
+// +-zdistcutoff are cleared (filterbands_kernel3).
+//
+// Assembly (assemblerealspacebands, gpuFunctionsImpl.cu:1741-1951) sums,
+// over every direction d and order o, w * Re(IFFT3(zoom-pad(band_{d,o})) *
+// exp(i phi_{d,o}(x, y))) with w = 1 for order 0 and 2 otherwise.  The ramp
+// does not depend on z, so the z transform commutes with the sum:
+//     out = Re( IFFTz( S ) ),  S = sum_{d,o} w ramp_{d,o} * IFFTxy(band_{d,o})
+// k_asm_y (pruned, zero-padded y IFFT of every in-band kz plane),
+// k_asm_x (zero-padded x IFFT, ramp, weighted sum over all (d, o) into S)
+// and k_asm_z (one z IFFT of S, real part) write the zoomed output once.
+#include <algorithm>
+#include <vector>
+
+#include "kernels.h"
+
+namespace simrecon {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kMaxElems = kFftEPT * kThreads;
+
+__device__ __forceinline__ float dev_suppress(float x)
+{
+  float x6 = x * x * x;
+  x6 *= x6;
+  return 1.0 / (1 + 20000 / (x6 + 20));
+}
+
+__device__ __forceinline__ float dev_order0damping(float radius, float zindex, float rlimit, int zlimit)
+{
+  float rfraction = radius / rlimit;
+  float zfraction = fabsf(zindex / zlimit);
+  return rfraction * rfraction + zfraction * zfraction * zfraction;
+}
+
+// Wiener scale of pixel (x1, y1, z0) of band (dir, order), the body of
+// filterbands_kernel1 (gpuFunctionsImpl.cu:1504-1592) without the final
+// conjamp factor.
+__device__ float2 filter_scale(const FilterArgs& a, int order, int x1, int y1, int z0, float rdist1, float x1f,
+                               float y1f)
+{
+  const int dir = a.dir, no = a.norders;
+  const float kx = order * a.k0[dir].x, ky = order * a.k0[dir].y;
+  const float min_dkr = a.dkx < a.dky ? a.dkx : a.dky;
+  const float suppRadius = a.supp_radius * min_dkr;
+  float xabs = x1f + kx, yabs = y1f + ky;
+  float rdistabs = sqrtf(xabs * xabs + yabs * yabs);
+  float2 otf1 = otf_lookup(a.otf.otf[order], a.otf, x1f, y1f, z0);
+  float weight = otf1.x * otf1.x + otf1.y * otf1.y;
+  if (order != 0) weight *= a.ampmag2[dir * no + order];
+  float dampfact = 1. / a.noisevar[dir * no + order];
+  if (a.suppress && order != 0 && rdist1 <= suppRadius)
+    dampfact *= dev_suppress(rdist1 / min_dkr);
+  else if (!a.dampen0 && a.suppress && order == 0 && rdist1 <= suppRadius)
+    dampfact *= dev_suppress(rdist1 / min_dkr);
+  else if (a.dampen0 && order == 0)
+    dampfact *= dev_order0damping(rdist1, z0, a.rdistcutoff, a.zdc[0]);
+  if (order == 0 && z0 == 0 && a.nokz0) dampfact = 0;
+  weight *= dampfact;
+  float sumweight = weight;
+  for (int dir2 = 0; dir2 < a.ndirs; dir2++) {
+    for (int order2 = -(no - 1); order2 < no; order2++) {
+      if (dir2 == dir && order2 == order) continue;
+      if (!a.filteroverlaps && !(order2 == 0 && order == 0)) continue;
+      int ao2 = order2 < 0 ? -order2 : order2;
+      float amp2mag2 = a.ampmag2[dir2 * no + ao2];
+      float kx2 = order2 * a.k0[dir2].x, ky2 = order2 * a.k0[dir2].y;
+      float x2 = xabs - kx2, y2 = yabs - ky2;
+      float rdist2 = sqrtf(x2 * x2 + y2 * y2);
+      if (rdist2 < a.rdistcutoff) {
+        float2 otf2 = otf_lookup(a.otf.otf[ao2], a.otf, x2, y2, z0);
+        float w = (otf2.x * otf2.x + otf2.y * otf2.y) / a.noisevar[dir2 * no + ao2];
+        if (order2 != 0) w *= amp2mag2;
+        if (a.suppress && order2 != 0 && rdist2 <= suppRadius)
+          w *= dev_suppress(rdist2 / min_dkr);
+        else if (!a.dampen0 && a.suppress && order2 == 0 && rdist2 <= suppRadius)
+          w *= dev_suppress(rdist2 / min_dkr);
+        else if (a.dampen0 && order2 == 0)
+          w *= dev_order0damping(rdist2, z0, a.rdistcutoff, a.zdc[0]);
+        if (a.nokz0 && order2 == 0 && z0 == 0) w = 0.0f;
+        sumweight += w;
+      }
+    }
+  }
+  sumweight += a.wiener2;
+  float2 scale = make_float2(dampfact * otf1.x / sumweight, dampfact * (-otf1.y) / sumweight);
+  if (a.apodizeoutput) {
+    float rho;
+    float zdistabs = abs(z0);
+    if (a.zapocutoff > 0)
+      rho = sqrtf((rdistabs / a.apocutoff) * (rdistabs / a.apocutoff) +
+                  (zdistabs / a.zapocutoff) * (zdistabs / a.zapocutoff));
+    else
+      rho = sqrtf((rdistabs / a.apocutoff) * (rdistabs / a.apocutoff));
+    if (rho > 1.f) rho = 1.0f;
+    float apofact = 1.f;
+    if (a.apodizeoutput == 1) apofact = cosf((M_PI * 0.5f) * rho);
+    else if (a.apodizeoutput == 2) apofact = 1.0f - rho;
+    scale.x *= apofact;
+    scale.y *= apofact;
+  }
+  return scale;
+}
+
+// split re/im into plus/minus, scale plus, recombine (gpuFunctionsImpl.cu:1617-1644)
+__device__ __forceinline__ void apply_side(float2& re, float2& im, float2 scale, bool conj)
+{
+  if (conj) {
+    re.y = -re.y;
+    im.y = -im.y;
+  }
+  float2 plus = make_float2(re.x - im.y, re.y + im.x);
+  float2 minus = make_float2(re.x + im.y, re.y - im.x);
+  plus = cmul(plus, scale);
+  re = make_float2(0.5f * (plus.x + minus.x), 0.5f * (plus.y + minus.y));
+  im = make_float2(0.5f * (plus.y - minus.y), 0.5f * (-plus.x + minus.x));
+  if (conj) {
+    re.y = -re.y;
+    im.y = -im.y;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_filter(FilterArgs a)
+{
+  const int nx = a.nx, ny = a.ny, nz = a.nz, nxh = nx / 2 + 1;
+  const int order = blockIdx.z, iz = blockIdx.y;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ny * nxh) return;
+  const int iin = e / nxh, jin = e - iin * nxh;
+  const size_t plane = (size_t)ny * nxh;
+  float2* b1 = a.bands + (size_t)(order == 0 ? 0 : 2 * order - 1) * nz * plane;
+  float2* b2 = order == 0 ? nullptr : a.bands + (size_t)(2 * order) * nz * plane;
+  const size_t ind = (size_t)iz * plane + e;
+  const int zdc = a.zdc[order];
+  const bool inband = (iz <= zdc) || (iz >= nz - zdc);
+  if (!inband) {  // filterbands_kernel3
+    b1[ind] = make_float2(0.f, 0.f);
+    if (b2) b2[ind] = make_float2(0.f, 0.f);
+    return;
+  }
+  const int z0 = iz <= zdc ? iz : iz - nz;
+  // the pixel this element is the non-conjugate copy of
+  const int y1 = (iin < ny - ny / 2) ? iin : iin - ny;
+  const int x1 = jin;
+  float x1f = x1 * a.dkx, y1f = y1 * a.dky;
+  float rdist1 = sqrtf(x1f * x1f + y1f * y1f);
+  if (!(rdist1 <= a.rdistcutoff)) {
+    b1[ind] = make_float2(0.f, 0.f);
+    if (b2) b2[ind] = make_float2(0.f, 0.f);
+    return;
+  }
+  float2 s1 = filter_scale(a, order, x1, y1, z0, rdist1, x1f, y1f);
+  if (order == 0) {
+    b1[ind] = cmul(b1[ind], s1);
+    return;
+  }
+  float2 re = b1[ind], im = b2[ind];
+  apply_side(re, im, cmul(s1, a.conjamp[order]), false);
+  if (jin >= 1 && jin <= nx / 2 - 1) {
+    // second pass: the conjugate pixel (-jin, -y, -z0)
+    const int y2 = (iin <= ny / 2) ? -iin : ny - iin;
+    const int x2 = -jin;
+    float x2f = x2 * a.dkx, y2f = y2 * a.dky;
+    float rdist2 = sqrtf(x2f * x2f + y2f * y2f);
+    float2 s2 = filter_scale(a, order, x2, y2, -z0, rdist2, x2f, y2f);
+    apply_side(re, im, cmul(s2, a.conjamp[order]), true);
+  }
+  b1[ind] = re;
+  b2[ind] = im;
+}
+
+struct Slot {
+  int dir, order, kz, zout;
+};
+
+// zero-padded inverse FFT along y of the in-band plane kz of band (d, o);
+// columns c = kx + nx/2 - 1, kx in [-nx/2+1, nx/2] (move_kernel ranges,
+// gpuFunctionsImpl.cu:1853-1913)
+__global__ void k_asm_y(AssembleArgs a, const Slot* __restrict__ slots, FFTPlan plan, int W)
+{
+  extern __shared__ float2 sm[];
+  const Slot sl = slots[blockIdx.y];
+  const int nx = a.nx, ny = a.ny, nz = a.nz, nxh = nx / 2 + 1, Y = a.Y;
+  const int c0 = blockIdx.x * W;
+  const size_t plane = (size_t)ny * nxh;
+  const float2* br = a.bands + ((size_t)sl.dir * a.nphases + (sl.order == 0 ? 0 : 2 * sl.order - 1)) * nz * plane;
+  const float2* bi = sl.order == 0 ? nullptr : a.bands + ((size_t)sl.dir * a.nphases + 2 * sl.order) * nz * plane;
+  const int ylo = ny / 2 - 1;  // ky in [-ylo, ny/2]
+  for (int t = threadIdx.x; t < Y * W; t += blockDim.x) {
+    int yr = t / W, w = t - yr * W;
+    int c = c0 + w;
+    float2 v = make_float2(0.f, 0.f);
+    int ky;
+    bool valid = c < nx;
+    if (yr <= ny / 2) ky = yr;
+    else if (yr >= Y - ylo) ky = yr - Y;
+    else valid = false;
+    if (valid) {
+      int x = c - (nx / 2 - 1), y = ky, z = sl.kz;
+      bool conj = x < 0;
+      if (conj) {
+        x = -x;
+        y = -y;
+        z = -z;
+      }
+      if (y < 0) y += ny;
+      if (z < 0) z += nz;
+      size_t indin = (size_t)z * plane + (size_t)y * nxh + x;
+      if (sl.order == 0) {
+        v = br[indin];
+        if (conj) v.y = -v.y;
+      } else {
+        float2 re = br[indin], im = bi[indin];
+        if (conj) {
+          re.y = -re.y;
+          im.y = -im.y;
+        }
+        v = make_float2(re.x - im.y, re.y + im.x);
+      }
+    }
+    sm[t] = v;
+  }
+  __syncthreads();
+  fft_lines<+1>(sm, plan, W, 1, W);
+  float2* dst = a.T + (size_t)blockIdx.y * Y * nx;
+  for (int t = threadIdx.x; t < Y * W; t += blockDim.x) {
+    int yr = t / W, w = t - yr * W;
+    if (c0 + w < nx) dst[(size_t)yr * nx + c0 + w] = sm[t];
+  }
+}
+
+// zero-padded inverse FFT along x of every slot of output plane zout, ramp,
+// weighted sum -> S[zout][yr][:]
+constexpr int kAccPerThread = 16;
+__global__ void __launch_bounds__(512) k_asm_x(AssembleArgs a, const int* __restrict__ plane_slot0,
+                                               const int* __restrict__ plane_nslot, const Slot* __restrict__ slots,
+                                               const int* __restrict__ plane_zout, FFTPlan plan, int lines)
+{
+  extern __shared__ float2 sm[];
+  const int nx = a.nx, X = a.X, Y = a.Y;
+  const int pidx = blockIdx.y, yr = blockIdx.x;
+  const int s0 = plane_slot0[pidx], ns = plane_nslot[pidx], zout = plane_zout[pidx];
+  float2 acc[kAccPerThread];
+#pragma unroll
+  for (int k = 0; k < kAccPerThread; ++k) acc[k] = make_float2(0.f, 0.f);
+  const int xlo = nx / 2 - 1;
+  for (int b0 = 0; b0 < ns; b0 += lines) {
+    int nb = min(lines, ns - b0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < lines * X; t += blockDim.x) {
+      int l = t / X, xo = t - l * X;
+      float2 v = make_float2(0.f, 0.f);
+      if (l < nb) {
+        int kx = xo <= nx / 2 ? xo : (xo >= X - xlo ? xo - X : 1 << 30);
+        if (kx != (1 << 30)) {
+          int c = kx + xlo;
+          v = a.T[((size_t)(s0 + b0 + l) * Y + yr) * nx + c];
+        }
+      }
+      sm[t] = v;
+    }
+    __syncthreads();
+    fft_lines<+1>(sm, plan, lines, X, 1);
+    for (int l = 0; l < nb; ++l) {
+      const Slot sl = slots[s0 + b0 + l];
+      const int ro = sl.dir * a.norders + sl.order;
+      const float w = sl.order == 0 ? 1.f : 2.f;
+      float2 ey = a.ey[(size_t)ro * Y + yr];
+      ey.x *= w;
+      ey.y *= w;
+#pragma unroll
+      for (int k = 0; k < kAccPerThread; ++k) {
+        int x = threadIdx.x + k * blockDim.x;
+        if (x < X) {
+          float2 e = cmul(a.ex[(size_t)ro * X + x], ey);
+          float2 v = cmul(sm[l * X + x], e);
+          acc[k].x += v.x;
+          acc[k].y += v.y;
+        }
+      }
+    }
+  }
+  float2* dst = a.S + ((size_t)zout * Y + yr) * X;
+#pragma unroll
+  for (int k = 0; k < kAccPerThread; ++k) {
+    int x = threadIdx.x + k * blockDim.x;
+    if (x < X) dst[x] = acc[k];
+  }
+}
+
+// inverse FFT along z of S, real part -> out
+__global__ void __launch_bounds__(kThreads) k_asm_z(AssembleArgs a, const unsigned char* __restrict__ zactive,
+                                                    FFTPlan plan, int W)
+{
+  extern __shared__ float2 sm[];
+  const int X = a.X, Y = a.Y, Z = a.Z;
+  const int yr = blockIdx.y, c0 = blockIdx.x * W;
+  for (int t = threadIdx.x; t < Z * W; t += blockDim.x) {
+    int z = t / W, w = t - z * W;
+    sm[t] = (zactive[z] && c0 + w < X) ? a.S[((size_t)z * Y + yr) * X + c0 + w] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  fft_lines<+1>(sm, plan, W, 1, W);
+  for (int t = threadIdx.x; t < Z * W; t += blockDim.x) {
+    int z = t / W, w = t - z * W;
+    if (c0 + w < X) a.out[((size_t)z * Y + yr) * X + c0 + w] = sm[t].x;
+  }
+}
+
+__global__ void k_ramp(const float2* k0, int ndirs, int norders, int X, int Y, float dxyz, float fact, float2* ex,
+                       float2* ey)
+{
+  int n = ndirs * norders * (X + Y);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    int ro = t / (X + Y), r = t - ro * (X + Y);
+    int d = ro / norders, o = ro - d * norders;
+    float kx = k0[d].x * (float)o, ky = k0[d].y * (float)o;
+    double ang;
+    if (r < X) ang = (double)fact * M_PI * (double)(r - X / 2) * (double)kx * (double)dxyz;
+    else ang = (double)fact * M_PI * (double)((r - X) - Y / 2) * (double)ky * (double)dxyz;
+    double s, c;
+    sincos(ang, &s, &c);
+    float2 v = make_float2((float)c, (float)s);
+    if (r < X) ex[(size_t)ro * X + r] = v;
+    else ey[(size_t)ro * Y + (r - X)] = v;
+  }
+}
+
+__global__ void k_fill(float* buf, size_t n, float v)
+{
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    buf[i] = v;
+}
+
+// per-process device scratch for the small slot tables (re-uploaded per call)
+struct SlotTables {
+  Slot* slots = nullptr;
+  int* p0 = nullptr;
+  int* pn = nullptr;
+  int* pz = nullptr;
+  unsigned char* zact = nullptr;
+  int cap_slots = 0, cap_planes = 0;
+};
+
+}  // namespace
+
+int launch_filter(const FilterArgs& a, cudaStream_t s, long long* launches)
+{
+  const int nxh = a.nx / 2 + 1;
+  dim3 g((a.ny * nxh + kThreads - 1) / kThreads, a.nz, a.norders);
+  k_filter<<<g, kThreads, 0, s>>>(a);
+  if (launches) *launches += 1;
+  return (int)cudaGetLastError();
+}
+
+int launch_ramp_tables(const float2* k0, int ndirs, int norders, int X, int Y, float dxyz, float fact, float2* ex,
+                       float2* ey, cudaStream_t s, long long* launches)
+{
+  int n = ndirs * norders * (X + Y);
+  k_ramp<<<std::min(1024, (n + 255) / 256), 256, 0, s>>>(k0, ndirs, norders, X, Y, dxyz, fact, ex, ey);
+  if (launches) *launches += 1;
+  return (int)cudaGetLastError();
+}
+
+int launch_fill(float* buf, size_t n, float v, cudaStream_t s, long long* launches)
+{
+  k_fill<<<1216, 256, 0, s>>>(buf, n, v);
+  if (launches) *launches += 1;
+  return (int)cudaGetLastError();
+}
+
+// The slot tables live in a small per-call device buffer carved from T's
+// tail: the host fills them with cudaMemcpyAsync from pageable memory, which
+// is synchronous with respect to the host but ordered on the stream.
+int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
+{
+  FFTPlan py, px, pz;
+  if (!get_fft_plan(a.Y, &py) || !get_fft_plan(a.X, &px) || !get_fft_plan(a.Z, &pz)) return -1;
+  const int nx = a.nx, nz = a.nz;
+  // signed kz planes of the band grid (move_kernel: z in [-nz/2+1, nz/2])
+  std::vector<int> kzs;
+  if (nz > 1)
+    for (int z = -(nz / 2 - 1); z <= nz / 2; ++z) kzs.push_back(z);
+  else
+    kzs.push_back(0);
+  // slots per plane
+  std::vector<Slot> slots;
+  std::vector<int> p0, pn, pz;
+  std::vector<unsigned char> zact(a.Z, 0);
+  for (int kz : kzs) {
+    int start = (int)slots.size();
+    for (int d = 0; d < a.ndirs; ++d)
+      for (int o = 0; o < a.norders; ++o) {
+        int az = kz < 0 ? -kz : kz;
+        if (az <= a.zdc[o]) {
+          int zo = kz;
+          if (zo < 0) zo += a.Z;
+          slots.push_back(Slot{d, o, kz, zo});
+        }
+      }
+    int cnt = (int)slots.size() - start;
+    if (cnt > 0) {
+      int zo = kz < 0 ? kz + a.Z : kz;
+      p0.push_back(start);
+      pn.push_back(cnt);
+      pz.push_back(zo);
+      zact[zo] = 1;
+    }
+  }
+  // device copies of the tables: placed after the T scratch region
+  const size_t per_slot = (size_t)a.Y * nx;  // complex elements of T per slot
+  size_t table_bytes = slots.size() * sizeof(Slot) + 3 * p0.size() * sizeof(int) + a.Z + 64;
+  size_t table_elems = (table_bytes + sizeof(float2) - 1) / sizeof(float2) + 8;
+  if (a.tcap < per_slot + table_elems) return -2;
+  const size_t tslots = (a.tcap - table_elems) / per_slot;  // slots that fit in T at once
+  char* tail = (char*)(a.T + tslots * per_slot);
+  tail = (char*)(((uintptr_t)tail + 15) & ~(uintptr_t)15);
+  Slot* d_slots = (Slot*)tail;
+  int* d_p0 = (int*)(d_slots + slots.size());
+  int* d_pn = d_p0 + p0.size();
+  int* d_pz = d_pn + p0.size();
+  unsigned char* d_zact = (unsigned char*)(d_pz + p0.size());
+  cudaMemcpyAsync(d_slots, slots.data(), slots.size() * sizeof(Slot), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(d_p0, p0.data(), p0.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(d_pn, pn.data(), pn.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(d_pz, pz.data(), pz.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(d_zact, zact.data(), a.Z, cudaMemcpyHostToDevice, s);
+  // tile sizes
+  int Wy = std::max(1, std::min(32, kMaxElems / a.Y));
+  size_t smy = (size_t)Wy * a.Y * sizeof(float2);
+  cudaFuncSetAttribute(k_asm_y, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
+  int xlines = std::max(1, (kFftEPT * 512) / a.X);
+  xlines = std::min(xlines, 16);
+  size_t smx = (size_t)xlines * a.X * sizeof(float2);
+  cudaFuncSetAttribute(k_asm_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+  if (a.X > kAccPerThread * 512) return -3;
+  // process whole planes in groups whose slots fit in T
+  size_t np = p0.size();
+  size_t pi = 0;
+  long long nl = 0;
+  while (pi < np) {
+    size_t pj = pi;
+    int first = p0[pi];
+    while (pj < np && (size_t)(p0[pj] + pn[pj] - first) <= tslots) ++pj;
+    if (pj == pi) return -4;
+    int nsl = p0[pj - 1] + pn[pj - 1] - first;
+    // T holds slots [first, first + nsl); shift the slot pointer so that
+    // blockIdx.y indexes T from 0
+    AssembleArgs ay = a;
+    k_asm_y<<<dim3((nx + Wy - 1) / Wy, nsl), kThreads, smy, s>>>(ay, d_slots + first, py, Wy);
+    // k_asm_x reads T[(slot - first)]: pass a shifted T base
+    AssembleArgs ax = a;
+    ax.T = a.T - (size_t)first * per_slot;
+    k_asm_x<<<dim3(a.Y, (unsigned)(pj - pi)), 512, smx, s>>>(ax, d_p0 + pi, d_pn + pi, d_slots, d_pz + pi, px,
+                                                              xlines);
+    nl += 2;
+    pi = pj;
+  }
+  int Wz = std::max(1, std::min(32, kMaxElems / a.Z));
+  size_t smz = (size_t)Wz * a.Z * sizeof(float2);
+  cudaFuncSetAttribute(k_asm_z, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
+  k_asm_z<<<dim3((a.X + Wz - 1) / Wz, a.Y), kThreads, smz, s>>>(a, d_zact, pz, Wz);
+  nl += 1;
+  if (launches) *launches += nl;
+  return (int)cudaGetLastError();
+}
+
+}  // namespace simrecon

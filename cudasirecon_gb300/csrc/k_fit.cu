@@ -1,0 +1,467 @@
+// Pattern-vector (k0) and modulation-amplitude fitting kernels.
+//
+// The reference builds two full-complex "overlap" volumes per fit step
+// (makeoverlaps, gpuFunctionsImpl.cu:497-872), inverse-3D-FFTs them, and then
+// reduces sum_z conj(X) Y e^{i phi} for every candidate k0 (reductionKernel,
+// gpuFunctionsImpl.cu:1150-1220) or sum_z X conj(Y) for the cross-correlation
+// (aTimesConjBKernel, 391-414).  Both only need, per lateral pixel, the
+// z-sum of conj(X) Y.  By Parseval along z that equals
+//     nz * sum_kz conj(X~(kz)) Y~(kz),   X~ = 2D inverse FFT of plane kz,
+// so the z transform is never performed: only the 2*zdc+1 non-zero kz
+// planes are built and transformed in x and y, and their products are
+// accumulated straight into a 2D map P(x, y).  Every candidate k0 of the
+// search is then a 2D weighted sum over P.
+//
+//   k_ovl_build_x   build both overlaps (OTF-weighted band values) row by
+//                   row and inverse-FFT along x
+//   k_ovl_y_accum   inverse FFT along y, accumulate conj(X)Y, |X|^2, |Y|^2
+//                   over a group of kz planes
+//   k_p_reduce      sum the plane-group partial maps, finish |X|^2, |Y|^2
+//   k_fft_rows/cols cross-correlation FFT of conj(P)
+//   k_argmax_*      intensity peak with its neighbours
+//   k_modamp_*      sum_xy P e^{i phi_c} for a batch of candidates
+#include <algorithm>
+
+#include "kernels.h"
+
+namespace simrecon {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kMaxElems = kFftEPT * kThreads;
+
+// ---------------------------------------------------------------- overlaps
+__global__ void __launch_bounds__(kThreads) k_ovl_build_x(OverlapArgs a, FFTPlan plan, int rows_per_cta)
+{
+  extern __shared__ float2 sm[];
+  const int nx = a.nx, ny = a.ny, nz = a.nz, nxh = nx / 2 + 1;
+  const int nzb = 2 * a.zdc + 1;
+  const int row0 = blockIdx.x * rows_per_cta;
+  const int nrows = min(rows_per_cta, nzb * ny - row0);
+  const size_t bplane = (size_t)ny * nxh;
+  const float2* b1re = a.order1 == 0 ? a.bands : a.bands + (size_t)(2 * a.order1 - 1) * nz * bplane;
+  const float2* b1im = a.order1 == 0 ? nullptr : a.bands + (size_t)(2 * a.order1) * nz * bplane;
+  const float2* b2re = a.bands + (size_t)(2 * a.order2 - 1) * nz * bplane;
+  const float2* b2im = a.bands + (size_t)(2 * a.order2) * nz * bplane;
+  const float2* otfA = a.otf.otf[a.order1];
+  const float2* otfB = a.otf.otf[a.order2];
+  const float cut = a.rdistcutoff;
+  for (int t = threadIdx.x; t < 2 * rows_per_cta * nx; t += blockDim.x) {
+    int l = t / nx, j = t - l * nx;
+    int r = l >> 1, ov = l & 1;
+    float2 val = make_float2(0.f, 0.f);
+    if (r < nrows) {
+      int row = row0 + r;
+      int zb = row / ny, i = row - zb * ny;
+      int z0 = zb - a.zdc;
+      float x1f = (float)j, y1f = (float)i;
+      if (x1f > nx / 2) x1f -= nx;
+      if (y1f > ny / 2) y1f -= ny;
+      x1f *= a.dkx;
+      y1f *= a.dky;
+      float rdist1 = sqrtf(x1f * x1f + y1f * y1f);
+      bool conj = j > nx / 2;
+      int jin = conj ? nx - j : j;
+      int iin = conj ? (ny - i) % ny : i;
+      int zin = ((conj ? -z0 : z0) + nz) % nz;
+      size_t indin = (size_t)zin * bplane + (size_t)iin * nxh + jin;
+      bool skip = (z0 == 0 && a.nokz0);
+      if (!skip && ov == 0 && rdist1 <= cut) {
+        // makeOverlaps0Kernel, gpuFunctionsImpl.cu:677-778
+        float x12 = x1f - a.kx, y12 = y1f - a.ky;
+        if (sqrtf(x12 * x12 + y12 * y12) <= cut) {
+          float2 o1 = otf_lookup(otfA, a.otf, x1f, y1f, z0);
+          if (sqrtf(cmag2(o1)) > a.otfcutoff) {
+            float2 o12 = otf_lookup(otfB, a.otf, x12, y12, z0);
+            if (sqrtf(cmag2(o12)) * a.order0_2_factor > a.otfcutoff) {
+              float root = sqrtf(cmag2(o1) + cmag2(o12));
+              float2 fact = make_float2(o12.x / root, o12.y / root);
+              float2 vre = b1re[indin];
+              float2 vim = b1im ? b1im[indin] : make_float2(0.f, 0.f);
+              if (conj) {
+                vre.y = -vre.y;
+                vim.y = -vim.y;
+              }
+              vre = cmul(vre, fact);
+              vim = cmul(vim, fact);
+              val = make_float2(vre.x - vim.y, vre.y + vim.x);
+            }
+          }
+        }
+      } else if (!skip && ov == 1 && rdist1 < cut) {
+        // makeOverlaps1Kernel, gpuFunctionsImpl.cu:780-872
+        float x21 = x1f + a.kx, y21 = y1f + a.ky;
+        if (sqrtf(x21 * x21 + y21 * y21) <= cut) {
+          float2 o2 = otf_lookup(otfB, a.otf, x1f, y1f, z0);
+          if (sqrtf(cmag2(o2)) * a.order0_2_factor > a.otfcutoff) {
+            float2 o21 = otf_lookup(otfA, a.otf, x21, y21, z0);
+            if (sqrtf(cmag2(o21)) > a.otfcutoff) {
+              float root = sqrtf(cmag2(o2) + cmag2(o21));
+              float2 fact = make_float2(o21.x / root, o21.y / root);
+              float2 vre = b2re[indin];
+              float2 vim = b2im[indin];
+              if (conj) {
+                vre.y = -vre.y;
+                vim.y = -vim.y;
+              }
+              vre = cmul(vre, fact);
+              vim = cmul(vim, fact);
+              val = make_float2(vre.x - vim.y, vre.y + vim.x);
+            }
+          }
+        }
+      }
+    }
+    sm[l * nx + j] = val;
+  }
+  __syncthreads();
+  fft_lines<+1>(sm, plan, 2 * rows_per_cta, nx, 1);
+  const size_t vol = (size_t)nzb * ny * nx;
+  for (int t = threadIdx.x; t < 2 * nrows * nx; t += blockDim.x) {
+    int l = t / nx, j = t - l * nx;
+    int r = l >> 1, ov = l & 1;
+    a.ovl[(size_t)ov * vol + (size_t)(row0 + r) * nx + j] = sm[t];
+  }
+}
+
+__global__ void k_ovl_y_accum(OverlapArgs a, FFTPlan plan, int W, int planes_per_group)
+{
+  extern __shared__ float2 sm[];
+  __shared__ double red[32];
+  const int nx = a.nx, ny = a.ny;
+  const int nzb = 2 * a.zdc + 1;
+  const int c0 = blockIdx.x * W;
+  const int zb0 = blockIdx.y * planes_per_group;
+  const int zb1 = min(nzb, zb0 + planes_per_group);
+  const int ld = 2 * W;
+  float2* acc = sm + (size_t)ny * ld;  // [ny][W]
+  for (int t = threadIdx.x; t < ny * W; t += blockDim.x) acc[t] = make_float2(0.f, 0.f);
+  double sx = 0.0, sy = 0.0;
+  const size_t vol = (size_t)nzb * ny * nx;
+  for (int zb = zb0; zb < zb1; ++zb) {
+    __syncthreads();
+    for (int t = threadIdx.x; t < ny * ld; t += blockDim.x) {
+      int y = t / ld, q = t - y * ld;
+      int ov = q >= W, w = q - ov * W;
+      sm[t] = (c0 + w < nx) ? a.ovl[(size_t)ov * vol + ((size_t)zb * ny + y) * nx + c0 + w] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    fft_lines<+1>(sm, plan, ld, 1, ld);
+    for (int t = threadIdx.x; t < ny * W; t += blockDim.x) {
+      int y = t / W, w = t - y * W;
+      float2 X = sm[y * ld + w], Y = sm[y * ld + W + w];
+      float2 p = acc[t];
+      // conj(X) * Y, as reductionKernel's xsy (gpuFunctionsImpl.cu:1177-1178)
+      p.x += X.x * Y.x + X.y * Y.y;
+      p.y += X.x * Y.y - X.y * Y.x;
+      acc[t] = p;
+      sx += (double)cmag2(X);
+      sy += (double)cmag2(Y);
+    }
+  }
+  __syncthreads();
+  float2* dst = a.ppart + (size_t)blockIdx.y * ny * nx;
+  for (int t = threadIdx.x; t < ny * W; t += blockDim.x) {
+    int y = t / W, w = t - y * W;
+    if (c0 + w < nx) dst[(size_t)y * nx + c0 + w] = acc[t];
+  }
+  double tx = block_sum_d(sx, red);
+  double ty = block_sum_d(sy, red);
+  if (threadIdx.x == 0) {
+    int cta = blockIdx.y * gridDim.x + blockIdx.x;
+    a.sums[2 * cta] = tx;
+    a.sums[2 * cta + 1] = ty;
+  }
+}
+
+// P = nz * sum_g Ppart[g];  sumxy = nz * sum of the CTA partial sums
+__global__ void k_p_reduce(OverlapArgs a, int ngroups, int nctas)
+{
+  __shared__ double red[32];
+  const size_t n = (size_t)a.nx * a.ny;
+  const float fz = (float)a.nz;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    float2 s = a.ppart[i];
+    for (int g = 1; g < ngroups; ++g) {
+      float2 v = a.ppart[(size_t)g * n + i];
+      s.x += v.x;
+      s.y += v.y;
+    }
+    a.pmap[i] = make_float2(s.x * fz, s.y * fz);
+  }
+  if (blockIdx.x == 0) {
+    double sx = 0.0, sy = 0.0;
+    for (int i = threadIdx.x; i < nctas; i += blockDim.x) {
+      sx += a.sums[2 * i];
+      sy += a.sums[2 * i + 1];
+    }
+    sx = block_sum_d(sx, red);
+    sy = block_sum_d(sy, red);
+    if (threadIdx.x == 0) {
+      a.sumxy[0] = sx * a.nz;
+      a.sumxy[1] = sy * a.nz;
+    }
+  }
+}
+
+// ---------------------------------------------------------- generic FFTs
+// rows of a [nrows][n] array; CONJ_IN conjugates the input on load
+template <int DIR, bool CONJ_IN>
+__global__ void __launch_bounds__(kThreads) k_fft_rows(const float2* in, float2* out, int n, int nrows, FFTPlan plan,
+                                                       int nl)
+{
+  extern __shared__ float2 sm[];
+  const int r0 = blockIdx.x * nl;
+  const int nr = min(nl, nrows - r0);
+  for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
+    int l = t / n;
+    float2 v = l < nr ? in[(size_t)r0 * n + t] : make_float2(0.f, 0.f);
+    if (CONJ_IN) v.y = -v.y;
+    sm[t] = v;
+  }
+  __syncthreads();
+  fft_lines<DIR>(sm, plan, nl, n, 1);
+  for (int t = threadIdx.x; t < nr * n; t += blockDim.x) out[(size_t)r0 * n + t] = sm[t];
+}
+
+template <int DIR>
+__global__ void __launch_bounds__(kThreads) k_fft_cols2(float2* data, int n, int ncol, FFTPlan plan, int W)
+{
+  extern __shared__ float2 sm[];
+  const int c0 = blockIdx.x * W;
+  for (int t = threadIdx.x; t < n * W; t += blockDim.x) {
+    int i = t / W, w = t - i * W;
+    sm[t] = (c0 + w < ncol) ? data[(size_t)i * ncol + c0 + w] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  fft_lines<DIR>(sm, plan, W, 1, W);
+  for (int t = threadIdx.x; t < n * W; t += blockDim.x) {
+    int i = t / W, w = t - i * W;
+    if (c0 + w < ncol) data[(size_t)i * ncol + c0 + w] = sm[t];
+  }
+}
+
+// ---------------------------------------------------------------- argmax
+// first maximum in row-major order (findpeak, gpuFunctionsImpl.cu:443-457)
+__device__ __forceinline__ void better(float& bv, int& bi, float v, int i)
+{
+  if (v > bv || (v == bv && i < bi)) {
+    bv = v;
+    bi = i;
+  }
+}
+
+__global__ void k_argmax_partial(const float2* cc, int n, float* bval, int* bidx)
+{
+  float bv = -1e30f;
+  int bi = 0x7fffffff;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float2 c = cc[i];
+    better(bv, bi, c.x * c.x + c.y * c.y, i);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    float ov = __shfl_down_sync(0xffffffffu, bv, o);
+    int oi = __shfl_down_sync(0xffffffffu, bi, o);
+    better(bv, bi, ov, oi);
+  }
+  __shared__ float sv[32];
+  __shared__ int si[32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    sv[wid] = bv;
+    si[wid] = bi;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    int nw = blockDim.x >> 5;
+    bv = lane < nw ? sv[lane] : -1e30f;
+    bi = lane < nw ? si[lane] : 0x7fffffff;
+    for (int o = 16; o > 0; o >>= 1) {
+      float ov = __shfl_down_sync(0xffffffffu, bv, o);
+      int oi = __shfl_down_sync(0xffffffffu, bi, o);
+      better(bv, bi, ov, oi);
+    }
+    if (lane == 0) {
+      bval[blockIdx.x] = bv;
+      bidx[blockIdx.x] = bi;
+    }
+  }
+}
+
+__device__ __forceinline__ float inten(const float2* cc, int i)
+{
+  float2 c = cc[i];
+  return c.x * c.x + c.y * c.y;
+}
+
+__global__ void k_argmax_final(const float2* cc, int nx, int ny, const float* bval, const int* bidx, int nb,
+                               float* peak)
+{
+  float bv = -1e30f;
+  int bi = 0x7fffffff;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) better(bv, bi, bval[i], bidx[i]);
+  for (int o = 16; o > 0; o >>= 1) {
+    float ov = __shfl_down_sync(0xffffffffu, bv, o);
+    int oi = __shfl_down_sync(0xffffffffu, bi, o);
+    better(bv, bi, ov, oi);
+  }
+  __shared__ float sv[32];
+  __shared__ int si[32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    sv[wid] = bv;
+    si[wid] = bi;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int nw = blockDim.x >> 5;
+    for (int w = 1; w < nw; ++w) better(sv[0], si[0], sv[w], si[w]);
+    int idx = si[0];
+    int ix = idx % nx, iy = idx / nx;
+    peak[0] = (float)ix;
+    peak[1] = (float)iy;
+    peak[2] = inten(cc, iy * nx + (ix + nx - 1) % nx);
+    peak[3] = inten(cc, idx);
+    peak[4] = inten(cc, iy * nx + (ix + 1) % nx);
+    peak[5] = inten(cc, ((iy + ny - 1) % ny) * nx + ix);
+    peak[6] = inten(cc, ((iy + 1) % ny) * nx + ix);
+  }
+}
+
+// ---------------------------------------------------- modamp candidates
+constexpr int kCand = 8;  // candidates per pass (register accumulators)
+
+// ex[c][x] = exp(i 2 pi (x - nx/2) kx_c dxy), ey[c][y] likewise
+__global__ void k_phase_tables(const float2* kc, int ncand, int nx, int ny, float dxy, float2* ex, float2* ey)
+{
+  int n = ncand * (nx + ny);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    int c = t / (nx + ny), r = t - c * (nx + ny);
+    double ang;
+    if (r < nx) ang = 2.0 * M_PI * ((double)r - 0.5 * nx) * (double)kc[c].x * (double)dxy;
+    else ang = 2.0 * M_PI * ((double)(r - nx) - 0.5 * ny) * (double)kc[c].y * (double)dxy;
+    double s, co;
+    sincos(ang, &s, &co);
+    float2 v = make_float2((float)co, (float)s);
+    if (r < nx) ex[(size_t)c * nx + r] = v;
+    else ey[(size_t)c * ny + (r - nx)] = v;
+  }
+}
+
+__global__ void k_modamp_partial(const float2* __restrict__ P, int nx, int ny, const float2* __restrict__ ex,
+                                 const float2* __restrict__ ey, int c0, int nc, double* partial, int ncand)
+{
+  __shared__ double red[32];
+  float2 acc[kCand];
+#pragma unroll
+  for (int c = 0; c < kCand; ++c) acc[c] = make_float2(0.f, 0.f);
+  const int n = nx * ny;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    int y = i / nx, x = i - y * nx;
+    float2 p = P[i];
+#pragma unroll
+    for (int c = 0; c < kCand; ++c) {
+      if (c < nc) {
+        float2 e = cmul(__ldg(ex + (size_t)(c0 + c) * nx + x), __ldg(ey + (size_t)(c0 + c) * ny + y));
+        float2 v = cmul(p, e);
+        acc[c].x += v.x;
+        acc[c].y += v.y;
+      }
+    }
+  }
+  for (int c = 0; c < nc; ++c) {
+    double re = block_sum_d((double)acc[c].x, red);
+    double im = block_sum_d((double)acc[c].y, red);
+    if (threadIdx.x == 0) {
+      partial[((size_t)blockIdx.x * ncand + c0 + c) * 2] = re;
+      partial[((size_t)blockIdx.x * ncand + c0 + c) * 2 + 1] = im;
+    }
+  }
+}
+
+__global__ void k_modamp_final(const double* partial, int nblocks, int ncand, double* out)
+{
+  __shared__ double red[32];
+  int c = blockIdx.x;
+  double re = 0.0, im = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+    re += partial[((size_t)b * ncand + c) * 2];
+    im += partial[((size_t)b * ncand + c) * 2 + 1];
+  }
+  re = block_sum_d(re, red);
+  im = block_sum_d(im, red);
+  if (threadIdx.x == 0) {
+    out[2 * c] = re;
+    out[2 * c + 1] = im;
+  }
+}
+
+}  // namespace
+
+int launch_overlaps(OverlapArgs& a, cudaStream_t s, long long* launches)
+{
+  FFTPlan px, py;
+  if (!get_fft_plan(a.nx, &px) || !get_fft_plan(a.ny, &py)) return -1;
+  const int nzb = 2 * a.zdc + 1;
+  // 1) build + x inverse FFT
+  int rows = std::max(1, kMaxElems / (2 * a.nx));
+  rows = std::min(rows, nzb * a.ny);
+  size_t sm1 = (size_t)2 * rows * a.nx * sizeof(float2);
+  int nb1 = (nzb * a.ny + rows - 1) / rows;
+  cudaFuncSetAttribute(k_ovl_build_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
+  k_ovl_build_x<<<nb1, kThreads, sm1, s>>>(a, px, rows);
+  // 2) y inverse FFT + accumulation over kz planes
+  int threads = 2 * 8 * a.ny > kMaxElems ? 512 : 256;
+  int W = std::max(1, std::min(16, (kFftEPT * threads) / (2 * a.ny)));
+  int tiles = (a.nx + W - 1) / W;
+  int groups = std::max(1, std::min(nzb, (2 * 152 + tiles - 1) / tiles));
+  int ppg = (nzb + groups - 1) / groups;
+  groups = (nzb + ppg - 1) / ppg;
+  size_t sm2 = (size_t)a.ny * (2 * W + W) * sizeof(float2);
+  cudaFuncSetAttribute(k_ovl_y_accum, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+  k_ovl_y_accum<<<dim3(tiles, groups), threads, sm2, s>>>(a, py, W, ppg);
+  // 3) reduce plane groups
+  k_p_reduce<<<std::min(1024, (a.nx * a.ny + 255) / 256), 256, 0, s>>>(a, groups, tiles * groups);
+  if (launches) *launches += 3;
+  return (int)cudaGetLastError();
+}
+
+int launch_crosscorr_peak(const float2* pmap, float2* cc, int nx, int ny, float* blockval, int* blockidx,
+                          float* peak, cudaStream_t s, long long* launches)
+{
+  FFTPlan px, py;
+  if (!get_fft_plan(nx, &px) || !get_fft_plan(ny, &py)) return -1;
+  int nl = std::max(1, std::min(ny, kMaxElems / nx));
+  size_t sm1 = (size_t)nl * nx * sizeof(float2);
+  cudaFuncSetAttribute(k_fft_rows<-1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
+  k_fft_rows<-1, true><<<(ny + nl - 1) / nl, kThreads, sm1, s>>>(pmap, cc, nx, ny, px, nl);
+  int W = std::max(1, std::min(32, kMaxElems / ny));
+  size_t sm2 = (size_t)W * ny * sizeof(float2);
+  cudaFuncSetAttribute(k_fft_cols2<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+  k_fft_cols2<-1><<<(nx + W - 1) / W, kThreads, sm2, s>>>(cc, ny, nx, py, W);
+  int nb = 256;
+  k_argmax_partial<<<nb, 256, 0, s>>>(cc, nx * ny, blockval, blockidx);
+  k_argmax_final<<<1, 256, 0, s>>>(cc, nx, ny, blockval, blockidx, nb, peak);
+  if (launches) *launches += 4;
+  return (int)cudaGetLastError();
+}
+
+int launch_modamp_candidates(const float2* pmap, int nx, int ny, float dxy, const float2* kcand, int ncand,
+                             float2* tables, double* partial, double* xstary, cudaStream_t s, long long* launches)
+{
+  float2* ex = tables;
+  float2* ey = tables + (size_t)ncand * nx;
+  k_phase_tables<<<std::min(256, (ncand * (nx + ny) + 255) / 256), 256, 0, s>>>(kcand, ncand, nx, ny, dxy, ex, ey);
+  const int nb = 256;
+  for (int c0 = 0; c0 < ncand; c0 += kCand) {
+    int nc = std::min(kCand, ncand - c0);
+    k_modamp_partial<<<nb, 256, 0, s>>>(pmap, nx, ny, ex, ey, c0, nc, partial, ncand);
+    if (launches) *launches += 1;
+  }
+  k_modamp_final<<<ncand, 256, 0, s>>>(partial, nb, ncand, xstary);
+  if (launches) *launches += 2;
+  return (int)cudaGetLastError();
+}
+
+}  // namespace simrecon

@@ -1,0 +1,242 @@
+// Ingest stage: raw camera planes -> separated, z-transformed bands.
+//
+//   k_ingest_x   flat-field, edge apodization and the x half of the 2D R2C
+//                FFT (two real rows packed in one complex line), per plane.
+//   k_fft_cols   forward FFT along y of the half spectra (in place).
+//   k_rescale    bleach-correction ratios from the plane sums (= DC terms).
+//   k_separate   ratio * plane, band separation (nphases x nphases matrix)
+//                and the forward FFT along z, in place, per (ky, kx tile).
+//
+// Reference stages replaced: load_and_flatfield (cudaSirecon.cpp:1715-1731),
+// rescale (gpuFunctionsImpl.cu:110-195), apodize (gpuFunctionsImpl.cu:39-82),
+// transformXYSlice (cudaSirecon.cpp:542-579), separate
+// (gpuFunctionsImpl.cu:214-291) and the z FFT (cudaSirecon.cpp:238-257).
+#include <algorithm>
+
+#include "kernels.h"
+
+namespace simrecon {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kMaxElems = kFftEPT * kThreads;  // complex elements per CTA
+
+__device__ __forceinline__ int raw_section(int d, int p, int z, int nz, int ndirs, int nph, int fastSI)
+{
+  // loadImageData section order, cudaSirecon.cpp:1374-1382
+  return fastSI ? (z * ndirs * nph + d * nph + p) : (d * nz * nph + z * nph + p);
+}
+
+template <typename T>
+__device__ __forceinline__ float flat(const T* __restrict__ plane, const IngestArgs& a, int y, int x)
+{
+  float v = (float)plane[(size_t)y * a.nx + x];
+  float bg = a.bg ? __ldg(a.bg + (size_t)y * a.nx + x) : a.bgconst;
+  float sl = a.slope ? __ldg(a.slope + (size_t)y * a.nx + x) : 1.0f;
+  return (v - bg - a.bgextra) * sl * a.inscale;
+}
+
+// One CTA: `nl` complex lines = 2*nl rows [y0, y0 + 2 nl) of plane `pl`.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_ingest_x(IngestArgs a, FFTPlan plan, int nl)
+{
+  extern __shared__ float2 sm[];
+  __shared__ float diffr[2 * 256];
+  const int nx = a.nx, ny = a.ny, nxh = nx / 2 + 1;
+  const int pl = blockIdx.y;  // plane id = (d*nph + p)*nz + z
+  const int z = pl % a.nz;
+  const int dp = pl / a.nz;
+  const int p = dp % a.nphases, d = dp / a.nphases;
+  const int y0 = blockIdx.x * 2 * nl;
+  const T* plane = (const T*)a.raw + (size_t)raw_section(d, p, z, a.nz, a.ndirs, a.nphases, a.fastSI) * nx * ny;
+  float* smr = (float*)sm;  // real view: row r at x -> smr[2*((r>>1)*nx + x) + (r&1)]
+  const int napo = a.napodize;
+  const int nrows = 2 * nl;
+  // 1) flat-field + top/bottom edge blend (apodize_x_kernel)
+  for (int t = threadIdx.x; t < nrows * nx; t += blockDim.x) {
+    int r = t / nx, x = t - r * nx;
+    int y = y0 + r;
+    float v = 0.f;
+    if (y < ny) {
+      v = flat(plane, a, y, x);
+      bool top = y < napo, bot = (ny - 1 - y) < napo;
+      if (top || bot) {
+        float diff = (flat(plane, a, ny - 1, x) - flat(plane, a, 0, x)) / 2.0f;
+        if (top) v += diff * a.apofact[y];
+        if (bot) v -= diff * a.apofact[ny - 1 - y];
+      }
+    }
+    smr[2 * ((r >> 1) * nx + x) + (r & 1)] = v;
+  }
+  __syncthreads();
+  // 2) left/right edge blend (apodize_y_kernel) using the blended row ends
+  if (napo > 0) {
+    for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
+      float e0 = smr[2 * ((r >> 1) * nx + 0) + (r & 1)];
+      float e1 = smr[2 * ((r >> 1) * nx + nx - 1) + (r & 1)];
+      diffr[r] = (e1 - e0) / 2.0f;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < nrows * 2 * napo; t += blockDim.x) {
+      int r = t / (2 * napo), q = t - r * 2 * napo;
+      if (y0 + r >= ny) continue;
+      int x = q < napo ? q : nx - 1 - (q - napo);
+      int l = q < napo ? q : q - napo;
+      float f = diffr[r] * a.apofact[l];
+      float* e = &smr[2 * ((r >> 1) * nx + x) + (r & 1)];
+      if (q < napo) *e += f;
+      else *e -= f;
+    }
+  }
+  __syncthreads();
+  // 3) forward FFT along x of the packed lines
+  fft_lines<-1>(sm, plan, nl, nx, 1);
+  // 4) split the two real transforms, keep kx in [0, nx/2]
+  for (int t = threadIdx.x; t < nl * nxh; t += blockDim.x) {
+    int l = t / nxh, k = t - l * nxh;
+    float2 zk = sm[l * nx + k];
+    float2 zn = sm[l * nx + (nx - k) % nx];
+    float2 A = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+    float2 B = make_float2(0.5f * (zk.y + zn.y), -0.5f * (zk.x - zn.x));
+    int y = y0 + 2 * l;
+    float2* dst = a.spec + (size_t)pl * ny * nxh;
+    if (y < ny) dst[(size_t)y * nxh + k] = A;
+    if (y + 1 < ny) dst[(size_t)(y + 1) * nxh + k] = B;
+  }
+}
+
+// Forward/inverse FFT along the middle axis of [nplanes][n][ncol], in place.
+template <int DIR>
+__global__ void __launch_bounds__(kThreads) k_fft_cols(float2* data, int n, int ncol, FFTPlan plan, int W)
+{
+  extern __shared__ float2 sm[];
+  const int c0 = blockIdx.x * W;
+  float2* base = data + (size_t)blockIdx.y * n * ncol;
+  for (int t = threadIdx.x; t < n * W; t += blockDim.x) {
+    int i = t / W, w = t - i * W;
+    sm[t] = (c0 + w < ncol) ? base[(size_t)i * ncol + c0 + w] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  fft_lines<DIR>(sm, plan, W, 1, W);
+  for (int t = threadIdx.x; t < n * W; t += blockDim.x) {
+    int i = t / W, w = t - i * W;
+    if (c0 + w < ncol) base[(size_t)i * ncol + c0 + w] = sm[t];
+  }
+}
+
+// Bleach correction (rescale, gpuFunctionsImpl.cu:110-157): per (d, z) the
+// nphases plane sums, ref = dir-0 phase-0 sum at z (or at z = 0 with
+// equalizez; from time 0 with equalizet), ratio = ref / sum.
+__global__ void k_rescale(const float2* __restrict__ spec, int ny, int nxh, int nz, int ndirs, int nph, int t,
+                          int equalizez, int equalizet, double* sdp0, float* scale)
+{
+  const size_t plane = (size_t)ny * nxh;
+  for (int z = threadIdx.x; z < nz; z += blockDim.x)
+    if (!(equalizet && t != 0)) sdp0[z] = (double)spec[(size_t)z * plane].x;  // d = 0, p = 0
+  __syncthreads();
+  for (int i = threadIdx.x; i < ndirs * nph * nz; i += blockDim.x) {
+    int z = i % nz;
+    float sum = spec[(size_t)i * plane].x;
+    float ref = (float)(equalizez ? sdp0[0] : sdp0[z]);
+    scale[i] = ref / sum;
+  }
+}
+
+// Separation + forward z FFT.  One CTA = (ky, W columns of kx) of one
+// direction; shared tile [z][band][w].
+__global__ void __launch_bounds__(kThreads) k_separate(float2* spec, const float* __restrict__ scale,
+                                                       const float* __restrict__ sepmat, int ny, int nxh, int nz,
+                                                       int nph, FFTPlan plan, int W)
+{
+  extern __shared__ float2 sm[];
+  __shared__ float M[kMaxPhases * kMaxPhases];
+  const int ky = blockIdx.y, c0 = blockIdx.x * W, d = blockIdx.z;
+  for (int i = threadIdx.x; i < nph * nph; i += blockDim.x) M[i] = sepmat[i];
+  __syncthreads();
+  const size_t plane = (size_t)ny * nxh;
+  float2* dbase = spec + (size_t)d * nph * nz * plane + (size_t)ky * nxh + c0;
+  const float* dscale = scale + d * nph * nz;
+  const int ld = nph * W;
+  for (int t = threadIdx.x; t < nz * W; t += blockDim.x) {
+    int z = t / W, w = t - z * W;
+    float2 in[kMaxPhases];
+    bool ok = c0 + w < nxh;
+    for (int p = 0; p < nph; ++p) {
+      float s = dscale[p * nz + z];
+      float2 v = ok ? dbase[((size_t)p * nz + z) * plane + w] : make_float2(0.f, 0.f);
+      in[p] = make_float2(v.x * s, v.y * s);
+    }
+    for (int b = 0; b < nph; ++b) {
+      float2 acc = make_float2(0.f, 0.f);
+      for (int p = 0; p < nph; ++p) {
+        float m = M[b * nph + p];
+        acc.x += m * in[p].x;
+        acc.y += m * in[p].y;
+      }
+      sm[z * ld + b * W + w] = acc;
+    }
+  }
+  __syncthreads();
+  if (nz > 1) fft_lines<-1>(sm, plan, nph * W, 1, ld);
+  for (int t = threadIdx.x; t < nz * nph * W; t += blockDim.x) {
+    int z = t / ld, r = t - z * ld;
+    int b = r / W, w = r - b * W;
+    if (c0 + w < nxh) dbase[((size_t)b * nz + z) * plane + w] = sm[t];
+  }
+}
+
+}  // namespace
+
+int launch_ingest(const IngestArgs& a, cudaStream_t s, long long* launches)
+{
+  FFTPlan px, py;
+  if (!get_fft_plan(a.nx, &px) || !get_fft_plan(a.ny, &py)) return -1;
+  const int nxh = a.nx / 2 + 1;
+  const int nplanes = a.ndirs * a.nphases * a.nz;
+  int nl = std::max(1, std::min(kMaxElems / a.nx, 256));
+  nl = std::min(nl, (a.ny + 1) / 2);
+  size_t smx = (size_t)nl * a.nx * sizeof(float2);
+  dim3 gx((a.ny + 2 * nl - 1) / (2 * nl), nplanes);
+  if (a.raw_is_u16) {
+    cudaFuncSetAttribute(k_ingest_x<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+    k_ingest_x<uint16_t><<<gx, kThreads, smx, s>>>(a, px, nl);
+  } else {
+    cudaFuncSetAttribute(k_ingest_x<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+    k_ingest_x<float><<<gx, kThreads, smx, s>>>(a, px, nl);
+  }
+  int W = std::max(1, std::min(32, kMaxElems / a.ny));
+  size_t smy = (size_t)W * a.ny * sizeof(float2);
+  dim3 gy((nxh + W - 1) / W, nplanes);
+  cudaFuncSetAttribute(k_fft_cols<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
+  k_fft_cols<-1><<<gy, kThreads, smy, s>>>(a.spec, a.ny, nxh, py, W);
+  if (launches) *launches += 2;
+  return (int)cudaGetLastError();
+}
+
+int launch_rescale(const float2* spec, int nx, int ny, int nz, int ndirs, int nphases, int t, int equalizez,
+                   int equalizet, double* sdp0, float* scale, cudaStream_t s, long long* launches)
+{
+  k_rescale<<<1, 256, 0, s>>>(spec, ny, nx / 2 + 1, nz, ndirs, nphases, t, equalizez, equalizet, sdp0, scale);
+  if (launches) *launches += 1;
+  return (int)cudaGetLastError();
+}
+
+int launch_separate(float2* spec, const float* scale, const float* sepmat, int nx, int ny, int nz, int ndirs,
+                    int nphases, cudaStream_t s, long long* launches)
+{
+  FFTPlan pz;
+  if (!get_fft_plan(nz, &pz)) return -1;
+  if (nphases > kMaxPhases) return -1;
+  const int nxh = nx / 2 + 1;
+  int W = 32;
+  while (W > 1 && nphases * W * nz > kMaxElems) W >>= 1;
+  size_t sm = (size_t)nphases * W * nz * sizeof(float2);
+  dim3 g((nxh + W - 1) / W, ny, ndirs);
+  cudaFuncSetAttribute(k_separate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_separate<<<g, kThreads, sm, s>>>(spec, scale, sepmat, ny, nxh, nz, nphases, pz, W);
+  if (launches) *launches += 1;
+  return (int)cudaGetLastError();
+}
+
+}  // namespace simrecon

@@ -1,0 +1,112 @@
+// Host-side launchers of the reconstruction kernels.  Every launcher takes
+// plain device pointers, sizes and a stream; none allocates.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sim_common.cuh"
+
+namespace simrecon {
+
+// ----------------------------------------------------------------- FFT plans
+// Returns a plan (radix sequence + device twiddles) for length n; cached per
+// (device, n).  n must factor into 2, 3, 5, 7.  Returns false if it cannot.
+bool get_fft_plan(int n, FFTPlan* plan);
+bool fft_length_ok(int n);
+
+// -------------------------------------------------------------------- ingest
+struct IngestArgs {
+  const void* raw;       // [nimg][ny][nx] uint16 or float
+  int raw_is_u16;
+  int nx, ny, nz, ndirs, nphases;
+  int fastSI;
+  const float* bg;       // [ny][nx] or null (then bgconst)
+  const float* slope;    // [ny][nx] or null (then 1)
+  float bgconst;
+  float bgextra;
+  float inscale;
+  int napodize;
+  const float* apofact;  // device [napodize]
+  float2* spec;          // [ndirs*nphases*nz][ny][nx/2+1]
+};
+// flat-field + apodize + 2D R2C FFT of every raw plane into spec
+int launch_ingest(const IngestArgs& a, cudaStream_t s, long long* launches);
+
+// Bleach-correction ratios from the plane sums (DC terms of spec):
+// scale[d][p][z] (float); sdp0 [nz] (double) persists across time points.
+int launch_rescale(const float2* spec, int nx, int ny, int nz, int ndirs, int nphases, int t, int equalizez,
+                   int equalizet, double* sdp0, float* scale, cudaStream_t s, long long* launches);
+
+// Separation (band_i = sum_j M[i][j] * scale[p][z] * spec_j) + forward z FFT,
+// in place, all directions.
+int launch_separate(float2* spec, const float* scale, const float* sepmat /* device [nb][nph] */, int nx, int ny,
+                    int nz, int ndirs, int nphases, cudaStream_t s, long long* launches);
+
+// ----------------------------------------------------------------- fitting
+struct OverlapArgs {
+  const float2* bands;  // bands of one direction: [nph][nz][ny][nxh]
+  int nx, ny, nz;
+  int order1, order2;
+  float kx, ky;         // k0 * (order2 - order1), 1/um
+  float dkx, dky;
+  float rdistcutoff, otfcutoff, order0_2_factor;
+  int zdc;              // planes -zdc..zdc are built
+  int nokz0;
+  OTFView otf;
+  float2* ovl;          // [2][2*zdc+1][ny][nx]   (x-inverse-transformed rows)
+  float2* ppart;        // [ngroups][ny][nx]
+  double* sums;         // [2 * nctas] partial |X|^2, |Y|^2
+  float2* pmap;         // [ny][nx] result: nz * sum_kz conj(X~) Y~
+  double* sumxy;        // [2] result: sum |X|^2, sum |Y|^2 (real-space, like the reference)
+};
+int launch_overlaps(OverlapArgs& a, cudaStream_t s, long long* launches);
+
+// crosscorr = FFT2(conj(pmap)); intensity argmax with the two-neighbour
+// values along x and y (wrap-around) written to peak[0..6]:
+// {ix, iy, a1x, a2, a3x, a1y, a3y}
+int launch_crosscorr_peak(const float2* pmap, float2* cc, int nx, int ny, float* blockval, int* blockidx,
+                          float* peak, cudaStream_t s, long long* launches);
+
+// XStarY[c] = sum_xy pmap(x,y) exp(i 2pi ((x - nx/2) kx_c + (y - ny/2) ky_c) dxy), c < ncand
+int launch_modamp_candidates(const float2* pmap, int nx, int ny, float dxy, const float2* kcand /* device */,
+                             int ncand, float2* tables, double* partial, double* xstary, cudaStream_t s,
+                             long long* launches);
+
+// ---------------------------------------------------------------- assembly
+struct FilterArgs {
+  float2* bands;         // bands of direction dir [nph][nz][ny][nxh]
+  int dir, ndirs, norders, nx, ny, nz;
+  float dkx, dky, rdistcutoff, apocutoff, zapocutoff, wiener2;
+  int zdc[kMaxOrders];
+  float2 k0[kMaxDirs];
+  float ampmag2[kMaxDirs * kMaxOrders];
+  float noisevar[kMaxDirs * kMaxOrders];
+  float2 conjamp[kMaxOrders];
+  int suppress, supp_radius, dampen0, nokz0, filteroverlaps, apodizeoutput, bessel;
+  OTFView otf;
+};
+int launch_filter(const FilterArgs& a, cudaStream_t s, long long* launches);
+
+struct AssembleArgs {
+  const float2* bands;  // all directions [ndirs][nph][nz][ny][nxh]
+  int ndirs, norders, nphases, nx, ny, nz;
+  int X, Y, Z;          // zoomed output grid
+  int zdc[kMaxOrders];  // in-band planes of each order after filtering
+  const float2* ex;     // [ndirs*norders][X] phase-ramp factors along x
+  const float2* ey;     // [ndirs*norders][Y]
+  float2* T;            // scratch: [maxslots][Y][nx]
+  size_t tcap;          // capacity of T in complex elements
+  float2* S;            // [Z][Y][X]
+  float* out;           // [Z][Y][X]
+};
+int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches);
+
+// Phase-ramp tables for assembly: ex[d*no+o][j] = exp(i fact pi (j - X/2) o k0x_d dxyz),
+// ey likewise along y (computed in double precision).
+int launch_ramp_tables(const float2* k0 /* device [ndirs] */, int ndirs, int norders, int X, int Y, float dxyz,
+                       float fact, float2* ex, float2* ey, cudaStream_t s, long long* launches);
+
+// L2 flush helper for timing
+int launch_fill(float* buf, size_t n, float v, cudaStream_t s, long long* launches);
+
+}  // namespace simrecon

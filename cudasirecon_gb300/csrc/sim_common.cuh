@@ -1,0 +1,69 @@
+// Device-side structs and helpers shared by the reconstruction kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fft.cuh"
+
+namespace simrecon {
+
+constexpr int kMaxDirs = 8;
+constexpr int kMaxOrders = 8;
+constexpr int kMaxPhases = 16;
+constexpr int kMaxApo = 64;
+
+// Rotationally averaged OTF tables: order o at otf[o], complex [nxotf][nzotf]
+// (kr-major, kz fastest, kz in FFT order).
+struct OTFView {
+  const float2* otf[kMaxOrders];
+  int nzotf;
+  int nxotf;
+  float dkrotf;
+  float kzscale;
+};
+
+// Bilinear lookup in a rotationally averaged OTF (the interpolation of
+// dev_otfinterpolate, gpuFunctionsImpl.cu:1677-1715).  Indices are clamped
+// to the table so a lookup at the very edge of the support never reads past
+// it (the reference reads one bin beyond there).
+__device__ __forceinline__ float2 otf_lookup(const float2* __restrict__ otf, const OTFView& v, float kx, float ky,
+                                             int kz)
+{
+  float krindex = sqrtf(kx * kx + ky * ky) / v.dkrotf;
+  float kzindex = kz * v.kzscale;
+  if (kzindex < 0) kzindex += v.nzotf;
+  int ir = (int)floorf(krindex);
+  int iz = (int)floorf(kzindex);
+  float ar = krindex - ir;
+  float az = kzindex - iz;
+  int izp = (iz == v.nzotf - 1) ? 0 : iz + 1;
+  int last = v.nxotf * v.nzotf - 1;
+  int i00 = min(max(ir * v.nzotf + iz, 0), last);
+  int i01 = min(max(ir * v.nzotf + izp, 0), last);
+  int i10 = min(max((ir + 1) * v.nzotf + iz, 0), last);
+  int i11 = min(max((ir + 1) * v.nzotf + izp, 0), last);
+  float2 a = __ldg(otf + i00), b = __ldg(otf + i01), c = __ldg(otf + i10), d = __ldg(otf + i11);
+  float2 r;
+  r.x = (1 - ar) * (a.x * (1 - az) + b.x * az) + ar * (c.x * (1 - az) + d.x * az);
+  r.y = (1 - ar) * (a.y * (1 - az) + b.y * az) + ar * (c.y * (1 - az) + d.y * az);
+  return r;
+}
+
+__device__ __forceinline__ float cmag2(float2 a) { return a.x * a.x + a.y * a.y; }
+
+// Block-wide sum of a double (all threads must call).  Result valid in thread 0.
+__device__ __forceinline__ double block_sum_d(double v, double* scratch /* >= 32 */)
+{
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) scratch[wid] = v;
+  __syncthreads();
+  int nw = (blockDim.x + 31) >> 5;
+  v = (threadIdx.x < nw) ? scratch[threadIdx.x] : 0.0;
+  if (wid == 0)
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+}  // namespace simrecon

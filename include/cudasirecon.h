@@ -1,0 +1,214 @@
+/*
+ * cudasirecon_gb300 -- C ABI of libcudasirecon.so (drop-in for the SR_* entry
+ * points of scopetools/cudasirecon, src/cudaSirecon/interface.cpp).
+ *
+ * The twelve SR_* functions keep the reference's names, argument meaning and
+ * call order; each declaration below cites the reference entry point it
+ * replaces.  ReconParams and ImageParams keep the reference's member order
+ * and types (src/cudaSirecon/cudaSireconImpl.h:104-195) because
+ * SR_getReconParams / SR_getImageParams hand out references into the object
+ * and callers read and write those structs in place.
+ *
+ * Additions (no reference counterpart): SR_delete, SR_getLastError,
+ * SR_clearError, SR_setRawU16, the SRX_* performance/introspection calls.
+ *
+ * Errors never cross the ABI as C++ exceptions and the library never calls
+ * exit(): a failing call records a message readable with SR_getLastError()
+ * (thread-local) and, for constructors, returns NULL.
+ *
+ * Threading: one SIM_Reconstructor may be used by one host thread at a time;
+ * distinct handles are independent (each owns its CUDA stream and device
+ * memory) and may be used concurrently from different threads.
+ */
+#ifndef CUDASIRECON_GB300_H
+#define CUDASIRECON_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+#include <string>
+#include <vector>
+
+/* Overall image reconstruction parameters (cudaSireconImpl.h:104-178). */
+struct ReconParams {
+  float k0startangle, linespacing;
+  float na, nimm;
+  int ndirs, nphases, norders_output;
+  int norders;
+  float* phaseSteps;
+  bool bTwolens;
+  bool bFastSIM;
+  bool bBessel;
+  float BesselNA;
+  float BesselLambdaEx;
+  float deskewAngle;
+  int extraShift;
+  bool bNoRecon;
+  unsigned cropXYto;
+  bool bWriteTitle;
+  float otfcutoff;
+  float zoomfact;
+  int z_zoom;
+  int nzPadTo;
+  float explodefact;
+  bool bFilteroverlaps;
+  int recalcarrays;
+  int napodize;
+  int bSearchforvector;
+  int bUseTime0k0;
+  int apodizeoutput;
+  float apoGamma;
+  int bSuppress_singularities;
+  int suppression_radius;
+  bool bDampenOrder0;
+  int bFitallphases;
+  int do_rescale;
+  bool equalizez;
+  bool equalizet;
+  bool bNoKz0;
+  float wiener, wienerInr;
+  std::vector<float> forceamp;
+  std::vector<float> k0angles;
+  int nxotf, nyotf, nzotf;
+  float dzPSF;
+  float dkzotf, dkrotf;
+  bool bRadAvgOTF;
+  bool bOneOTFperAngle;
+  int bFixdrift;
+  float drift_filter_fact;
+  float constbkgd;
+  int bBgInExtHdr;
+  int bUsecorr;
+  std::string corrfiles;
+  float readoutNoiseVar;
+  float electrons_per_bit;
+  int bMakemodel;
+  int bSaveSeparated;
+  std::string fileSeparated;
+  int bSaveAlignedRaw;
+  std::string fileRawAligned;
+  int bSaveOverlaps;
+  std::string fileOverlaps;
+  bool bTIFF;
+  std::string ifiles;
+  std::string ofiles;
+  std::string otffiles;
+};
+
+/* Image geometry (cudaSireconImpl.h:179-195). */
+struct ImageParams {
+  int nx;
+  int nx_raw;
+  int ny;
+  int nz;
+  int nz0;
+  short nwaves;
+  short wave[5];
+  short ntimes;
+  unsigned short curTimeIdx;
+  float dxy;
+  float dz;
+  float dz_raw;
+  float inscale;
+};
+
+class SIM_Reconstructor;
+extern "C" {
+#define SR_PARAMS_REF(T) T&
+#else
+typedef struct SIM_Reconstructor SIM_Reconstructor;
+typedef struct ReconParams ReconParams;
+typedef struct ImageParams ImageParams;
+#define SR_PARAMS_REF(T) T*
+#endif
+
+/* --- the reference's twelve entry points --------------------------------- */
+
+/* interface.cpp:13-17.  nImages = ndirs*nphases*nz raw planes; the config
+ * file uses the reference's key=value option names and must name the OTF
+ * TIFF with otf-file=.  Returns NULL on error (see SR_getLastError). */
+SIM_Reconstructor* SR_new_from_shape(int nx, int ny, int nImages, const char* configFileName);
+
+/* interface.cpp:19-25.  raw_data is [nz][ny][nx] float (nz = total planes),
+ * sections in the reference's order (Angle->Z->Phase, or Z->Angle->Phase
+ * with fastSI). */
+void SR_setRaw(SIM_Reconstructor* sr, const float* raw_data, int nx, int ny, int nz);
+
+/* interface.cpp:26-29: bleach correction of the loaded volume. */
+void SR_loadAndRescaleImage(SIM_Reconstructor* sr, int it, int iw);
+
+/* interface.cpp:30-33 */
+void SR_setCurTimeIdx(SIM_Reconstructor* sr, int it);
+
+/* interface.cpp:34-37: k0 / modamp fit, Wiener filter and band assembly. */
+void SR_processOneVolume(SIM_Reconstructor* sr);
+
+/* interface.cpp:38-41: result is (zoom*nx)*(zoom*ny)*(zzoom*nz) floats. */
+void SR_getResult(SIM_Reconstructor* sr, float* result);
+
+/* interface.cpp:42-45 / 47-50: references into the object. */
+SR_PARAMS_REF(ReconParams) SR_getReconParams(SIM_Reconstructor* sr);
+SR_PARAMS_REF(ImageParams) SR_getImageParams(SIM_Reconstructor* sr);
+
+/* interface.cpp:54-57: construct from a cudasirecon command line
+ * (input output otf [--options] [-c config]). */
+SIM_Reconstructor* SR_new_from_argv(int argc, char** argv);
+
+/* interface.cpp:59-62: read time point it of the input file(s). */
+void SR_setFile(SIM_Reconstructor* sr, int it, int iw);
+
+/* interface.cpp:63-66: write the result of time point it. */
+void SR_writeResult(SIM_Reconstructor* sr, int it, int iw);
+
+/* interface.cpp:67-70 */
+void SR_closeFiles(SIM_Reconstructor* sr);
+
+/* --- additions (no counterpart in the reference) -------------------------- */
+
+/* Destroy a handle and release its device memory (the reference leaks). */
+void SR_delete(SIM_Reconstructor* sr);
+
+/* Last error of the calling thread ("" if none); SR_clearError resets it. */
+const char* SR_getLastError(void);
+void SR_clearError(void);
+
+/* Integer camera readout: raw_data is [nz][ny][nx] uint16.  Same result as
+ * SR_setRaw of the same values converted to float. */
+void SR_setRawU16(SIM_Reconstructor* sr, const uint16_t* raw_data, int nx, int ny, int nz);
+
+/* Number of time points of a file-backed reconstructor (getNTimes). */
+int SR_getNTimes(SIM_Reconstructor* sr);
+
+/* Fitted pattern vectors (1/um, [ndirs][2]) and modulation amplitudes
+ * ([ndirs][norders] complex as float pairs) of the last processed volume. */
+void SRX_getFit(SIM_Reconstructor* sr, float* k0, float* amps);
+
+/* Copy the separated (before processOneVolume's filter) or current bands of
+ * direction dir, band b, as complex [nz][ny][nx/2+1] (float pairs).
+ * Stage 0 = after separation (SRX_prepare), 1 = current device contents. */
+int SRX_prepare(SIM_Reconstructor* sr);
+int SRX_getBand(SIM_Reconstructor* sr, int dir, int b, float* out);
+
+/* Device-resident timing: run the full device pipeline (ingest of the staged
+ * raw planes, bleach correction, fit, filter, assembly) `steps` times from
+ * the raw data already in device memory, flushing L2 between steps, and
+ * return the summed device time in ms (CUDA events on the handle's stream). */
+int SRX_benchDevice(SIM_Reconstructor* sr, int steps, double* total_ms);
+
+/* Per-stage profiling: when enabled, every stage is bracketed by CUDA events
+ * on the handle's stream.  SRX_getProfile writes a JSON object
+ * {"stage": {"ms": t, "launches": n}, ...} accumulated since the last reset. */
+void SRX_setProfiling(SIM_Reconstructor* sr, int on);
+int SRX_getProfile(SIM_Reconstructor* sr, char* json, int maxlen);
+void SRX_resetProfile(SIM_Reconstructor* sr);
+
+/* Number of this library's kernels launched since the handle was created. */
+long long SRX_kernelLaunches(SIM_Reconstructor* sr);
+
+#ifdef __cplusplus
+}
+#endif
+#undef SR_PARAMS_REF
+
+#endif /* CUDASIRECON_GB300_H */
