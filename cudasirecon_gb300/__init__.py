@@ -1,0 +1,259 @@
+"""cudasirecon_gb300: GB300-native 3-beam SIM reconstruction.
+
+The product is ``libcudasirecon.so`` (C++ host code + hand-written sm_103a
+CUDA kernels) exposing the reference's SR_* C ABI (include/cudasirecon.h).
+This module is a thin ctypes mirror of that ABI for Python callers, tests
+and benchmarks.  There is no CPU fallback: if the library is missing or the
+GPU is unavailable, calls fail loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcudasirecon.so")
+CLI_PATH = os.path.join(HERE, "bin", "cudasirecon")
+
+_lib = None
+
+
+class SIReconError(RuntimeError):
+    pass
+
+
+def build(force: bool = False) -> str:
+    from . import buildlib
+    return buildlib.build(force=force)
+
+
+def load_library(path: str | None = None) -> C.CDLL:
+    """Load libcudasirecon.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise SIReconError(f"{path} not found: build it with `python -m cudasirecon_gb300.buildlib`")
+    lib = C.CDLL(path)
+    vp, ip, fp = C.c_void_p, C.c_int, C.POINTER(C.c_float)
+    lib.SR_new_from_shape.restype = vp
+    lib.SR_new_from_shape.argtypes = [ip, ip, ip, C.c_char_p]
+    lib.SR_new_from_argv.restype = vp
+    lib.SR_new_from_argv.argtypes = [ip, C.POINTER(C.c_char_p)]
+    lib.SR_setRaw.argtypes = [vp, fp, ip, ip, ip]
+    lib.SR_setRawU16.argtypes = [vp, C.POINTER(C.c_uint16), ip, ip, ip]
+    for n in ("SR_loadAndRescaleImage", "SR_setFile", "SR_writeResult"):
+        getattr(lib, n).argtypes = [vp, ip, ip]
+    lib.SR_setCurTimeIdx.argtypes = [vp, ip]
+    for n in ("SR_processOneVolume", "SR_closeFiles", "SR_delete"):
+        getattr(lib, n).argtypes = [vp]
+    lib.SR_getResult.argtypes = [vp, fp]
+    lib.SR_getReconParams.restype = vp
+    lib.SR_getReconParams.argtypes = [vp]
+    lib.SR_getImageParams.restype = vp
+    lib.SR_getImageParams.argtypes = [vp]
+    lib.SR_getLastError.restype = C.c_char_p
+    lib.SR_getLastError.argtypes = []
+    lib.SR_clearError.argtypes = []
+    lib.SR_getNTimes.restype = ip
+    lib.SR_getNTimes.argtypes = [vp]
+    lib.SRX_getFit.argtypes = [vp, fp, fp]
+    lib.SRX_prepare.restype = ip
+    lib.SRX_prepare.argtypes = [vp]
+    lib.SRX_getBand.restype = ip
+    lib.SRX_getBand.argtypes = [vp, ip, ip, fp]
+    lib.SRX_benchDevice.restype = ip
+    lib.SRX_benchDevice.argtypes = [vp, ip, C.POINTER(C.c_double)]
+    lib.SRX_setProfiling.argtypes = [vp, ip]
+    lib.SRX_getProfile.restype = ip
+    lib.SRX_getProfile.argtypes = [vp, C.c_char_p, ip]
+    lib.SRX_resetProfile.argtypes = [vp]
+    lib.SRX_kernelLaunches.restype = C.c_longlong
+    lib.SRX_kernelLaunches.argtypes = [vp]
+    _lib = lib
+    return lib
+
+
+class ImageParams(C.Structure):
+    """ctypes view of ImageParams (cudaSireconImpl.h:179-195 layout)."""
+    _fields_ = [("nx", C.c_int), ("nx_raw", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("nz0", C.c_int),
+                ("nwaves", C.c_short), ("wave", C.c_short * 5), ("ntimes", C.c_short),
+                ("curTimeIdx", C.c_ushort), ("dxy", C.c_float), ("dz", C.c_float), ("dz_raw", C.c_float),
+                ("inscale", C.c_float)]
+
+
+class ReconParamsHead(C.Structure):
+    """ctypes view of the leading plain members of ReconParams (up to wienerInr)."""
+    _fields_ = [("k0startangle", C.c_float), ("linespacing", C.c_float), ("na", C.c_float), ("nimm", C.c_float),
+                ("ndirs", C.c_int), ("nphases", C.c_int), ("norders_output", C.c_int), ("norders", C.c_int),
+                ("phaseSteps", C.c_void_p), ("bTwolens", C.c_bool), ("bFastSIM", C.c_bool), ("bBessel", C.c_bool),
+                ("BesselNA", C.c_float), ("BesselLambdaEx", C.c_float), ("deskewAngle", C.c_float),
+                ("extraShift", C.c_int), ("bNoRecon", C.c_bool), ("cropXYto", C.c_uint), ("bWriteTitle", C.c_bool),
+                ("otfcutoff", C.c_float), ("zoomfact", C.c_float), ("z_zoom", C.c_int), ("nzPadTo", C.c_int),
+                ("explodefact", C.c_float), ("bFilteroverlaps", C.c_bool), ("recalcarrays", C.c_int),
+                ("napodize", C.c_int), ("bSearchforvector", C.c_int), ("bUseTime0k0", C.c_int),
+                ("apodizeoutput", C.c_int), ("apoGamma", C.c_float), ("bSuppress_singularities", C.c_int),
+                ("suppression_radius", C.c_int), ("bDampenOrder0", C.c_bool), ("bFitallphases", C.c_int),
+                ("do_rescale", C.c_int), ("equalizez", C.c_bool), ("equalizet", C.c_bool), ("bNoKz0", C.c_bool),
+                ("wiener", C.c_float), ("wienerInr", C.c_float)]
+
+
+def write_tiff_float(path: str, pages: np.ndarray) -> None:
+    """Write a float32 stack [depth][height][width] as an uncompressed multi-page TIFF."""
+    pages = np.ascontiguousarray(pages, np.float32)
+    if pages.ndim == 2:
+        pages = pages[None]
+    d, h, w = pages.shape
+    import struct
+    out = bytearray(b"II*\x00" + struct.pack("<I", 8))
+    for p in range(d):
+        ntags = 10
+        data_off = len(out) + 2 + 12 * ntags + 4
+        nbytes = w * h * 4
+        nxt = data_off + nbytes if p + 1 < d else 0
+        ent = b"".join([
+            struct.pack("<HHII", 256, 4, 1, w), struct.pack("<HHII", 257, 4, 1, h),
+            struct.pack("<HHIHH", 258, 3, 1, 32, 0), struct.pack("<HHIHH", 259, 3, 1, 1, 0),
+            struct.pack("<HHIHH", 262, 3, 1, 1, 0), struct.pack("<HHII", 273, 4, 1, data_off),
+            struct.pack("<HHIHH", 277, 3, 1, 1, 0), struct.pack("<HHII", 278, 4, 1, h),
+            struct.pack("<HHII", 279, 4, 1, nbytes), struct.pack("<HHIHH", 339, 3, 1, 3, 0)])
+        out += struct.pack("<H", ntags) + ent + struct.pack("<I", nxt)
+        out += pages[p].tobytes()
+    with open(path, "wb") as f:
+        f.write(out)
+
+
+def _err(lib) -> str:
+    return (lib.SR_getLastError() or b"").decode(errors="replace")
+
+
+class Reconstructor:
+    """One SIM_Reconstructor through the C ABI (SR_new_from_shape path).
+
+    ``config`` is the reference's key=value config text (or a path); the OTF
+    is given as TIFF pages (written to a temporary file and named with
+    ``otf-file=``) or as an existing ``otf_path``.
+    """
+
+    def __init__(self, nx: int, ny: int, nimages: int, config: str, otf_pages: np.ndarray | None = None,
+                 otf_path: str | None = None):
+        self.lib = load_library()
+        self._tmp = tempfile.TemporaryDirectory(prefix="sirecon_")
+        if otf_path is None:
+            otf_path = os.path.join(self._tmp.name, "otf.tif")
+            write_tiff_float(otf_path, otf_pages)
+        text = config if "=" in config else open(config).read()
+        cfg = os.path.join(self._tmp.name, "config.txt")
+        with open(cfg, "w") as f:
+            f.write(text.rstrip("\n") + f"\notf-file={otf_path}\n")
+        self.lib.SR_clearError()
+        self.h = self.lib.SR_new_from_shape(nx, ny, nimages, cfg.encode())
+        if not self.h:
+            raise SIReconError(_err(self.lib))
+        self.nx, self.ny, self.nimages = nx, ny, nimages
+        ip = self.image_params()
+        rp = self.recon_params()
+        self.nz = ip.nz
+        self.ndirs = rp.ndirs
+        self.nphases = rp.nphases
+        self.norders = rp.norders
+        self.out_shape = (rp.z_zoom * ip.nz0, int(round(rp.zoomfact * ny)), int(round(rp.zoomfact * nx)))
+
+    def _check(self):
+        e = _err(self.lib)
+        if e:
+            self.lib.SR_clearError()
+            raise SIReconError(e)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.SR_delete(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def image_params(self) -> ImageParams:
+        return ImageParams.from_address(self.lib.SR_getImageParams(self.h))
+
+    def recon_params(self) -> ReconParamsHead:
+        return ReconParamsHead.from_address(self.lib.SR_getReconParams(self.h))
+
+    def set_raw(self, raw: np.ndarray):
+        raw = np.ascontiguousarray(raw)
+        if raw.dtype == np.uint16:
+            self.lib.SR_setRawU16(self.h, raw.ctypes.data_as(C.POINTER(C.c_uint16)), self.nx, self.ny,
+                                  raw.shape[0])
+        else:
+            raw = np.ascontiguousarray(raw, np.float32)
+            self.lib.SR_setRaw(self.h, raw.ctypes.data_as(C.POINTER(C.c_float)), self.nx, self.ny, raw.shape[0])
+        self._check()
+
+    def load_and_rescale(self, it: int = 0, iw: int = 0):
+        self.lib.SR_loadAndRescaleImage(self.h, it, iw)
+        self._check()
+
+    def set_cur_time(self, it: int):
+        self.lib.SR_setCurTimeIdx(self.h, it)
+        self._check()
+
+    def process(self):
+        self.lib.SR_processOneVolume(self.h)
+        self._check()
+
+    def result(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self.out_shape, np.float32)
+        self.lib.SR_getResult(self.h, out.ctypes.data_as(C.POINTER(C.c_float)))
+        self._check()
+        return out
+
+    def fit(self):
+        k0 = np.zeros((self.ndirs, 2), np.float32)
+        amp = np.zeros((self.ndirs, self.norders, 2), np.float32)
+        self.lib.SRX_getFit(self.h, k0.ctypes.data_as(C.POINTER(C.c_float)),
+                            amp.ctypes.data_as(C.POINTER(C.c_float)))
+        return k0, amp[..., 0] + 1j * amp[..., 1]
+
+    def prepare(self):
+        self.lib.SRX_prepare(self.h)
+        self._check()
+
+    def band(self, d: int, b: int) -> np.ndarray:
+        nxh = self.nx // 2 + 1
+        out = np.empty((self.nz, self.ny, nxh * 2), np.float32)
+        self.lib.SRX_getBand(self.h, d, b, out.ctypes.data_as(C.POINTER(C.c_float)))
+        self._check()
+        return out[..., 0::2] + 1j * out[..., 1::2]
+
+    def set_ntimes(self, n: int):
+        self.image_params().ntimes = n
+
+    def bench_device(self, steps: int) -> float:
+        t = C.c_double(0)
+        rc = self.lib.SRX_benchDevice(self.h, steps, C.byref(t))
+        if rc != 0:
+            self._check()
+        return t.value
+
+    def set_profiling(self, on: bool = True):
+        self.lib.SRX_setProfiling(self.h, int(on))
+
+    def profile(self) -> dict:
+        import json
+        buf = C.create_string_buffer(1 << 16)
+        self.lib.SRX_getProfile(self.h, buf, len(buf))
+        return json.loads(buf.value.decode() or "{}")
+
+    def reset_profile(self):
+        self.lib.SRX_resetProfile(self.h)
+
+    def kernel_launches(self) -> int:
+        return int(self.lib.SRX_kernelLaunches(self.h))

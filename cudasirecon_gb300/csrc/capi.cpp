@@ -1,0 +1,192 @@
+// extern "C" SR_* entry points (src/cudaSirecon/interface.cpp:10-71 of the
+// reference) plus the additions declared in include/cudasirecon.h.  No C++
+// exception crosses this boundary and nothing here calls exit(): failures are
+// recorded as a thread-local message for SR_getLastError.
+#include <cstring>
+#include <stdexcept>
+#include <string>
+
+#include "cudasirecon.h"
+#include "reconstructor.h"
+
+namespace {
+thread_local std::string g_last_error;
+
+template <typename F>
+bool guarded(F&& f)
+{
+  try {
+    f();
+    return true;
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+  } catch (...) {
+    g_last_error = "unknown error";
+  }
+  return false;
+}
+
+bool need(SIM_Reconstructor* sr)
+{
+  if (!sr) {
+    g_last_error = "null SIM_Reconstructor handle";
+    return false;
+  }
+  return true;
+}
+
+ReconParams g_dummy_params;
+ImageParams g_dummy_image;
+}  // namespace
+
+extern "C" {
+
+SIM_Reconstructor* SR_new_from_shape(int nx, int ny, int nImages, const char* configFileName)
+{
+  SIM_Reconstructor* r = nullptr;
+  guarded([&] {
+    std::string err;
+    r = SIM_Reconstructor::from_shape(nx, ny, nImages, configFileName ? configFileName : "", &err);
+    if (!r) g_last_error = err;
+  });
+  return r;
+}
+
+void SR_setRaw(SIM_Reconstructor* sr, const float* raw_data, int nx, int ny, int nz)
+{
+  if (need(sr)) guarded([&] { sr->set_raw_float(raw_data, nx, ny, nz); });
+}
+
+void SR_setRawU16(SIM_Reconstructor* sr, const uint16_t* raw_data, int nx, int ny, int nz)
+{
+  if (need(sr)) guarded([&] { sr->set_raw_u16(raw_data, nx, ny, nz); });
+}
+
+void SR_loadAndRescaleImage(SIM_Reconstructor* sr, int it, int iw)
+{
+  if (need(sr)) guarded([&] { sr->load_and_rescale(it, iw); });
+}
+
+void SR_setCurTimeIdx(SIM_Reconstructor* sr, int it)
+{
+  if (need(sr)) guarded([&] { sr->set_cur_time(it); });
+}
+
+void SR_processOneVolume(SIM_Reconstructor* sr)
+{
+  if (need(sr)) guarded([&] { sr->process_one_volume(); });
+}
+
+void SR_getResult(SIM_Reconstructor* sr, float* result)
+{
+  if (need(sr)) guarded([&] { sr->get_result(result); });
+}
+
+ReconParams& SR_getReconParams(SIM_Reconstructor* sr)
+{
+  if (!need(sr)) return g_dummy_params;
+  return sr->opt.p;
+}
+
+ImageParams& SR_getImageParams(SIM_Reconstructor* sr)
+{
+  if (!need(sr)) return g_dummy_image;
+  return sr->opt.ip;
+}
+
+SIM_Reconstructor* SR_new_from_argv(int argc, char** argv)
+{
+  SIM_Reconstructor* r = nullptr;
+  guarded([&] {
+    std::string err;
+    r = SIM_Reconstructor::from_argv(argc, argv, &err);
+    if (!r) g_last_error = err;
+  });
+  return r;
+}
+
+void SR_setFile(SIM_Reconstructor* sr, int it, int iw)
+{
+  if (need(sr)) guarded([&] { sr->set_file(it, iw); });
+}
+
+void SR_writeResult(SIM_Reconstructor* sr, int it, int iw)
+{
+  if (need(sr)) guarded([&] { sr->write_result(it, iw); });
+}
+
+void SR_closeFiles(SIM_Reconstructor* sr)
+{
+  if (need(sr)) guarded([&] { sr->close_files(); });
+}
+
+void SR_delete(SIM_Reconstructor* sr)
+{
+  guarded([&] { delete sr; });
+}
+
+const char* SR_getLastError(void) { return g_last_error.c_str(); }
+
+void SR_clearError(void) { g_last_error.clear(); }
+
+int SR_getNTimes(SIM_Reconstructor* sr) { return need(sr) ? sr->ntimes() : 0; }
+
+void SRX_getFit(SIM_Reconstructor* sr, float* k0, float* amps)
+{
+  if (need(sr)) guarded([&] { sr->get_fit(k0, amps); });
+}
+
+int SRX_prepare(SIM_Reconstructor* sr)
+{
+  int rc = -1;
+  if (need(sr)) guarded([&] { rc = sr->prepare(); });
+  return rc;
+}
+
+int SRX_getBand(SIM_Reconstructor* sr, int dir, int b, float* out)
+{
+  int rc = -1;
+  if (need(sr)) guarded([&] { rc = sr->get_band(dir, b, out); });
+  return rc;
+}
+
+int SRX_benchDevice(SIM_Reconstructor* sr, int steps, double* total_ms)
+{
+  int rc = -1;
+  if (need(sr))
+    guarded([&] {
+      double t = sr->bench_device(steps);
+      if (total_ms) *total_ms = t;
+      rc = 0;
+    });
+  return rc;
+}
+
+void SRX_setProfiling(SIM_Reconstructor* sr, int on)
+{
+  if (need(sr)) sr->set_profiling(on != 0);
+}
+
+int SRX_getProfile(SIM_Reconstructor* sr, char* json, int maxlen)
+{
+  int rc = -1;
+  if (need(sr))
+    guarded([&] {
+      std::string s = sr->profile_json();
+      if (json && maxlen > 0) {
+        strncpy(json, s.c_str(), maxlen - 1);
+        json[maxlen - 1] = '\0';
+      }
+      rc = (int)s.size();
+    });
+  return rc;
+}
+
+void SRX_resetProfile(SIM_Reconstructor* sr)
+{
+  if (need(sr)) guarded([&] { sr->reset_profile(); });
+}
+
+long long SRX_kernelLaunches(SIM_Reconstructor* sr) { return need(sr) ? sr->launches() : -1; }
+
+}  // extern "C"

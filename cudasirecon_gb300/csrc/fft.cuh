@@ -7,8 +7,7 @@
 //     strided axis staged as an [n][W] tile (y / z transforms), so that the
 //     global loads and stores of a tile are 8*W-byte coalesced segments.
 // The transform is an autosorting Stockham sequence of radix-2/3/4/5/7/8
-// stages, each stage reading all of its inputs into registers before a
-// barrier and writing them back in place.  Twiddles come from a per-length
+// stages ping-ponging between two shared buffers of the same layout.  Twiddles come from a per-length
 // table tw[k] = exp(-2 pi i k / n) computed in double precision on the host.
 //
 // Kernels built on this engine supply a Loader that fills the shared lines
@@ -30,6 +29,8 @@ struct FFTPlan {
   int radix[kMaxStages];
   const float2* tw;  // device table of n twiddles exp(-2 pi i k/n)
 };
+
+#ifdef __CUDACC__
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
@@ -174,82 +175,78 @@ __device__ __forceinline__ void dftR(float2* v)
   else if (R == 8) dft8<DIR>(v);
 }
 
-// Elements per thread the engine supports: callers size their CTAs so that
-// n * nl <= kFftEPT * blockDim.x (every butterfly of a stage is then held in
-// registers before the stage's barrier, which makes the in-place update safe).
-constexpr int kFftEPT = 32;
-
-// One Stockham stage of radix R over nl lines.
+// One Stockham stage of radix R over nl lines, reading `src` and writing
+// `dst` (ping-pong shared buffers of identical layout), then a barrier.
 template <int R, int DIR>
-__device__ __forceinline__ void stockham_stage(float2* sm, int n, int nl, int ldl, int ldi, int Ns,
-                                               const float2* __restrict__ tw)
+__device__ __forceinline__ void stockham_stage(const float2* __restrict__ src, float2* __restrict__ dst, int n,
+                                               int nl, int ldl, int ldi, int Ns, const float2* __restrict__ tw)
 {
-  constexpr int Q = (kFftEPT + R - 1) / R;  // butterflies per thread
-  const int m = n / R;                      // butterflies per line
+  const int m = n / R;  // butterflies per line
   const int total = m * nl;
   const int twstep = n / (Ns * R);
   const bool rows = (ldi == 1);
-  float2 v[Q][R];
-  int dst[Q];
-#pragma unroll
-  for (int q = 0; q < Q; ++q) {
-    int t = q * blockDim.x + threadIdx.x;
-    dst[q] = -1;
-    if (t < total) {
-      int l, j;
-      if (rows) {
-        l = t / m;
-        j = t - l * m;
-      } else {
-        j = t / nl;
-        l = t - j * nl;
-      }
-      const float2* src = sm + l * ldl;
-#pragma unroll
-      for (int r = 0; r < R; ++r) v[q][r] = src[(j + r * m) * ldi];
-      int k = j % Ns;
-      if (Ns > 1) {
-#pragma unroll
-        for (int r = 1; r < R; ++r) {
-          float2 w = __ldg(tw + r * k * twstep);
-          if (DIR > 0) w.y = -w.y;
-          v[q][r] = cmul(v[q][r], w);
-        }
-      }
-      dftR<R, DIR>(v[q]);
-      dst[q] = l * ldl + ((j / Ns) * Ns * R + k) * ldi;
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    int l, j;
+    if (rows) {
+      l = t / m;
+      j = t - l * m;
+    } else {
+      j = t / nl;
+      l = t - j * nl;
     }
-  }
-  __syncthreads();
+    float2 v[R];
+    const float2* s = src + l * ldl;
 #pragma unroll
-  for (int q = 0; q < Q; ++q) {
-    if (dst[q] >= 0) {
+    for (int r = 0; r < R; ++r) v[r] = s[(j + r * m) * ldi];
+    const int k = j % Ns;
+    if (Ns > 1) {
 #pragma unroll
-      for (int r = 0; r < R; ++r) sm[dst[q] + r * Ns * ldi] = v[q][r];
+      for (int r = 1; r < R; ++r) {
+        float2 w = __ldg(tw + r * k * twstep);
+        if (DIR > 0) w.y = -w.y;
+        v[r] = cmul(v[r], w);
+      }
     }
+    dftR<R, DIR>(v);
+    float2* d = dst + l * ldl + ((j / Ns) * Ns * R + k) * ldi;
+#pragma unroll
+    for (int r = 0; r < R; ++r) d[r * Ns * ldi] = v[r];
   }
   __syncthreads();
 }
 
-// In-place transform of nl lines held in shared memory.  Requires the whole
-// CTA; callers must __syncthreads() after filling the lines.  The transform
-// is unnormalised (DIR = -1 forward e^{-i}, +1 inverse e^{+i}).
+// Transform of nl lines held in shared buffer `a` (same layout scratch in
+// `b`).  Requires the whole CTA and a barrier after the lines were filled.
+// Returns the buffer that holds the result (a or b).  Unnormalised:
+// DIR = -1 forward e^{-i}, +1 inverse e^{+i}.
 template <int DIR>
-__device__ void fft_lines(float2* sm, const FFTPlan& p, int nl, int ldl, int ldi)
+__device__ float2* fft_lines(float2* a, float2* b, const FFTPlan& p, int nl, int ldl, int ldi)
 {
   int Ns = 1;
+  float2* src = a;
+  float2* dst = b;
   for (int s = 0; s < p.nstages; ++s) {
     int R = p.radix[s];
     switch (R) {
-      case 2: stockham_stage<2, DIR>(sm, p.n, nl, ldl, ldi, Ns, p.tw); break;
-      case 3: stockham_stage<3, DIR>(sm, p.n, nl, ldl, ldi, Ns, p.tw); break;
-      case 4: stockham_stage<4, DIR>(sm, p.n, nl, ldl, ldi, Ns, p.tw); break;
-      case 5: stockham_stage<5, DIR>(sm, p.n, nl, ldl, ldi, Ns, p.tw); break;
-      case 7: stockham_stage<7, DIR>(sm, p.n, nl, ldl, ldi, Ns, p.tw); break;
-      default: stockham_stage<8, DIR>(sm, p.n, nl, ldl, ldi, Ns, p.tw); break;
+      case 2: stockham_stage<2, DIR>(src, dst, p.n, nl, ldl, ldi, Ns, p.tw); break;
+      case 3: stockham_stage<3, DIR>(src, dst, p.n, nl, ldl, ldi, Ns, p.tw); break;
+      case 4: stockham_stage<4, DIR>(src, dst, p.n, nl, ldl, ldi, Ns, p.tw); break;
+      case 5: stockham_stage<5, DIR>(src, dst, p.n, nl, ldl, ldi, Ns, p.tw); break;
+      case 7: stockham_stage<7, DIR>(src, dst, p.n, nl, ldl, ldi, Ns, p.tw); break;
+      default: stockham_stage<8, DIR>(src, dst, p.n, nl, ldl, ldi, Ns, p.tw); break;
     }
     Ns *= R;
+    float2* t = src;
+    src = dst;
+    dst = t;
   }
+  return src;
 }
+
+// Complex elements a CTA of kFftThreads threads stages per transform.
+constexpr int kFftThreads = 256;
+constexpr int kFftElems = 4096;
+
+#endif  // __CUDACC__
 
 }  // namespace simrecon

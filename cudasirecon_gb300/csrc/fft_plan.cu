@@ -48,6 +48,12 @@ bool factor(int n, std::vector<int>& radix)
 }
 }  // namespace
 
+namespace {
+thread_local KernelTimer* t_timer = nullptr;
+}
+void set_kernel_timer(KernelTimer* t) { t_timer = t; }
+KernelTimer* kernel_timer() { return t_timer; }
+
 bool fft_length_ok(int n)
 {
   std::vector<int> r;

@@ -28,7 +28,7 @@ namespace simrecon {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kMaxElems = kFftEPT * kThreads;
+constexpr int kMaxElems = kFftElems;
 
 __device__ __forceinline__ float dev_suppress(float x)
 {
@@ -232,18 +232,18 @@ __global__ void k_asm_y(AssembleArgs a, const Slot* __restrict__ slots, FFTPlan 
     sm[t] = v;
   }
   __syncthreads();
-  fft_lines<+1>(sm, plan, W, 1, W);
+  const float2* res = fft_lines<+1>(sm, sm + Y * W, plan, W, 1, W);
   float2* dst = a.T + (size_t)blockIdx.y * Y * nx;
   for (int t = threadIdx.x; t < Y * W; t += blockDim.x) {
     int yr = t / W, w = t - yr * W;
-    if (c0 + w < nx) dst[(size_t)yr * nx + c0 + w] = sm[t];
+    if (c0 + w < nx) dst[(size_t)yr * nx + c0 + w] = res[t];
   }
 }
 
 // zero-padded inverse FFT along x of every slot of output plane zout, ramp,
 // weighted sum -> S[zout][yr][:]
 constexpr int kAccPerThread = 16;
-__global__ void __launch_bounds__(512) k_asm_x(AssembleArgs a, const int* __restrict__ plane_slot0,
+__global__ void __launch_bounds__(kThreads) k_asm_x(AssembleArgs a, const int* __restrict__ plane_slot0,
                                                const int* __restrict__ plane_nslot, const Slot* __restrict__ slots,
                                                const int* __restrict__ plane_zout, FFTPlan plan, int lines)
 {
@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(512) k_asm_x(AssembleArgs a, const int* __rest
       sm[t] = v;
     }
     __syncthreads();
-    fft_lines<+1>(sm, plan, lines, X, 1);
+    const float2* res = fft_lines<+1>(sm, sm + lines * X, plan, lines, X, 1);
     for (int l = 0; l < nb; ++l) {
       const Slot sl = slots[s0 + b0 + l];
       const int ro = sl.dir * a.norders + sl.order;
@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(512) k_asm_x(AssembleArgs a, const int* __rest
         int x = threadIdx.x + k * blockDim.x;
         if (x < X) {
           float2 e = cmul(a.ex[(size_t)ro * X + x], ey);
-          float2 v = cmul(sm[l * X + x], e);
+          float2 v = cmul(res[l * X + x], e);
           acc[k].x += v.x;
           acc[k].y += v.y;
         }
@@ -311,10 +311,10 @@ __global__ void __launch_bounds__(kThreads) k_asm_z(AssembleArgs a, const unsign
     sm[t] = (zactive[z] && c0 + w < X) ? a.S[((size_t)z * Y + yr) * X + c0 + w] : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  fft_lines<+1>(sm, plan, W, 1, W);
+  const float2* res = fft_lines<+1>(sm, sm + Z * W, plan, W, 1, W);
   for (int t = threadIdx.x; t < Z * W; t += blockDim.x) {
     int z = t / W, w = t - z * W;
-    if (c0 + w < X) a.out[((size_t)z * Y + yr) * X + c0 + w] = sm[t].x;
+    if (c0 + w < X) a.out[((size_t)z * Y + yr) * X + c0 + w] = res[t].x;
   }
 }
 
@@ -359,7 +359,19 @@ int launch_filter(const FilterArgs& a, cudaStream_t s, long long* launches)
 {
   const int nxh = a.nx / 2 + 1;
   dim3 g((a.ny * nxh + kThreads - 1) / kThreads, a.nz, a.norders);
+  KernelTimer* kt = kernel_timer();
+  if (kt) kt->begin(s);
   k_filter<<<g, kThreads, 0, s>>>(a);
+  // every element of the 2*norders-1 bands of this direction is read (in
+  // band) or only written (cleared)
+  double planeb = (double)a.ny * nxh * sizeof(float2);
+  double bytes = 0;
+  for (int o = 0; o < a.norders; ++o) {
+    int nb = o == 0 ? 1 : 2;
+    int inb = std::min(a.nz, 2 * a.zdc[o] + 1);
+    bytes += nb * planeb * (2.0 * inb + (a.nz - inb));
+  }
+  if (kt) kt->end("k_filter", s, bytes);
   if (launches) *launches += 1;
   return (int)cudaGetLastError();
 }
@@ -396,7 +408,7 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
     kzs.push_back(0);
   // slots per plane
   std::vector<Slot> slots;
-  std::vector<int> p0, pn, pz;
+  std::vector<int> p0, pn, pzo;
   std::vector<unsigned char> zact(a.Z, 0);
   for (int kz : kzs) {
     int start = (int)slots.size();
@@ -414,7 +426,7 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
       int zo = kz < 0 ? kz + a.Z : kz;
       p0.push_back(start);
       pn.push_back(cnt);
-      pz.push_back(zo);
+      pzo.push_back(zo);
       zact[zo] = 1;
     }
   }
@@ -434,17 +446,17 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
   cudaMemcpyAsync(d_slots, slots.data(), slots.size() * sizeof(Slot), cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(d_p0, p0.data(), p0.size() * sizeof(int), cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(d_pn, pn.data(), pn.size() * sizeof(int), cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(d_pz, pz.data(), pz.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(d_pz, pzo.data(), pzo.size() * sizeof(int), cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(d_zact, zact.data(), a.Z, cudaMemcpyHostToDevice, s);
   // tile sizes
   int Wy = std::max(1, std::min(32, kMaxElems / a.Y));
-  size_t smy = (size_t)Wy * a.Y * sizeof(float2);
+  size_t smy = (size_t)2 * Wy * a.Y * sizeof(float2);
   cudaFuncSetAttribute(k_asm_y, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
-  int xlines = std::max(1, (kFftEPT * 512) / a.X);
+  int xlines = std::max(1, kMaxElems / a.X);
   xlines = std::min(xlines, 16);
-  size_t smx = (size_t)xlines * a.X * sizeof(float2);
+  size_t smx = (size_t)2 * xlines * a.X * sizeof(float2);
   cudaFuncSetAttribute(k_asm_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
-  if (a.X > kAccPerThread * 512) return -3;
+  if (a.X > kAccPerThread * kThreads) return -3;
   // process whole planes in groups whose slots fit in T
   size_t np = p0.size();
   size_t pi = 0;
@@ -458,19 +470,31 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
     // T holds slots [first, first + nsl); shift the slot pointer so that
     // blockIdx.y indexes T from 0
     AssembleArgs ay = a;
+    KernelTimer* kt = kernel_timer();
+    if (kt) kt->begin(s);
     k_asm_y<<<dim3((nx + Wy - 1) / Wy, nsl), kThreads, smy, s>>>(ay, d_slots + first, py, Wy);
+    if (kt) {
+      double rd = 0;
+      for (int q = first; q < first + nsl; ++q) rd += (slots[q].order == 0 ? 1 : 2) * (double)a.ny * nx * 8;
+      kt->end("k_asm_y", s, rd + (double)nsl * per_slot * sizeof(float2));
+    }
     // k_asm_x reads T[(slot - first)]: pass a shifted T base
     AssembleArgs ax = a;
     ax.T = a.T - (size_t)first * per_slot;
-    k_asm_x<<<dim3(a.Y, (unsigned)(pj - pi)), 512, smx, s>>>(ax, d_p0 + pi, d_pn + pi, d_slots, d_pz + pi, px,
+    if (kt) kt->begin(s);
+    k_asm_x<<<dim3(a.Y, (unsigned)(pj - pi)), kThreads, smx, s>>>(ax, d_p0 + pi, d_pn + pi, d_slots, d_pz + pi, px,
                                                               xlines);
+    if (kt) kt->end("k_asm_x", s, (double)nsl * per_slot * sizeof(float2) + (double)(pj - pi) * a.X * a.Y * 8);
     nl += 2;
     pi = pj;
   }
   int Wz = std::max(1, std::min(32, kMaxElems / a.Z));
-  size_t smz = (size_t)Wz * a.Z * sizeof(float2);
+  size_t smz = (size_t)2 * Wz * a.Z * sizeof(float2);
   cudaFuncSetAttribute(k_asm_z, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
+  KernelTimer* kt = kernel_timer();
+  if (kt) kt->begin(s);
   k_asm_z<<<dim3((a.X + Wz - 1) / Wz, a.Y), kThreads, smz, s>>>(a, d_zact, pz, Wz);
+  if (kt) kt->end("k_asm_z", s, (double)np * a.X * a.Y * 8 + (double)a.X * a.Y * a.Z * 4);
   nl += 1;
   if (launches) *launches += nl;
   return (int)cudaGetLastError();

@@ -29,7 +29,7 @@ namespace simrecon {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kMaxElems = kFftEPT * kThreads;
+constexpr int kMaxElems = kFftElems;
 
 // ---------------------------------------------------------------- overlaps
 __global__ void __launch_bounds__(kThreads) k_ovl_build_x(OverlapArgs a, FFTPlan plan, int rows_per_cta)
@@ -116,16 +116,16 @@ __global__ void __launch_bounds__(kThreads) k_ovl_build_x(OverlapArgs a, FFTPlan
     sm[l * nx + j] = val;
   }
   __syncthreads();
-  fft_lines<+1>(sm, plan, 2 * rows_per_cta, nx, 1);
+  const float2* res = fft_lines<+1>(sm, sm + 2 * rows_per_cta * nx, plan, 2 * rows_per_cta, nx, 1);
   const size_t vol = (size_t)nzb * ny * nx;
   for (int t = threadIdx.x; t < 2 * nrows * nx; t += blockDim.x) {
     int l = t / nx, j = t - l * nx;
     int r = l >> 1, ov = l & 1;
-    a.ovl[(size_t)ov * vol + (size_t)(row0 + r) * nx + j] = sm[t];
+    a.ovl[(size_t)ov * vol + (size_t)(row0 + r) * nx + j] = res[t];
   }
 }
 
-__global__ void k_ovl_y_accum(OverlapArgs a, FFTPlan plan, int W, int planes_per_group)
+__global__ void __launch_bounds__(kThreads) k_ovl_y_accum(OverlapArgs a, FFTPlan plan, int W, int planes_per_group)
 {
   extern __shared__ float2 sm[];
   __shared__ double red[32];
@@ -135,7 +135,7 @@ __global__ void k_ovl_y_accum(OverlapArgs a, FFTPlan plan, int W, int planes_per
   const int zb0 = blockIdx.y * planes_per_group;
   const int zb1 = min(nzb, zb0 + planes_per_group);
   const int ld = 2 * W;
-  float2* acc = sm + (size_t)ny * ld;  // [ny][W]
+  float2* acc = sm + (size_t)2 * ny * ld;  // [ny][W], after the two FFT buffers
   for (int t = threadIdx.x; t < ny * W; t += blockDim.x) acc[t] = make_float2(0.f, 0.f);
   double sx = 0.0, sy = 0.0;
   const size_t vol = (size_t)nzb * ny * nx;
@@ -147,10 +147,10 @@ __global__ void k_ovl_y_accum(OverlapArgs a, FFTPlan plan, int W, int planes_per
       sm[t] = (c0 + w < nx) ? a.ovl[(size_t)ov * vol + ((size_t)zb * ny + y) * nx + c0 + w] : make_float2(0.f, 0.f);
     }
     __syncthreads();
-    fft_lines<+1>(sm, plan, ld, 1, ld);
+    const float2* res = fft_lines<+1>(sm, sm + ny * ld, plan, ld, 1, ld);
     for (int t = threadIdx.x; t < ny * W; t += blockDim.x) {
       int y = t / W, w = t - y * W;
-      float2 X = sm[y * ld + w], Y = sm[y * ld + W + w];
+      float2 X = res[y * ld + w], Y = res[y * ld + W + w];
       float2 p = acc[t];
       // conj(X) * Y, as reductionKernel's xsy (gpuFunctionsImpl.cu:1177-1178)
       p.x += X.x * Y.x + X.y * Y.y;
@@ -221,8 +221,8 @@ __global__ void __launch_bounds__(kThreads) k_fft_rows(const float2* in, float2*
     sm[t] = v;
   }
   __syncthreads();
-  fft_lines<DIR>(sm, plan, nl, n, 1);
-  for (int t = threadIdx.x; t < nr * n; t += blockDim.x) out[(size_t)r0 * n + t] = sm[t];
+  const float2* res = fft_lines<DIR>(sm, sm + nl * n, plan, nl, n, 1);
+  for (int t = threadIdx.x; t < nr * n; t += blockDim.x) out[(size_t)r0 * n + t] = res[t];
 }
 
 template <int DIR>
@@ -235,10 +235,10 @@ __global__ void __launch_bounds__(kThreads) k_fft_cols2(float2* data, int n, int
     sm[t] = (c0 + w < ncol) ? data[(size_t)i * ncol + c0 + w] : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  fft_lines<DIR>(sm, plan, W, 1, W);
+  const float2* res = fft_lines<DIR>(sm, sm + n * W, plan, W, 1, W);
   for (int t = threadIdx.x; t < n * W; t += blockDim.x) {
     int i = t / W, w = t - i * W;
-    if (c0 + w < ncol) data[(size_t)i * ncol + c0 + w] = sm[t];
+    if (c0 + w < ncol) data[(size_t)i * ncol + c0 + w] = res[t];
   }
 }
 
@@ -318,6 +318,7 @@ __global__ void k_argmax_final(const float2* cc, int nx, int ny, const float* bv
     int nw = blockDim.x >> 5;
     for (int w = 1; w < nw; ++w) better(sv[0], si[0], sv[w], si[w]);
     int idx = si[0];
+    if (idx < 0 || idx >= nx * ny) idx = 0;  // all-NaN input: no maximum
     int ix = idx % nx, iy = idx / nx;
     peak[0] = (float)ix;
     peak[1] = (float)iy;
@@ -407,20 +408,27 @@ int launch_overlaps(OverlapArgs& a, cudaStream_t s, long long* launches)
   // 1) build + x inverse FFT
   int rows = std::max(1, kMaxElems / (2 * a.nx));
   rows = std::min(rows, nzb * a.ny);
-  size_t sm1 = (size_t)2 * rows * a.nx * sizeof(float2);
+  size_t sm1 = (size_t)4 * rows * a.nx * sizeof(float2);
   int nb1 = (nzb * a.ny + rows - 1) / rows;
   cudaFuncSetAttribute(k_ovl_build_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
+  KernelTimer* kt = kernel_timer();
+  const double ovlb = 2.0 * nzb * a.ny * a.nx * sizeof(float2);
+  const double bandplanes = (double)nzb * a.ny * (a.nx / 2 + 1) * sizeof(float2);
+  if (kt) kt->begin(s);
   k_ovl_build_x<<<nb1, kThreads, sm1, s>>>(a, px, rows);
+  if (kt) kt->end("k_ovl_build_x", s, ovlb + (a.order1 == 0 ? 3 : 4) * bandplanes);
   // 2) y inverse FFT + accumulation over kz planes
-  int threads = 2 * 8 * a.ny > kMaxElems ? 512 : 256;
-  int W = std::max(1, std::min(16, (kFftEPT * threads) / (2 * a.ny)));
+  const int threads = kThreads;
+  int W = std::max(1, std::min(16, kMaxElems / (2 * a.ny)));
   int tiles = (a.nx + W - 1) / W;
   int groups = std::max(1, std::min(nzb, (2 * 152 + tiles - 1) / tiles));
   int ppg = (nzb + groups - 1) / groups;
   groups = (nzb + ppg - 1) / ppg;
-  size_t sm2 = (size_t)a.ny * (2 * W + W) * sizeof(float2);
+  size_t sm2 = (size_t)a.ny * (4 * W + W) * sizeof(float2);
   cudaFuncSetAttribute(k_ovl_y_accum, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+  if (kt) kt->begin(s);
   k_ovl_y_accum<<<dim3(tiles, groups), threads, sm2, s>>>(a, py, W, ppg);
+  if (kt) kt->end("k_ovl_y_accum", s, ovlb + (double)groups * a.ny * a.nx * sizeof(float2));
   // 3) reduce plane groups
   k_p_reduce<<<std::min(1024, (a.nx * a.ny + 255) / 256), 256, 0, s>>>(a, groups, tiles * groups);
   if (launches) *launches += 3;
@@ -433,11 +441,11 @@ int launch_crosscorr_peak(const float2* pmap, float2* cc, int nx, int ny, float*
   FFTPlan px, py;
   if (!get_fft_plan(nx, &px) || !get_fft_plan(ny, &py)) return -1;
   int nl = std::max(1, std::min(ny, kMaxElems / nx));
-  size_t sm1 = (size_t)nl * nx * sizeof(float2);
+  size_t sm1 = (size_t)2 * nl * nx * sizeof(float2);
   cudaFuncSetAttribute(k_fft_rows<-1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
   k_fft_rows<-1, true><<<(ny + nl - 1) / nl, kThreads, sm1, s>>>(pmap, cc, nx, ny, px, nl);
   int W = std::max(1, std::min(32, kMaxElems / ny));
-  size_t sm2 = (size_t)W * ny * sizeof(float2);
+  size_t sm2 = (size_t)2 * W * ny * sizeof(float2);
   cudaFuncSetAttribute(k_fft_cols2<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
   k_fft_cols2<-1><<<(nx + W - 1) / W, kThreads, sm2, s>>>(cc, ny, nx, py, W);
   int nb = 256;

@@ -20,7 +20,7 @@ namespace simrecon {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kMaxElems = kFftEPT * kThreads;  // complex elements per CTA
+constexpr int kMaxElems = kFftElems;  // complex elements per CTA and buffer
 
 __device__ __forceinline__ int raw_section(int d, int p, int z, int nz, int ndirs, int nph, int fastSI)
 {
@@ -91,12 +91,12 @@ __global__ void __launch_bounds__(kThreads) k_ingest_x(IngestArgs a, FFTPlan pla
   }
   __syncthreads();
   // 3) forward FFT along x of the packed lines
-  fft_lines<-1>(sm, plan, nl, nx, 1);
+  const float2* res = fft_lines<-1>(sm, sm + nl * nx, plan, nl, nx, 1);
   // 4) split the two real transforms, keep kx in [0, nx/2]
   for (int t = threadIdx.x; t < nl * nxh; t += blockDim.x) {
     int l = t / nxh, k = t - l * nxh;
-    float2 zk = sm[l * nx + k];
-    float2 zn = sm[l * nx + (nx - k) % nx];
+    float2 zk = res[l * nx + k];
+    float2 zn = res[l * nx + (nx - k) % nx];
     float2 A = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
     float2 B = make_float2(0.5f * (zk.y + zn.y), -0.5f * (zk.x - zn.x));
     int y = y0 + 2 * l;
@@ -118,10 +118,10 @@ __global__ void __launch_bounds__(kThreads) k_fft_cols(float2* data, int n, int 
     sm[t] = (c0 + w < ncol) ? base[(size_t)i * ncol + c0 + w] : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  fft_lines<DIR>(sm, plan, W, 1, W);
+  const float2* res = fft_lines<DIR>(sm, sm + n * W, plan, W, 1, W);
   for (int t = threadIdx.x; t < n * W; t += blockDim.x) {
     int i = t / W, w = t - i * W;
-    if (c0 + w < ncol) base[(size_t)i * ncol + c0 + w] = sm[t];
+    if (c0 + w < ncol) base[(size_t)i * ncol + c0 + w] = res[t];
   }
 }
 
@@ -178,11 +178,12 @@ __global__ void __launch_bounds__(kThreads) k_separate(float2* spec, const float
     }
   }
   __syncthreads();
-  if (nz > 1) fft_lines<-1>(sm, plan, nph * W, 1, ld);
+  const float2* res = sm;
+  if (nz > 1) res = fft_lines<-1>(sm, sm + nz * ld, plan, nph * W, 1, ld);
   for (int t = threadIdx.x; t < nz * nph * W; t += blockDim.x) {
     int z = t / ld, r = t - z * ld;
     int b = r / W, w = r - b * W;
-    if (c0 + w < nxh) dbase[((size_t)b * nz + z) * plane + w] = sm[t];
+    if (c0 + w < nxh) dbase[((size_t)b * nz + z) * plane + w] = res[t];
   }
 }
 
@@ -196,8 +197,11 @@ int launch_ingest(const IngestArgs& a, cudaStream_t s, long long* launches)
   const int nplanes = a.ndirs * a.nphases * a.nz;
   int nl = std::max(1, std::min(kMaxElems / a.nx, 256));
   nl = std::min(nl, (a.ny + 1) / 2);
-  size_t smx = (size_t)nl * a.nx * sizeof(float2);
+  size_t smx = (size_t)2 * nl * a.nx * sizeof(float2);
   dim3 gx((a.ny + 2 * nl - 1) / (2 * nl), nplanes);
+  KernelTimer* kt = kernel_timer();
+  const double specb = (double)nplanes * a.ny * nxh * sizeof(float2);
+  if (kt) kt->begin(s);
   if (a.raw_is_u16) {
     cudaFuncSetAttribute(k_ingest_x<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
     k_ingest_x<uint16_t><<<gx, kThreads, smx, s>>>(a, px, nl);
@@ -205,11 +209,14 @@ int launch_ingest(const IngestArgs& a, cudaStream_t s, long long* launches)
     cudaFuncSetAttribute(k_ingest_x<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
     k_ingest_x<float><<<gx, kThreads, smx, s>>>(a, px, nl);
   }
+  if (kt) kt->end("k_ingest_x", s, (double)nplanes * a.nx * a.ny * (a.raw_is_u16 ? 2 : 4) + specb);
   int W = std::max(1, std::min(32, kMaxElems / a.ny));
-  size_t smy = (size_t)W * a.ny * sizeof(float2);
+  size_t smy = (size_t)2 * W * a.ny * sizeof(float2);
   dim3 gy((nxh + W - 1) / W, nplanes);
   cudaFuncSetAttribute(k_fft_cols<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
+  if (kt) kt->begin(s);
   k_fft_cols<-1><<<gy, kThreads, smy, s>>>(a.spec, a.ny, nxh, py, W);
+  if (kt) kt->end("k_fft_y", s, 2 * specb);
   if (launches) *launches += 2;
   return (int)cudaGetLastError();
 }
@@ -231,10 +238,13 @@ int launch_separate(float2* spec, const float* scale, const float* sepmat, int n
   const int nxh = nx / 2 + 1;
   int W = 32;
   while (W > 1 && nphases * W * nz > kMaxElems) W >>= 1;
-  size_t sm = (size_t)nphases * W * nz * sizeof(float2);
+  size_t sm = (size_t)2 * nphases * W * nz * sizeof(float2);
   dim3 g((nxh + W - 1) / W, ny, ndirs);
   cudaFuncSetAttribute(k_separate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  KernelTimer* kt = kernel_timer();
+  if (kt) kt->begin(s);
   k_separate<<<g, kThreads, sm, s>>>(spec, scale, sepmat, ny, nxh, nz, nphases, pz, W);
+  if (kt) kt->end("k_separate", s, 2.0 * ndirs * nphases * nz * (double)ny * nxh * sizeof(float2));
   if (launches) *launches += 1;
   return (int)cudaGetLastError();
 }

@@ -8,6 +8,18 @@
 
 namespace simrecon {
 
+// ------------------------------------------------------------ kernel timing
+// When a timer is installed on the calling thread, every launcher brackets
+// its launches with begin()/end() on the launch stream and reports the
+// algorithmic bytes of that launch (ideal single-pass reads + writes).
+struct KernelTimer {
+  virtual ~KernelTimer() {}
+  virtual void begin(cudaStream_t s) = 0;
+  virtual void end(const char* kernel, cudaStream_t s, double alg_bytes) = 0;
+};
+void set_kernel_timer(KernelTimer* t);
+KernelTimer* kernel_timer();
+
 // ----------------------------------------------------------------- FFT plans
 // Returns a plan (radix sequence + device twiddles) for length n; cached per
 // (device, n).  n must factor into 2, 3, 5, 7.  Returns false if it cannot.

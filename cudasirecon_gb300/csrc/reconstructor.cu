@@ -1,0 +1,1258 @@
+// Host orchestration of the reconstruction (the reference's
+// SIM_Reconstructor, cudaSirecon.cpp:792-1713, and the host halves of
+// gpuFunctionsImpl.cu).  All device work is issued on the handle's own
+// stream; the host only steers the k0 / modamp search, reading back a few
+// scalars per search step.
+#include "reconstructor.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <dirent.h>
+#include <regex>
+#include <sstream>
+#include <stdexcept>
+#include <sys/stat.h>
+
+using namespace simrecon;
+
+namespace {
+
+constexpr float kK0WarningThresh = 0.05f;  // cudaSireconImpl.h:55
+constexpr int kMaxCand = 64;
+
+uint32_t fbits(float f)
+{
+  uint32_t u;
+  memcpy(&u, &f, 4);
+  return u;
+}
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// fitparabola, gpuFunctionsImpl.cu:479-495
+float fitparabola(float a1, float a2, float a3)
+{
+  float slope = 0.5 * (a3 - a1);
+  float curve = (a3 + a1) - 2 * a2;
+  if (curve == 0) return 0.0;
+  float peak = -slope / curve;
+  if (peak > 1.5 || peak < -1.5) return 0.0;
+  return peak;
+}
+
+// fitxyparabola, gpuFunctionsImpl.cu:1022-1044
+float fitxyparabola(float x1, float y1, float x2, float y2, float x3, float y3)
+{
+  if (x1 == x2 || x2 == x3 || x3 == x1) return 0.0;
+  float xbar1 = 0.5 * (x1 + x2);
+  float xbar2 = 0.5 * (x2 + x3);
+  float slope1 = (y2 - y1) / (x2 - x1);
+  float slope2 = (y3 - y2) / (x3 - x2);
+  float curve = (slope2 - slope1) / (xbar2 - xbar1);
+  if (curve == 0) return 0.0;
+  return xbar2 - slope2 / curve;
+}
+
+bool is_directory(const std::string& p)
+{
+  struct stat st;
+  return stat(p.c_str(), &st) == 0 && S_ISDIR(st.st_mode);
+}
+
+// gatherMatchingFiles (boostfs.cpp:9-56): regular files of the folder whose
+// full path matches ".*<pattern>" (".*<pattern>.*\.[tT][iI][fF]" unless the
+// pattern already names a .tif), sorted
+std::vector<std::string> gather_matching(const std::string& dir, std::string pattern)
+{
+  std::vector<std::string> out;
+  if (pattern.rfind(".tif") == std::string::npos && pattern.rfind(".TIF") == std::string::npos)
+    pattern.append(".*\\.[tT][iI][fF]");
+  pattern.insert(0, ".*");
+  std::regex filt;
+  try {
+    filt = std::regex(pattern);
+  } catch (...) {
+    return out;
+  }
+  DIR* dp = opendir(dir.c_str());
+  if (!dp) return out;
+  while (struct dirent* e = readdir(dp)) {
+    std::string name = e->d_name;
+    if (name == "." || name == "..") continue;
+    std::string full = dir + (dir.empty() || dir.back() == '/' ? "" : "/") + name;
+    struct stat st;
+    if (stat(full.c_str(), &st) != 0 || !S_ISREG(st.st_mode)) continue;
+    if (std::regex_match(full, filt)) out.push_back(full);
+  }
+  closedir(dp);
+  std::sort(out.begin(), out.end());
+  if (!out.empty()) mkdir((dir + "/GPUsirecon").c_str(), 0755);
+  return out;
+}
+
+// makeOutputFilePath (boostfs.cpp:59-72)
+std::string output_path_for(const std::string& input, const std::string& insert)
+{
+  std::string base = input.substr(input.find_last_of('/') + 1);
+  std::string dir = input.substr(0, input.find_last_of('/') + 1);
+  size_t pos = base.find_last_of(".tif");
+  if (pos != std::string::npos && pos >= 3) base.insert(pos - 3, insert);
+  return dir + "GPUsirecon/" + base;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ construction
+void SIM_Reconstructor::check(cudaError_t e, const char* what)
+{
+  if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void SIM_Reconstructor::check_launch(int rc, const char* what)
+{
+  if (rc != 0) {
+    if (rc > 0) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString((cudaError_t)rc));
+    throw std::runtime_error(std::string(what) + ": unsupported size (code " + std::to_string(rc) + ")");
+  }
+}
+
+bool SIM_Reconstructor::load_otf_tiff(const std::string& path, Stack* out, std::string* err)
+{
+  return tiff_read(path, out, err);
+}
+
+SIM_Reconstructor* SIM_Reconstructor::from_shape(int nx, int ny, int nimages, const std::string& config,
+                                                 std::string* err)
+{
+  SIM_Reconstructor* r = new SIM_Reconstructor();
+  set_defaults(&r->opt);
+  // the config file is parsed if it can be opened (cudaSirecon.cpp:884-890)
+  if (!apply_config_file(&r->opt, config, false, err)) {
+    delete r;
+    return nullptr;
+  }
+  if (r->opt.p.otffiles.empty()) {
+    *err = "the option '--otf-file' is required but missing";
+    delete r;
+    return nullptr;
+  }
+  Stack otf;
+  if (!r->load_otf_tiff(r->opt.p.otffiles, &otf, err)) {
+    delete r;
+    return nullptr;
+  }
+  r->opt.p.bTIFF = true;  // cudaSirecon.cpp:901
+  if (!r->setup(nx, ny, nimages, 1, &otf, err)) {
+    delete r;
+    return nullptr;
+  }
+  return r;
+}
+
+SIM_Reconstructor* SIM_Reconstructor::from_argv(int argc, char** argv, std::string* err)
+{
+  SIM_Reconstructor* r = new SIM_Reconstructor();
+  set_defaults(&r->opt);
+  for (int i = 0; i < argc; ++i) r->argv_.push_back(argv[i] ? argv[i] : "");
+  if (!parse_command_line(&r->opt, argc, argv, err)) {
+    delete r;
+    return nullptr;
+  }
+  if (r->opt.help || argc <= 1) {
+    *err = "help requested\n" + usage_text();
+    delete r;
+    return nullptr;
+  }
+  if (r->opt.version) {
+    *err = "version requested";
+    delete r;
+    return nullptr;
+  }
+  ReconParams& p = r->opt.p;
+  ImageParams& ip = r->opt.ip;
+  if (p.ifiles.empty() || p.ofiles.empty()) {
+    *err = "Calling openFiles() but no input or output files were specified";
+    delete r;
+    return nullptr;
+  }
+  // TIFF mode when the input is a folder with files matching the pattern
+  if (is_directory(p.ifiles)) {
+    r->tiff_files_ = gather_matching(p.ifiles, p.ofiles);
+    p.bTIFF = !r->tiff_files_.empty();
+  }
+  Stack otf;
+  int nx = 0, ny = 0, nimg = 0, nwaves = 1;
+  if (p.bTIFF) {
+    ip.ntimes = (short)r->tiff_files_.size();
+    int depth;
+    if (!tiff_info(r->tiff_files_[0], &nx, &ny, &depth, err)) {
+      delete r;
+      return nullptr;
+    }
+    nimg = depth;
+    if (!tiff_read(p.otffiles, &otf, err)) {
+      delete r;
+      return nullptr;
+    }
+  } else {
+    // MRC / DV input (loadHeader, mrc.h:18-45)
+    if (!mrc_open(p.ifiles, &r->mrc_in_, err)) {
+      delete r;
+      return nullptr;
+    }
+    const MrcHeader& h = r->mrc_in_.hdr;
+    nx = h.nx;
+    ny = h.ny;
+    nwaves = std::max<int>(1, h.num_waves);
+    int ntimes = std::max<int>(1, h.num_times);
+    nimg = h.nz / ntimes;  // sections per time point (all waves)
+    ip.ntimes = (short)ntimes;
+    ip.wave[0] = h.iwav1;
+    ip.wave[1] = h.iwav2;
+    ip.wave[2] = h.iwav3;
+    ip.wave[3] = h.iwav4;
+    ip.wave[4] = h.iwav5;
+    ip.dxy = h.ylen;
+    ip.dz = h.zlen;
+    // the OTF: MRC (complex) or TIFF
+    MrcFile of;
+    std::string e2;
+    if (mrc_open(p.otffiles, &of, &e2)) {
+      std::vector<float> all;
+      if (!mrc_read_all(of, &all, err)) {
+        delete r;
+        return nullptr;
+      }
+      // determine_otf_dimensions, MRC branch (cudaSirecon.cpp:1484-1523):
+      // complex sections of nx (kz) by ny (kr); stored like the TIFF layout
+      otf.width = 2 * of.hdr.nx;
+      otf.height = of.hdr.ny;
+      otf.depth = of.hdr.nz;
+      otf.data = all;
+      // dkz / dkr come from the header
+      p.dkzotf = of.hdr.xlen;
+      p.dkrotf = of.hdr.ylen;
+      if (nimg / (nwaves * p.nphases * p.ndirs) == 1) p.dkrotf = of.hdr.xlen;
+      r->otf_dk_from_header_ = true;
+    } else if (!tiff_read(p.otffiles, &otf, err)) {
+      delete r;
+      return nullptr;
+    }
+  }
+  if (!r->setup(nx, ny, nimg, nwaves, &otf, err)) {
+    delete r;
+    return nullptr;
+  }
+  if (!p.bTIFF) {
+    // output header (setOutputHeader, mrc.h:47-60)
+    MrcHeader h = r->mrc_in_.hdr;
+    h.mode = 2;
+    h.nz = ip.nz * ip.nwaves * ip.ntimes * p.z_zoom;
+    h.nx = (int)(ip.nx * p.zoomfact);
+    h.ny = (int)(h.ny * p.zoomfact);
+    h.xlen /= p.zoomfact;
+    h.ylen /= p.zoomfact;
+    h.zlen /= p.z_zoom;
+    h.next = 0;
+    r->out_hdr_ = h;
+    r->out_path_ = p.ofiles;
+    r->mrc_out_.open(p.ofiles, std::ios::binary | std::ios::trunc);
+    if (!r->mrc_out_) {
+      *err = "File " + p.ofiles + " can not be created.";
+      delete r;
+      return nullptr;
+    }
+    r->mrc_out_.write((const char*)&r->out_hdr_, sizeof(MrcHeader));
+  }
+  return r;
+}
+
+// setup() + setup_common(), cudaSirecon.cpp:1104-1261
+bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Stack* otf, std::string* err)
+{
+  ReconParams& p = opt.p;
+  ImageParams& ip = opt.ip;
+  ip.nx = nx;
+  ip.nx_raw = nx;
+  ip.ny = ny;
+  ip.nwaves = (short)nwaves;
+  ip.nz = nimages / (nwaves * p.nphases * p.ndirs);
+  ip.nz0 = ip.nz;
+  ip.dz_raw = 0;
+  if (ip.nz < 1 || nimages != ip.nz * nwaves * p.nphases * p.ndirs) {
+    *err = "number of images (" + std::to_string(nimages) + ") is not a multiple of ndirs*nphases";
+    return false;
+  }
+  if (fabs(p.deskewAngle) > 0.f || p.bBessel || p.bTwolens || p.nzPadTo || p.cropXYto) {
+    *err = "deskew, Bessel, two-lens, nzPadTo and cropXY modes are not supported by this build";
+    return false;
+  }
+  p.norders = p.norders_output != 0 ? p.norders_output : p.nphases / 2 + 1;
+  if (2 * p.norders - 1 != p.nphases) {
+    *err = "nphases must equal 2*norders-1 (the band separation swaps nphases bands)";
+    return false;
+  }
+  if (p.ndirs > kMaxDirs || p.norders > kMaxOrders || p.nphases > kMaxPhases) {
+    *err = "too many directions / orders / phases";
+    return false;
+  }
+  if (!p.bRadAvgOTF) {
+    *err = "only rotationally averaged OTFs (otfRA) are supported: the reference's GPU OTF lookup returns 0 "
+           "for other OTFs (gpuFunctionsImpl.cu:1677-1715)";
+    return false;
+  }
+  nx_ = nx;
+  ny_ = ny;
+  nz_ = ip.nz;
+  nxh_ = nx / 2 + 1;
+  nimg_ = nimages;
+  nph_ = p.nphases;
+  ndirs_ = p.ndirs;
+  norders_ = p.norders;
+  X_ = (int)lrint(p.zoomfact * nx);
+  Y_ = (int)lrint(p.zoomfact * ny);
+  Z_ = p.z_zoom * nz_;
+  if (X_ < nx || Y_ < ny || Z_ < nz_) {
+    *err = "zoom factors below 1 are not supported";
+    return false;
+  }
+  for (int n : {nx, ny, nz_, X_, Y_, Z_})
+    if (!fft_length_ok(n) || n > 8192) {
+      *err = "image size " + std::to_string(n) + " does not factor into 2, 3, 5 and 7 (or exceeds 8192)";
+      return false;
+    }
+  if (p.napodize > ny / 2 || p.napodize > nx / 2 || p.napodize > kMaxApo) {
+    *err = "napodize too large for the image";
+    return false;
+  }
+  // determine_otf_dimensions (cudaSirecon.cpp:1446-1523), RA OTF
+  const int w2 = otf->width / 2;
+  if (nz_ == 1) {
+    p.nxotf = w2;
+    p.nyotf = 1;
+    p.nzotf = 1;
+    if (!otf_dk_from_header_) p.dkrotf = 1 / (ip.dxy * (w2 - 1) * 2);
+    p.dkzotf = 1;
+  } else {
+    p.nzotf = w2;
+    p.nxotf = otf->height;
+    p.nyotf = 1;
+    if (!otf_dk_from_header_) {
+      p.dkzotf = 1 / (p.dzPSF * p.nzotf);
+      p.dkrotf = 1 / (ip.dxy * (p.nxotf - 1) * 2);
+    }
+  }
+  ndirs_otf_ = p.bOneOTFperAngle ? p.ndirs : 1;
+  const size_t otf_size = (size_t)p.nxotf * p.nzotf;
+  const size_t page = (size_t)otf->width * otf->height;
+  std::vector<float2v> hotf((size_t)ndirs_otf_ * norders_ * otf_size);
+  // loadOTFs: section i of the file is order i; missing ones copy otf[0][0]
+  for (int d = 0; d < ndirs_otf_; ++d)
+    for (int o = 0; o < norders_; ++o) {
+      int sec = o + d * norders_;
+      const float* src = (otf->depth > sec) ? otf->data.data() + page * sec : otf->data.data();
+      if (otf_size * 2 > page) {
+        *err = "OTF file smaller than its declared size";
+        return false;
+      }
+      memcpy(&hotf[((size_t)d * norders_ + o) * otf_size], src, otf_size * sizeof(float2v));
+    }
+
+  // makematrix, default branch (cudaSirecon.cpp:606-617)
+  sepmat_.assign((size_t)nph_ * nph_, 0.f);
+  float phi = 2.0 * M_PI / nph_;
+  for (int j = 0; j < nph_; ++j) {
+    sepmat_[0 * nph_ + j] = 1.0;
+    for (int order = 1; order < norders_; ++order) {
+      sepmat_[(2 * order - 1) * nph_ + j] = cos(j * order * phi);
+      sepmat_[2 * order * nph_ + j] = sin(j * order * phi);
+    }
+  }
+  noisevar_.assign((size_t)ndirs_ * norders_, 1.0f);
+
+  // inscale and k0guess (cudaSirecon.cpp:1231-1252)
+  ip.inscale = 1.0 / (ip.nx * ip.ny * ip.nz0 * p.zoomfact * p.zoomfact * p.z_zoom * p.ndirs);
+  k0_.assign(ndirs_, float2v{0, 0});
+  k0_time0_.assign(ndirs_, float2v{0, 0});
+  k0guess_.assign(ndirs_, float2v{0, 0});
+  float delta_angle = M_PI / p.ndirs;
+  float k0magguess = 1.0 / p.linespacing;
+  if (ip.nz > 1) {
+    int nordersIn = p.nphases / 2 + 1;
+    k0magguess /= nordersIn - 1;
+  }
+  for (int i = 0; i < p.ndirs; ++i) {
+    float k0angleguess;
+    if (p.k0angles.size() < (size_t)p.ndirs) k0angleguess = p.k0startangle + i * delta_angle;
+    else k0angleguess = p.k0angles[i];
+    k0guess_[i].x = k0magguess * cos(k0angleguess);
+    k0guess_[i].y = k0magguess * sin(k0angleguess);
+  }
+  amp_.assign(ndirs_, std::vector<float2v>(norders_, float2v{0, 0}));
+  for (int i = 0; i < ndirs_; ++i) amp_[i][0] = float2v{1.0f, 0.0f};
+
+  // makeoverlaps zdistcutoff (gpuFunctionsImpl.cu:529-548) bounds the overlap planes
+  {
+    float dkz = 1.0f / (nz_ * ip.dz);
+    float lambdaem = (ip.wave[0] / p.nimm) / 1.0e3;
+    float alpha = asinf(p.na / p.nimm);
+    float zd = (int)ceil(((1.0 - cosf(alpha)) / lambdaem) / dkz);
+    if (zd > nz_ / 2) zd = ((nz_ / 2 - 1) > 0) ? (nz_ / 2 - 1) : 0;
+    zdc_ovl_ = (int)zd;
+  }
+
+  // device arena
+  check(cudaGetDevice(&device_), "cudaGetDevice");
+  check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  const size_t nspec = (size_t)ndirs_ * nph_ * nz_ * ny_ * nxh_;
+  const int nzb = 2 * zdc_ovl_ + 1;
+  const size_t nxy = (size_t)nx_ * ny_;
+  // assembly scratch: at least all slots of one plane, up to 64 MiB
+  const size_t per_slot = (size_t)Y_ * nx_;
+  size_t want_slots = std::max<size_t>((size_t)ndirs_ * norders_, (64ull << 20) / (per_slot * sizeof(float2)));
+  tcap_ = want_slots * per_slot + 65536;
+  struct Req {
+    void** ptr;
+    size_t bytes;
+  };
+  std::vector<Req> reqs = {
+      {&d_raw_, (size_t)nimg_ * nxy * sizeof(float)},
+      {(void**)&d_spec_, nspec * sizeof(float2)},
+      {(void**)&d_scale_, (size_t)ndirs_ * nph_ * nz_ * sizeof(float)},
+      {(void**)&d_sdp0_, (size_t)nz_ * sizeof(double)},
+      {(void**)&d_sepmat_, sepmat_.size() * sizeof(float)},
+      {(void**)&d_apofact_, (size_t)kMaxApo * sizeof(float)},
+      {(void**)&d_otf_, hotf.size() * sizeof(float2)},
+      {(void**)&d_ovl_, 2 * (size_t)nzb * nxy * sizeof(float2)},
+      {(void**)&d_ppart_, (size_t)nzb * nxy * sizeof(float2)},
+      {(void**)&d_sums_, 2 * (size_t)(nx_ + 1) * nzb * sizeof(double)},
+      {(void**)&d_pmap_, nxy * sizeof(float2)},
+      {(void**)&d_sumxy_, 2 * sizeof(double)},
+      {(void**)&d_cc_, nxy * sizeof(float2)},
+      {(void**)&d_bval_, 256 * sizeof(float)},
+      {(void**)&d_bidx_, 256 * sizeof(int)},
+      {(void**)&d_peak_, 8 * sizeof(float)},
+      {(void**)&d_kcand_, kMaxCand * sizeof(float2)},
+      {(void**)&d_tables_, (size_t)kMaxCand * (nx_ + ny_) * sizeof(float2)},
+      {(void**)&d_partial_, (size_t)256 * kMaxCand * 2 * sizeof(double)},
+      {(void**)&d_xstary_, (size_t)kMaxCand * 2 * sizeof(double)},
+      {(void**)&d_k0_, (size_t)kMaxDirs * sizeof(float2)},
+      {(void**)&d_ex_, (size_t)ndirs_ * norders_ * X_ * sizeof(float2)},
+      {(void**)&d_ey_, (size_t)ndirs_ * norders_ * Y_ * sizeof(float2)},
+      {(void**)&d_T_, tcap_ * sizeof(float2)},
+      {(void**)&d_S_, (size_t)X_ * Y_ * Z_ * sizeof(float2)},
+      {(void**)&d_out_, (size_t)X_ * Y_ * Z_ * sizeof(float)},
+  };
+  size_t total = 0;
+  for (auto& r : reqs) total += align_up(r.bytes, 256);
+  cudaError_t e = cudaMalloc((void**)&arena_, total);
+  if (e != cudaSuccess) {
+    *err = std::string("device allocation of ") + std::to_string(total >> 20) + " MiB failed: " +
+           cudaGetErrorString(e);
+    return false;
+  }
+  arena_bytes_ = total;
+  size_t off = 0;
+  for (auto& r : reqs) {
+    *r.ptr = arena_ + off;
+    off += align_up(r.bytes, 256);
+  }
+  check(cudaMallocHost((void**)&h_pinned_, 4096), "cudaMallocHost");
+  std::vector<float> fact(kMaxApo, 0.f);
+  for (int l = 0; l < p.napodize; ++l) fact[l] = 1.0 - sinf((l + 0.5) / (float)p.napodize * M_PI * 0.5);
+  check(cudaMemcpy(d_apofact_, fact.data(), kMaxApo * sizeof(float), cudaMemcpyHostToDevice), "upload");
+  check(cudaMemcpy(d_sepmat_, sepmat_.data(), sepmat_.size() * sizeof(float), cudaMemcpyHostToDevice), "upload");
+  check(cudaMemcpy(d_otf_, hotf.data(), hotf.size() * sizeof(float2), cudaMemcpyHostToDevice), "upload");
+  check(cudaMemset(d_sdp0_, 0, (size_t)nz_ * sizeof(double)), "memset");
+  check(cudaMemset(d_spec_, 0, nspec * sizeof(float2)), "memset");
+  return true;
+}
+
+SIM_Reconstructor::~SIM_Reconstructor()
+{
+  for (auto& pd : pending_) {
+    cudaEventDestroy(pd.a);
+    cudaEventDestroy(pd.b);
+  }
+  if (stream_) cudaStreamSynchronize(stream_);
+  if (arena_) cudaFree(arena_);
+  if (d_flush_) cudaFree(d_flush_);
+  if (h_pinned_) cudaFreeHost(h_pinned_);
+  if (stream_) cudaStreamDestroy(stream_);
+}
+
+// ---------------------------------------------------------------- profiling
+void SIM_Reconstructor::stage_begin(const char* name, cudaEvent_t* a, long long* l0)
+{
+  (void)name;
+  *l0 = launches_;
+  if (!profiling_) return;
+  cudaEventCreate(a);
+  cudaEventRecord(*a, stream_);
+}
+
+void SIM_Reconstructor::stage_end(const char* name, cudaEvent_t a, long long l0)
+{
+  if (!profiling_) return;
+  cudaEvent_t b;
+  cudaEventCreate(&b);
+  cudaEventRecord(b, stream_);
+  pending_.push_back(Pending{name, a, b, launches_ - l0, 0.0, false});
+}
+
+void SIM_Reconstructor::KTimer::begin(cudaStream_t s)
+{
+  cudaEventCreate(&cur);
+  cudaEventRecord(cur, s);
+}
+
+void SIM_Reconstructor::KTimer::end(const char* kernel, cudaStream_t s, double alg_bytes)
+{
+  cudaEvent_t b;
+  cudaEventCreate(&b);
+  cudaEventRecord(b, s);
+  r->pending_.push_back(Pending{kernel, cur, b, 1, alg_bytes, true});
+}
+
+SIM_Reconstructor::TimerScope::TimerScope(SIM_Reconstructor* r) : prev(kernel_timer())
+{
+  r->ktimer_.r = r;
+  set_kernel_timer(r->profiling_ ? &r->ktimer_ : nullptr);
+}
+
+SIM_Reconstructor::TimerScope::~TimerScope() { set_kernel_timer(prev); }
+
+std::string SIM_Reconstructor::profile_json()
+{
+  cudaStreamSynchronize(stream_);
+  for (auto& pd : pending_) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, pd.a, pd.b);
+    if (pd.kernel) {
+      auto& e = kprof_[pd.stage];
+      e.ms += ms;
+      e.launches += pd.launches;
+      e.bytes += pd.bytes;
+    } else {
+      auto& e = prof_[pd.stage];
+      e.first += ms;
+      e.second += pd.launches;
+    }
+    cudaEventDestroy(pd.a);
+    cudaEventDestroy(pd.b);
+  }
+  pending_.clear();
+  std::ostringstream s;
+  s.precision(9);
+  s << "{\"stages\": {";
+  bool first = true;
+  for (auto& kv : prof_) {
+    if (!first) s << ", ";
+    first = false;
+    s << "\"" << kv.first << "\": {\"ms\": " << kv.second.first << ", \"launches\": " << kv.second.second << "}";
+  }
+  s << "}, \"kernels\": {";
+  first = true;
+  for (auto& kv : kprof_) {
+    if (!first) s << ", ";
+    first = false;
+    s << "\"" << kv.first << "\": {\"ms\": " << kv.second.ms << ", \"launches\": " << kv.second.launches
+      << ", \"alg_bytes\": " << kv.second.bytes << "}";
+  }
+  s << "}}";
+  return s.str();
+}
+
+void SIM_Reconstructor::reset_profile()
+{
+  profile_json();
+  prof_.clear();
+  kprof_.clear();
+}
+
+// -------------------------------------------------------------- ingestion
+void SIM_Reconstructor::stage_raw(const void* raw, bool u16)
+{
+  const size_t n = (size_t)nimg_ * nx_ * ny_;
+  raw_u16_ = u16;
+  check(cudaMemcpyAsync(d_raw_, raw, n * (u16 ? 2 : 4), cudaMemcpyHostToDevice, stream_), "raw upload");
+  have_raw_ = true;
+  ingest();
+}
+
+void SIM_Reconstructor::ingest()
+{
+  TimerScope ts(this);
+  cudaEvent_t a;
+  long long l0;
+  stage_begin("ingest", &a, &l0);
+  IngestArgs ia{};
+  ia.raw = d_raw_;
+  ia.raw_is_u16 = raw_u16_;
+  ia.nx = nx_;
+  ia.ny = ny_;
+  ia.nz = nz_;
+  ia.ndirs = ndirs_;
+  ia.nphases = nph_;
+  ia.fastSI = opt.p.bFastSIM;
+  ia.bg = nullptr;
+  ia.slope = nullptr;
+  ia.bgconst = opt.p.constbkgd;
+  ia.bgextra = 0.f;
+  ia.inscale = opt.ip.inscale;
+  ia.napodize = opt.p.napodize;
+  ia.apofact = d_apofact_;
+  ia.spec = d_spec_;
+  check_launch(launch_ingest(ia, stream_, &launches_), "ingest");
+  stage_end("ingest", a, l0);
+  // processOneVolume without loadAndRescaleImage uses unit ratios
+  std::vector<float> ones((size_t)ndirs_ * nph_ * nz_, 1.0f);
+  check(cudaMemcpyAsync(d_scale_, ones.data(), ones.size() * sizeof(float), cudaMemcpyHostToDevice, stream_),
+        "scale init");
+  check(cudaStreamSynchronize(stream_), "ingest");
+  rescaled_ = false;
+}
+
+void SIM_Reconstructor::set_raw_float(const float* raw, int nx, int ny, int nz)
+{
+  if (nx != nx_ || ny != ny_ || nz != nimg_)
+    throw std::runtime_error("setRaw: shape does not match the reconstructor");
+  stage_raw(raw, false);
+}
+
+void SIM_Reconstructor::set_raw_u16(const uint16_t* raw, int nx, int ny, int nz)
+{
+  if (nx != nx_ || ny != ny_ || nz != nimg_)
+    throw std::runtime_error("setRaw: shape does not match the reconstructor");
+  stage_raw(raw, true);
+}
+
+// loadAndRescaleImage -> rescaleDriver (cudaSirecon.cpp:520-540, 1323-1329)
+void SIM_Reconstructor::load_and_rescale(int it, int iw)
+{
+  TimerScope ts(this);
+  (void)iw;
+  if (!have_raw_) throw std::runtime_error("loadAndRescaleImage before setRaw/setFile");
+  if (!opt.p.do_rescale) return;
+  cudaEvent_t a;
+  long long l0;
+  stage_begin("rescale", &a, &l0);
+  check_launch(launch_rescale(d_spec_, nx_, ny_, nz_, ndirs_, nph_, it, opt.p.equalizez, opt.p.equalizet, d_sdp0_,
+                              d_scale_, stream_, &launches_),
+               "rescale");
+  stage_end("rescale", a, l0);
+  rescaled_ = true;
+}
+
+void SIM_Reconstructor::separate()
+{
+  TimerScope ts(this);
+  cudaEvent_t a;
+  long long l0;
+  stage_begin("separate", &a, &l0);
+  check_launch(launch_separate(d_spec_, d_scale_, d_sepmat_, nx_, ny_, nz_, ndirs_, nph_, stream_, &launches_),
+               "separate");
+  stage_end("separate", a, l0);
+}
+
+// ------------------------------------------------------------------ fitting
+void SIM_Reconstructor::build_overlaps(int d, int o1, int o2, float k0x, float k0y)
+{
+  const ReconParams& p = opt.p;
+  const ImageParams& ip = opt.ip;
+  OverlapArgs a{};
+  a.bands = d_spec_ + (size_t)d * nph_ * nz_ * ny_ * nxh_;
+  a.nx = nx_;
+  a.ny = ny_;
+  a.nz = nz_;
+  a.order1 = o1;
+  a.order2 = o2;
+  // makeoverlaps scalars, gpuFunctionsImpl.cu:497-555 (float arithmetic)
+  float order0_2_factor = 1.0f;
+  if (nz_ > 1) order0_2_factor = 5.0f;
+  float dxy = ip.dxy;
+  float dkx = 1.0f / (nx_ * dxy);
+  float dky = 1.0f / (ny_ * dxy);
+  float dkz = ip.dz > 0.0f ? 1.0f / (nz_ * ip.dz) : p.dkzotf;
+  float kzscale = dkz / p.dkzotf;
+  float rdistcutoff = p.na * 2.0 / (ip.wave[0] * 0.001);
+  if (rdistcutoff > 1. / (2. * dxy)) rdistcutoff = 1. / (2. * dxy);
+  a.kx = k0x * (o2 - o1);
+  a.ky = k0y * (o2 - o1);
+  a.dkx = dkx;
+  a.dky = dky;
+  a.rdistcutoff = rdistcutoff;
+  a.otfcutoff = p.otfcutoff;
+  a.order0_2_factor = order0_2_factor;
+  a.zdc = zdc_ovl_;
+  a.nokz0 = effective_nokz0(opt);
+  const int dir_ = p.bOneOTFperAngle ? d : 0;
+  for (int o = 0; o < norders_; ++o)
+    a.otf.otf[o] = d_otf_ + ((size_t)dir_ * norders_ + o) * p.nxotf * p.nzotf;
+  a.otf.nzotf = p.nzotf;
+  a.otf.nxotf = p.nxotf;
+  a.otf.dkrotf = p.dkrotf;
+  a.otf.kzscale = kzscale;
+  a.ovl = d_ovl_;
+  a.ppart = d_ppart_;
+  a.sums = d_sums_;
+  a.pmap = d_pmap_;
+  a.sumxy = d_sumxy_;
+  check_launch(launch_overlaps(a, stream_, &launches_), "makeoverlaps");
+  cur_o1_ = o1;
+  cur_o2_ = o2;
+  cache_.clear();
+  sumx_ = sumy_ = -1;
+}
+
+// XStarY for a batch of (angle, mag) candidates, cached as modamp1 = XStarY/sumX
+void SIM_Reconstructor::eval_candidates(int o1, int o2, const std::vector<std::pair<float, float>>& cands)
+{
+  std::vector<std::pair<float, float>> todo;
+  for (auto& c : cands)
+    if (!cache_.count({fbits(c.first), fbits(c.second)})) todo.push_back(c);
+  for (size_t b0 = 0; b0 < todo.size(); b0 += kMaxCand) {
+    size_t nc = std::min<size_t>(kMaxCand, todo.size() - b0);
+    std::vector<float2> kc(nc);
+    for (size_t i = 0; i < nc; ++i) {
+      float angle = todo[b0 + i].first, mag = todo[b0 + i].second;
+      // getmodamp: k1 = klength*(cosf, sinf)(kangle); findrealspacemodamp: k1*(order2-order1)
+      float k1x = mag * cosf(angle), k1y = mag * sinf(angle);
+      kc[i] = make_float2(k1x * (o2 - o1), k1y * (o2 - o1));
+    }
+    check(cudaMemcpyAsync(d_kcand_, kc.data(), nc * sizeof(float2), cudaMemcpyHostToDevice, stream_), "cand");
+    check_launch(launch_modamp_candidates(d_pmap_, nx_, ny_, opt.ip.dxy, d_kcand_, (int)nc, d_tables_, d_partial_,
+                                          d_xstary_, stream_, &launches_),
+                 "modamp");
+    check(cudaMemcpyAsync(h_pinned_, d_xstary_, nc * 2 * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
+    check(cudaMemcpyAsync(h_pinned_ + 2 * kMaxCand, d_sumxy_, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream_),
+          "d2h");
+    check(cudaStreamSynchronize(stream_), "modamp");
+    sumx_ = h_pinned_[2 * kMaxCand];
+    sumy_ = h_pinned_[2 * kMaxCand + 1];
+    float sx = (float)sumx_;
+    for (size_t i = 0; i < nc; ++i) {
+      float xr = (float)h_pinned_[2 * i], xi = (float)h_pinned_[2 * i + 1];
+      cache_[{fbits(todo[b0 + i].first), fbits(todo[b0 + i].second)}] = float2v{xr / sx, xi / sx};
+    }
+  }
+}
+
+// getmodamp (gpuFunctionsImpl.cu:1046-1072); redo rebuilds the overlaps at k1
+float SIM_Reconstructor::getmodamp(int d, float angle, float mag, int o1, int o2, int redo, float2v* modamp)
+{
+  if (redo || o1 != cur_o1_ || o2 != cur_o2_) {
+    float k1x = mag * cosf(angle), k1y = mag * sinf(angle);
+    build_overlaps(d, o1, o2, k1x, k1y);
+  }
+  auto key = std::make_pair(fbits(angle), fbits(mag));
+  if (!cache_.count(key)) eval_candidates(o1, o2, {{angle, mag}});
+  float2v m = cache_[key];
+  if (modamp) *modamp = m;
+  return m.x * m.x + m.y * m.y;
+}
+
+// queue `count` candidates along the search line (float-accumulated steps,
+// exactly the values the sequential search would visit)
+void SIM_Reconstructor::prefetch_line(int o1, int o2, bool angle_axis, float fixed, float start, float step,
+                                      int count, int dir)
+{
+  std::vector<std::pair<float, float>> c;
+  float x = start;
+  for (int i = 0; i < count; ++i) {
+    x = dir > 0 ? x + step : x - step;
+    c.push_back(angle_axis ? std::make_pair(x, fixed) : std::make_pair(fixed, x));
+  }
+  eval_candidates(o1, o2, c);
+}
+
+// findrealspacemodamp (gpuFunctionsImpl.cu:1074-1148): modamp1 at k0
+float2v SIM_Reconstructor::findrealspacemodamp(int d, int o1, int o2, float k0x, float k0y, int redo)
+{
+  if (redo || o1 != cur_o1_ || o2 != cur_o2_) build_overlaps(d, o1, o2, k0x, k0y);
+  // the candidate kernel takes (angle, mag) pairs; pass k0 through an exact
+  // (angle, mag) key by evaluating directly
+  std::vector<float2> kc = {make_float2(k0x * (o2 - o1), k0y * (o2 - o1))};
+  check(cudaMemcpyAsync(d_kcand_, kc.data(), sizeof(float2), cudaMemcpyHostToDevice, stream_), "cand");
+  check_launch(launch_modamp_candidates(d_pmap_, nx_, ny_, opt.ip.dxy, d_kcand_, 1, d_tables_, d_partial_,
+                                        d_xstary_, stream_, &launches_),
+               "modamp");
+  check(cudaMemcpyAsync(h_pinned_, d_xstary_, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
+  check(cudaMemcpyAsync(h_pinned_ + 2, d_sumxy_, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
+  check(cudaStreamSynchronize(stream_), "modamp");
+  float sx = (float)h_pinned_[2];
+  return float2v{(float)h_pinned_[0] / sx, (float)h_pinned_[1] / sx};
+}
+
+// findk0 (gpuFunctionsImpl.cu:306-372)
+void SIM_Reconstructor::findk0(int d)
+{
+  const int fitorder2 = nz_ > 1 ? 2 : 1;
+  float2v k0 = k0_[d];
+  build_overlaps(d, 0, fitorder2, k0.x, k0.y);
+  check_launch(launch_crosscorr_peak(d_pmap_, d_cc_, nx_, ny_, d_bval_, d_bidx_, d_peak_, stream_, &launches_),
+               "crosscorr");
+  float* pk = (float*)(h_pinned_ + 256);
+  check(cudaMemcpyAsync(pk, d_peak_, 7 * sizeof(float), cudaMemcpyDeviceToHost, stream_), "d2h");
+  check(cudaStreamSynchronize(stream_), "findk0");
+  int xcent = (int)pk[0], ycent = (int)pk[1];
+  float peakx = fitparabola(pk[2], pk[3], pk[4]) + xcent;
+  float peaky = fitparabola(pk[5], pk[3], pk[6]) + ycent;
+  float dxy = opt.ip.dxy;
+  float dkx = 1 / (nx_ * dxy);
+  float dky = 1 / (ny_ * dxy);
+  if (k0.x / dkx < peakx - nx_ / 2) peakx -= nx_;
+  if (k0.x / dkx > peakx + nx_ / 2) peakx += nx_;
+  if (k0.y / dky < peaky - ny_ / 2) peaky -= ny_;
+  if (k0.y / dky > peaky + ny_ / 2) peaky += ny_;
+  k0_[d].x = peakx * (dkx / fitorder2);
+  k0_[d].y = peaky * (dky / fitorder2);
+}
+
+// fitk0andmodamps (gpuFunctionsImpl.cu:874-1020).  The search visits the same
+// float-accumulated angles and magnitudes as the reference; their modamps are
+// evaluated in batches on the device and the sequential logic reads them
+// from a cache.
+void SIM_Reconstructor::fitk0andmodamps(int d)
+{
+  ReconParams& p = opt.p;
+  const int fitorder1 = 0;
+  const int fitorder2 = nz_ > 1 ? 2 : 1;
+  float2v* k0 = &k0_[d];
+  float k0mag = sqrt(k0->x * k0->x + k0->y * k0->y);
+  float k0angle = atan2(k0->y, k0->x);
+  int redoarrays = (p.recalcarrays >= 1);
+  float x2 = k0angle;
+  float2v modamp;
+  float amp2 = getmodamp(d, k0angle, k0mag, fitorder1, fitorder2, redoarrays, &modamp);
+  redoarrays = (p.recalcarrays >= 3);
+  float deltaangle = 0.001;
+  float deltamag = 0.1 / (std::max(nx_, ny_) * opt.ip.dxy);
+  const int K = 12;
+  // both directions of the angle search in one batch
+  prefetch_line(fitorder1, fitorder2, true, k0mag, k0angle, deltaangle, K, +1);
+  prefetch_line(fitorder1, fitorder2, true, k0mag, k0angle, deltaangle, K, -1);
+  float angle = k0angle + deltaangle;
+  float x3 = angle;
+  float amp3 = getmodamp(d, angle, k0mag, fitorder1, fitorder2, redoarrays, &modamp);
+  float amp1 = 0, x1 = 0.0, a;
+  int steps = 0;
+  if (amp3 > amp2) {
+    while (amp3 > amp2) {
+      amp1 = amp2;
+      x1 = x2;
+      amp2 = amp3;
+      x2 = x3;
+      angle += deltaangle;
+      x3 = angle;
+      if (++steps % K == K - 1) prefetch_line(fitorder1, fitorder2, true, k0mag, angle, deltaangle, K, +1);
+      amp3 = getmodamp(d, angle, k0mag, fitorder1, fitorder2, redoarrays, &modamp);
+    }
+  } else {
+    angle = k0angle;
+    a = amp3;
+    amp3 = amp2;
+    amp2 = a;
+    a = x3;
+    x3 = x2;
+    x2 = a;
+    while (amp3 > amp2) {
+      amp1 = amp2;
+      x1 = x2;
+      amp2 = amp3;
+      x2 = x3;
+      angle -= deltaangle;
+      x3 = angle;
+      if (++steps % K == K - 1) prefetch_line(fitorder1, fitorder2, true, k0mag, angle, deltaangle, K, -1);
+      amp3 = getmodamp(d, angle, k0mag, fitorder1, fitorder2, redoarrays, &modamp);
+    }
+  }
+  angle = fitxyparabola(x1, amp1, x2, amp2, x3, amp3);
+
+  x2 = k0mag;
+  // magnitude search at the fitted angle
+  std::vector<std::pair<float, float>> first = {{angle, k0mag}};
+  eval_candidates(fitorder1, fitorder2, first);
+  prefetch_line(fitorder1, fitorder2, false, angle, k0mag, deltamag, K, +1);
+  prefetch_line(fitorder1, fitorder2, false, angle, k0mag, deltamag, K, -1);
+  amp2 = getmodamp(d, angle, k0mag, fitorder1, fitorder2, redoarrays, &modamp);
+  float mag = k0mag + deltamag;
+  x3 = mag;
+  amp3 = getmodamp(d, angle, mag, fitorder1, fitorder2, redoarrays, &modamp);
+  steps = 0;
+  if (amp3 > amp2) {
+    while (amp3 > amp2) {
+      amp1 = amp2;
+      x1 = x2;
+      amp2 = amp3;
+      x2 = x3;
+      mag += deltamag;
+      x3 = mag;
+      if (++steps % K == K - 1) prefetch_line(fitorder1, fitorder2, false, angle, mag, deltamag, K, +1);
+      amp3 = getmodamp(d, angle, mag, fitorder1, fitorder2, redoarrays, &modamp);
+    }
+  } else {
+    mag = k0mag;
+    a = amp3;
+    amp3 = amp2;
+    amp2 = a;
+    a = x3;
+    x3 = x2;
+    x2 = a;
+    while (amp3 > amp2) {
+      amp1 = amp2;
+      x1 = x2;
+      amp2 = amp3;
+      x2 = x3;
+      mag -= deltamag;
+      x3 = mag;
+      if (++steps % K == K - 1) prefetch_line(fitorder1, fitorder2, false, angle, mag, deltamag, K, -1);
+      amp3 = getmodamp(d, angle, mag, fitorder1, fitorder2, redoarrays, &modamp);
+    }
+  }
+  mag = fitxyparabola(x1, amp1, x2, amp2, x3, amp3);
+
+  redoarrays = (p.recalcarrays >= 2);
+  getmodamp(d, angle, mag, fitorder1, fitorder2, redoarrays, &modamp);
+  k0->x = mag * cosf(angle);
+  k0->y = mag * sinf(angle);
+  amp_[d][fitorder2] = modamp;
+  redoarrays = 1;
+  if (nz_ == 1) {
+    for (int order = 2; order < norders_; ++order) {
+      getmodamp(d, angle, mag, order - 1, order, redoarrays, &modamp);
+      amp_[d][order] = modamp;
+    }
+  } else {
+    for (int order = 1; order < norders_; ++order) {
+      if (order != fitorder2) {
+        getmodamp(d, angle, mag, 0, order, redoarrays, &modamp);
+        amp_[d][order] = modamp;
+      }
+    }
+  }
+}
+
+static float2v cmulh(float2v a, float2v b) { return float2v{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+static float cmagh(float2v a) { return sqrt(a.x * a.x + a.y * a.y); }
+
+// findModulationVectorsAndPhasesForAllDirections, k0 / modamp part
+// (cudaSirecon.cpp:296-493)
+void SIM_Reconstructor::fit_direction(int direction)
+{
+  ReconParams& p = opt.p;
+  const ImageParams& ip = opt.ip;
+  const bool reuse = ip.ntimes > 1 && ip.curTimeIdx > 0 && p.bUseTime0k0;
+  if (!reuse) k0_[direction] = k0guess_[direction];
+  cur_o1_ = cur_o2_ = -1;  // overlaps belong to another direction
+  if (p.bSearchforvector && !reuse) {
+    findk0(direction);
+    p.recalcarrays = 1;
+    fitk0andmodamps(direction);
+    if (ip.curTimeIdx == 0) k0_time0_[direction] = k0_[direction];
+    float dx = k0_[direction].x - k0guess_[direction].x, dy = k0_[direction].y - k0guess_[direction].y;
+    float dist = sqrt(dx * dx + dy * dy);
+    if (ip.ntimes > 1 && ip.curTimeIdx > 0 && dist > 2 * kK0WarningThresh) {
+      k0_[direction] = k0_time0_[direction];
+      for (int order = 1; order < norders_; ++order) {
+        int o1 = nz_ > 1 ? 0 : order - 1;
+        amp_[direction][order] = findrealspacemodamp(direction, o1, order, k0_[direction].x, k0_[direction].y, 1);
+      }
+    }
+  } else {
+    for (int order = 1; order < norders_; ++order)
+      amp_[direction][order] = findrealspacemodamp(direction, 0, order, k0_[direction].x, k0_[direction].y, 1);
+  }
+  if (ip.nz == 1)
+    for (int order = 2; order < norders_; ++order)
+      amp_[direction][order] = cmulh(amp_[direction][order], amp_[direction][order - 1]);
+  if (p.forceamp.size() > 0 && p.forceamp[0] > 0.0) {
+    for (int order = 1; order < norders_; ++order) {
+      float a = cmagh(amp_[direction][order]);
+      float want = (size_t)(order - 1) < p.forceamp.size() ? p.forceamp[order - 1] : 0.f;
+      if (a < want) {
+        float ampfact = want / a;
+        amp_[direction][order].x *= ampfact;
+        amp_[direction][order].y *= ampfact;
+      }
+    }
+  }
+  if (!p.bFitallphases) {
+    float base_phase = atan2(amp_[direction][1].y, amp_[direction][1].x);
+    for (int order = 2; order < norders_; ++order) {
+      float2v amplitude{cmagh(amp_[direction][order]), 0};
+      float phi = order * base_phase;
+      float2v expiphi{cosf(phi), sinf(phi)};
+      amp_[direction][order] = cmulh(amplitude, expiphi);
+    }
+  }
+}
+
+void SIM_Reconstructor::fit_all()
+{
+  TimerScope ts(this);
+  cudaEvent_t a;
+  long long l0;
+  stage_begin("fit", &a, &l0);
+  for (int d = 0; d < ndirs_; ++d) fit_direction(d);
+  stage_end("fit", a, l0);
+}
+
+// ------------------------------------------------------ filter + assembly
+void SIM_Reconstructor::filter_and_assemble()
+{
+  TimerScope ts(this);
+  const ReconParams& p = opt.p;
+  const ImageParams& ip = opt.ip;
+  cudaEvent_t ev;
+  long long l0;
+  stage_begin("filter", &ev, &l0);
+  // filterbands scalars (gpuFunctionsImpl.cu:1222-1298), float arithmetic
+  FilterArgs fa{};
+  fa.ndirs = ndirs_;
+  fa.norders = norders_;
+  fa.nx = nx_;
+  fa.ny = ny_;
+  fa.nz = nz_;
+  float dxy = ip.dxy;
+  float dkz = ip.dz > 0 ? (1 / (nz_ * ip.dz)) : p.dkzotf;
+  float kzscale = dkz / p.dkzotf;
+  float k0mag = sqrt(k0_[0].x * k0_[0].x + k0_[0].y * k0_[0].y);
+  float lambdaem = (ip.wave[0] / p.nimm) / 1000.0;
+  float lambdaexc = 0.88 * lambdaem;
+  float alpha = asinf(p.na / p.nimm);
+  float rdistcutoff = (p.na * 2 / (ip.wave[0] / 1000.0));
+  if (rdistcutoff > 1. / (2. * dxy)) rdistcutoff = 1. / (2. * dxy);
+  int zdc[kMaxOrders] = {0};
+  zdc[0] = (int)ceil(((1 - cosf(alpha)) / lambdaem) / dkz);
+  zdc[norders_ - 1] = 1.3 * zdc[0];
+  if (norders_ >= 3)
+    for (int order = 1; order < norders_ - 1; order++) zdc[order] = (1 + lambdaem / lambdaexc) * zdc[0];
+  for (int order = 0; order < norders_; order++)
+    if (zdc[order] >= nz_ / 2) zdc[order] = ((nz_ / 2 - 1) > 0 ? (nz_ / 2 - 1) : 0);
+  float apocutoff = rdistcutoff + k0mag * (norders_ - 1);
+  float zapocutoff = norders_ > 1 ? zdc[1] : 0;
+  fa.dkx = 1. / (nx_ * dxy);
+  fa.dky = 1. / (ny_ * dxy);
+  fa.rdistcutoff = rdistcutoff;
+  fa.apocutoff = apocutoff;
+  fa.zapocutoff = zapocutoff;
+  fa.wiener2 = p.wiener * p.wiener;
+  for (int o = 0; o < norders_; ++o) fa.zdc[o] = zdc[o];
+  for (int d = 0; d < ndirs_; ++d) {
+    fa.k0[d] = make_float2(k0_[d].x, k0_[d].y);
+    for (int o = 0; o < norders_; ++o) {
+      fa.ampmag2[d * norders_ + o] = amp_[d][o].x * amp_[d][o].x + amp_[d][o].y * amp_[d][o].y;
+      fa.noisevar[d * norders_ + o] = noisevar_[d * norders_ + o];
+    }
+  }
+  fa.suppress = p.bSuppress_singularities;
+  fa.supp_radius = p.suppression_radius;
+  fa.dampen0 = p.bDampenOrder0;
+  fa.nokz0 = effective_nokz0(opt);
+  fa.filteroverlaps = p.bFilteroverlaps;
+  fa.apodizeoutput = p.apodizeoutput;
+  fa.bessel = 0;
+  fa.otf.nzotf = p.nzotf;
+  fa.otf.nxotf = p.nxotf;
+  fa.otf.dkrotf = p.dkrotf;
+  fa.otf.kzscale = kzscale;
+  for (int d = 0; d < ndirs_; ++d) {
+    const int dir_ = p.bOneOTFperAngle ? d : 0;
+    for (int o = 0; o < norders_; ++o)
+      fa.otf.otf[o] = d_otf_ + ((size_t)dir_ * norders_ + o) * p.nxotf * p.nzotf;
+    fa.dir = d;
+    fa.bands = d_spec_ + (size_t)d * nph_ * nz_ * ny_ * nxh_;
+    for (int o = 0; o < norders_; ++o) fa.conjamp[o] = make_float2(amp_[d][o].x, -amp_[d][o].y);
+    check_launch(launch_filter(fa, stream_, &launches_), "filterbands");
+  }
+  stage_end("filter", ev, l0);
+
+  stage_begin("assemble", &ev, &l0);
+  std::vector<float2> k0h(kMaxDirs, make_float2(0, 0));
+  for (int d = 0; d < ndirs_; ++d) k0h[d] = make_float2(k0_[d].x, k0_[d].y);
+  check(cudaMemcpyAsync(d_k0_, k0h.data(), kMaxDirs * sizeof(float2), cudaMemcpyHostToDevice, stream_), "k0");
+  float fact = p.explodefact / 0.5;
+  check_launch(launch_ramp_tables(d_k0_, ndirs_, norders_, X_, Y_, dxy / p.zoomfact, fact, d_ex_, d_ey_, stream_,
+                                  &launches_),
+               "ramp");
+  AssembleArgs aa{};
+  aa.bands = d_spec_;
+  aa.ndirs = ndirs_;
+  aa.norders = norders_;
+  aa.nphases = nph_;
+  aa.nx = nx_;
+  aa.ny = ny_;
+  aa.nz = nz_;
+  aa.X = X_;
+  aa.Y = Y_;
+  aa.Z = Z_;
+  for (int o = 0; o < norders_; ++o) aa.zdc[o] = zdc[o];
+  aa.ex = d_ex_;
+  aa.ey = d_ey_;
+  aa.T = d_T_;
+  aa.tcap = tcap_;
+  aa.S = d_S_;
+  aa.out = d_out_;
+  check_launch(launch_assemble(aa, stream_, &launches_), "assemble");
+  stage_end("assemble", ev, l0);
+}
+
+// processOneVolume (cudaSirecon.cpp:1264-1321)
+int SIM_Reconstructor::process_one_volume()
+{
+  if (!have_raw_) throw std::runtime_error("processOneVolume before setRaw/setFile");
+  separate();
+  fit_all();
+  filter_and_assemble();
+  check(cudaStreamSynchronize(stream_), "processOneVolume");
+  have_raw_ = false;  // the bands are consumed (filtered in place)
+  return 1;
+}
+
+int SIM_Reconstructor::prepare()
+{
+  if (!have_raw_) throw std::runtime_error("prepare before setRaw");
+  separate();
+  check(cudaStreamSynchronize(stream_), "prepare");
+  have_raw_ = false;
+  return 0;
+}
+
+int SIM_Reconstructor::get_band(int dir, int b, float* out)
+{
+  if (dir < 0 || dir >= ndirs_ || b < 0 || b >= nph_) throw std::runtime_error("getBand: index out of range");
+  const size_t n = (size_t)nz_ * ny_ * nxh_;
+  check(cudaMemcpyAsync(out, d_spec_ + ((size_t)dir * nph_ + b) * n, n * sizeof(float2), cudaMemcpyDeviceToHost,
+                        stream_),
+        "getBand");
+  check(cudaStreamSynchronize(stream_), "getBand");
+  return 0;
+}
+
+void SIM_Reconstructor::get_fit(float* k0, float* amps) const
+{
+  for (int d = 0; d < ndirs_; ++d) {
+    if (k0) {
+      k0[2 * d] = k0_[d].x;
+      k0[2 * d + 1] = k0_[d].y;
+    }
+    if (amps)
+      for (int o = 0; o < norders_; ++o) {
+        amps[2 * (d * norders_ + o)] = amp_[d][o].x;
+        amps[2 * (d * norders_ + o) + 1] = amp_[d][o].y;
+      }
+  }
+}
+
+// getResult (cudaSirecon.cpp:1620-1634)
+void SIM_Reconstructor::get_result(float* out)
+{
+  check(cudaMemcpyAsync(out, d_out_, out_elems() * sizeof(float), cudaMemcpyDeviceToHost, stream_), "getResult");
+  check(cudaStreamSynchronize(stream_), "getResult");
+}
+
+double SIM_Reconstructor::bench_device(int steps)
+{
+  if (!d_flush_) {
+    flush_n_ = (size_t)64 << 20;  // 256 MiB of floats: twice the L2
+    check(cudaMalloc(&d_flush_, flush_n_ * sizeof(float)), "flush buffer");
+  }
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  double total = 0;
+  for (int s = 0; s < steps; ++s) {
+    check_launch(launch_fill(d_flush_, flush_n_, (float)s, stream_, nullptr), "flush");
+    cudaEventRecord(a, stream_);
+    have_raw_ = true;
+    ingest();
+    load_and_rescale(opt.ip.curTimeIdx, 0);
+    process_one_volume();
+    cudaEventRecord(b, stream_);
+    check(cudaEventSynchronize(b), "bench");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    total += ms;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  have_raw_ = true;
+  return total;
+}
+
+// ------------------------------------------------------------------ files
+// setFile (cudaSirecon.cpp:1337-1352)
+void SIM_Reconstructor::set_file(int it, int iw)
+{
+  std::string err;
+  if (opt.p.bTIFF) {
+    if (it < 0 || (size_t)it >= tiff_files_.size()) throw std::runtime_error("setFile: time index out of range");
+    Stack s;
+    if (!tiff_read(tiff_files_[it], &s, &err)) throw std::runtime_error(err);
+    if (s.width != nx_ || s.height != ny_ || s.depth != nimg_)
+      throw std::runtime_error("setFile: TIFF size differs from the first file");
+    stage_raw(s.data.data(), false);
+  } else {
+    // sections of time point it (single wave): nimg consecutive sections
+    std::vector<float> all((size_t)nimg_ * nx_ * ny_), sec;
+    for (int s = 0; s < nimg_; ++s) {
+      int idx = it * nimg_ * opt.ip.nwaves + iw * nimg_ + s;
+      if (!mrc_read_section(mrc_in_, idx, &sec, &err)) throw std::runtime_error(err);
+      memcpy(&all[(size_t)s * nx_ * ny_], sec.data(), (size_t)nx_ * ny_ * sizeof(float));
+    }
+    stage_raw(all.data(), false);
+  }
+}
+
+// writeResult (cudaSirecon.cpp:1636-1699)
+void SIM_Reconstructor::write_result(int it, int iw)
+{
+  std::vector<float> out(out_elems());
+  get_result(out.data());
+  std::string err;
+  if (opt.p.bTIFF) {
+    std::string path = output_path_for(tiff_files_[it], "_proc");
+    if (!tiff_write_float(path, out.data(), X_, Y_, Z_, &err)) throw std::runtime_error(err);
+  } else {
+    if (!mrc_out_) throw std::runtime_error("output file is not open");
+    float maxval = -FLT_MAX, minval = FLT_MAX;
+    const size_t plane = (size_t)X_ * Y_;
+    for (int z = 0; z < Z_; ++z) {
+      const float* ptr = out.data() + z * plane;
+      mrc_out_.write((const char*)ptr, plane * sizeof(float));
+      if (it == 0)
+        for (size_t j = 0; j < plane; ++j) {
+          // the reference's min/max update (cudaSirecon.cpp:1676-1680)
+          if (ptr[j] > maxval) maxval = ptr[j];
+          else if (ptr[j] < minval) minval = ptr[j];
+        }
+    }
+    if (it == 0 && iw == 0) {
+      out_hdr_.amin = minval;
+      out_hdr_.amax = maxval;
+    }
+  }
+}
+
+// closeFiles (cudaSirecon.cpp:1702-1713 and saveCommandLineToHeader, mrc.h:62-74)
+void SIM_Reconstructor::close_files()
+{
+  if (opt.p.bTIFF || !mrc_out_.is_open()) return;
+  if (opt.p.bWriteTitle) {
+    std::string titles;
+    for (size_t i = 3; i < argv_.size(); ++i) titles += argv_[i] + " ";
+    if (out_hdr_.nlab < 10) {
+      char* lab = out_hdr_.label[out_hdr_.nlab];
+      memset(lab, ' ', 80);
+      memcpy(lab, titles.data(), std::min<size_t>(80, titles.size()));
+      out_hdr_.nlab++;
+    }
+  }
+  mrc_out_.seekp(0);
+  mrc_out_.write((const char*)&out_hdr_, sizeof(MrcHeader));
+  mrc_out_.close();
+}

@@ -1,0 +1,173 @@
+// SIM_Reconstructor: the object behind the SR_* C ABI (the reference's
+// class of the same name, src/cudaSirecon/SIM_reconstructor.hpp:19-158),
+// rebuilt around device-resident buffers, one CUDA stream per handle and the
+// fused kernels of this library.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <complex>
+#include <fstream>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "image_io.h"
+#include "kernels.h"
+#include "params.h"
+
+struct float2v {
+  float x, y;
+};
+
+class SIM_Reconstructor {
+ public:
+  // construction paths (interface.cpp:13-17, 54-57)
+  static SIM_Reconstructor* from_shape(int nx, int ny, int nimages, const std::string& config, std::string* err);
+  static SIM_Reconstructor* from_argv(int argc, char** argv, std::string* err);
+  ~SIM_Reconstructor();
+
+  void set_raw_float(const float* raw, int nx, int ny, int nz);
+  void set_raw_u16(const uint16_t* raw, int nx, int ny, int nz);
+  void load_and_rescale(int it, int iw);
+  void set_cur_time(int it) { opt.ip.curTimeIdx = (unsigned short)it; }
+  int process_one_volume();
+  void get_result(float* out);
+  void set_file(int it, int iw);
+  void write_result(int it, int iw);
+  void close_files();
+  int ntimes() const { return opt.ip.ntimes; }
+
+  // introspection / performance
+  void get_fit(float* k0, float* amps) const;
+  int prepare();  // separate bands without fitting (for stage checks)
+  int get_band(int dir, int b, float* out);
+  double bench_device(int steps);
+  void set_profiling(bool on) { profiling_ = on; }
+  std::string profile_json();
+  void reset_profile();
+  long long launches() const { return launches_; }
+  size_t out_elems() const { return (size_t)X_ * Y_ * Z_; }
+
+  simrecon::Options opt;  // ReconParams + ImageParams live here (references handed out)
+
+ private:
+  SIM_Reconstructor() = default;
+  bool setup(int nx, int ny, int nimages, int nwaves, const simrecon::Stack* otf, std::string* err);
+  bool load_otf_tiff(const std::string& path, simrecon::Stack* out, std::string* err);
+  void stage_raw(const void* raw, bool u16);
+  void ingest();
+  void separate();
+  void fit_all();
+  void fit_direction(int d);
+  void filter_and_assemble();
+  void check(cudaError_t e, const char* what);
+  void check_launch(int rc, const char* what);
+
+  // fitting helpers (gpuFunctionsImpl.cu:306-1148 semantics)
+  void build_overlaps(int d, int o1, int o2, float k0x, float k0y);
+  // evaluate XStarY for candidate (angle, mag) pairs on the current overlaps
+  void eval_candidates(int o1, int o2, const std::vector<std::pair<float, float>>& cands);
+  float getmodamp(int d, float angle, float mag, int o1, int o2, int redo, float2v* modamp);
+  void findk0(int d);
+  void fitk0andmodamps(int d);
+  float2v findrealspacemodamp(int d, int o1, int o2, float k0x, float k0y, int redo);
+  void prefetch_line(int o1, int o2, bool angle_axis, float fixed, float start, float step, int count, int dir);
+
+  // geometry
+  int nx_ = 0, ny_ = 0, nz_ = 0, nxh_ = 0, nimg_ = 0, norders_ = 0, nph_ = 0, ndirs_ = 0;
+  int X_ = 0, Y_ = 0, Z_ = 0;
+  int ndirs_otf_ = 1;
+  int zdc_ovl_ = 0;  // makeoverlaps zdistcutoff
+  bool otf_dk_from_header_ = false;  // MRC OTF: dkr / dkz taken from its header
+  cudaStream_t stream_ = nullptr;
+  int device_ = 0;
+
+  // device arena
+  char* arena_ = nullptr;
+  size_t arena_bytes_ = 0;
+  void* d_raw_ = nullptr;
+  float2* d_spec_ = nullptr;
+  float* d_scale_ = nullptr;
+  double* d_sdp0_ = nullptr;
+  float* d_sepmat_ = nullptr;
+  float* d_apofact_ = nullptr;
+  float2* d_otf_ = nullptr;
+  float2* d_ovl_ = nullptr;
+  float2* d_ppart_ = nullptr;
+  double* d_sums_ = nullptr;
+  float2* d_pmap_ = nullptr;
+  double* d_sumxy_ = nullptr;
+  float2* d_cc_ = nullptr;
+  float* d_bval_ = nullptr;
+  int* d_bidx_ = nullptr;
+  float* d_peak_ = nullptr;
+  float2* d_kcand_ = nullptr;
+  float2* d_tables_ = nullptr;
+  double* d_partial_ = nullptr;
+  double* d_xstary_ = nullptr;
+  float2* d_k0_ = nullptr;
+  float2* d_ex_ = nullptr;
+  float2* d_ey_ = nullptr;
+  float2* d_T_ = nullptr;
+  size_t tcap_ = 0;
+  float2* d_S_ = nullptr;
+  float* d_out_ = nullptr;
+  float* d_flush_ = nullptr;
+  size_t flush_n_ = 0;
+  double* h_pinned_ = nullptr;  // small pinned host buffer for results of the fit
+
+  // host-side state (ReconData equivalents)
+  std::vector<float> sepmat_;
+  std::vector<float> noisevar_;
+  std::vector<float2v> k0_, k0_time0_, k0guess_;
+  std::vector<std::vector<float2v>> amp_;
+  bool raw_u16_ = false;
+  bool have_raw_ = false;
+  bool rescaled_ = false;
+  // overlap state for the candidate evaluator
+  int cur_o1_ = -1, cur_o2_ = -1;
+  double sumx_ = 0, sumy_ = 0;
+  std::map<std::pair<uint32_t, uint32_t>, float2v> cache_;
+  std::vector<std::complex<double>> xstary_;
+
+  // files
+  std::vector<std::string> tiff_files_;
+  simrecon::MrcFile mrc_in_;
+  std::string out_path_;
+  std::ofstream mrc_out_;
+  simrecon::MrcHeader out_hdr_{};
+  std::vector<float> host_raw_;
+  std::vector<std::string> argv_;
+
+  // profiling: stage events and, per kernel, events + algorithmic bytes
+  bool profiling_ = false;
+  struct Pending {
+    std::string stage;
+    cudaEvent_t a, b;
+    long long launches;
+    double bytes;
+    bool kernel;
+  };
+  std::vector<Pending> pending_;
+  std::map<std::string, std::pair<double, long long>> prof_;
+  struct KStat {
+    double ms = 0;
+    long long launches = 0;
+    double bytes = 0;
+  };
+  std::map<std::string, KStat> kprof_;
+  struct KTimer : simrecon::KernelTimer {
+    SIM_Reconstructor* r = nullptr;
+    cudaEvent_t cur = nullptr;
+    void begin(cudaStream_t s) override;
+    void end(const char* kernel, cudaStream_t s, double alg_bytes) override;
+  } ktimer_;
+  struct TimerScope {
+    simrecon::KernelTimer* prev;
+    explicit TimerScope(SIM_Reconstructor* r);
+    ~TimerScope();
+  };
+  long long launches_ = 0;
+  void stage_begin(const char* name, cudaEvent_t* a, long long* l0);
+  void stage_end(const char* name, cudaEvent_t a, long long l0);
+};

@@ -22,6 +22,7 @@ struct OTFView {
   float kzscale;
 };
 
+#ifdef __CUDACC__
 // Bilinear lookup in a rotationally averaged OTF (the interpolation of
 // dev_otfinterpolate, gpuFunctionsImpl.cu:1677-1715).  Indices are clamped
 // to the table so a lookup at the very edge of the support never reads past
@@ -65,5 +66,7 @@ __device__ __forceinline__ double block_sum_d(double v, double* scratch /* >= 32
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   return v;
 }
+
+#endif  // __CUDACC__
 
 }  // namespace simrecon
