@@ -1,0 +1,367 @@
+#!/usr/bin/env python
+"""Benchmark: SIM reconstruction throughput on one GB300.
+
+Workload (default): the time-series configuration -- 512 x 512 px x 48 z x
+15 images (3 angles x 5 phases, uint16) per time point, output 1024 x 1024 x
+48 float32; k0 is fitted at time 0 (untimed warm-up) and reused for the timed
+time points, modamps are re-fitted every time point.  A "step" is one time
+point through the whole hot path (ingest -> bleach correction -> band
+separation -> modamp fit -> Wiener filter -> assembly).  Metric: output
+Mvoxels/s.
+
+  value : steps x output voxels / device time with the raw stack already
+          resident in HBM (CUDA events on the library's stream, L2 flushed
+          between steps by writing 256 MiB).
+  e2e   : the same through the C ABI from pinned host memory:
+          SR_setRawU16 (H2D) -> SR_loadAndRescaleImage -> SR_setCurTimeIdx ->
+          SR_processOneVolume -> SR_getResult (D2H), host wall clock.
+
+--impl reference runs the reference's own CUDA build (gpuFunctionsImpl.cu +
+cuFFT, compiled from the reference sources by oracle/build_ref.py) through
+its SR_* flow on the same workload.
+
+Prints one JSON line (rank 0).  N>1 runs independent replicas (one process
+per GPU, weak scaling: each rank reconstructs its own time points).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (nx, ny, nz, description)
+    "timeseries_512x512x48": (512, 512, 48, "512x512x48x15 uint16 per time point, k0 fitted at t=0 and reused"),
+    "plain_256x256x32": (256, 256, 32, "256x256x32x15 uint16 single volume, k0 search on every step"),
+}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return rank, world, local, dist
+    return rank, world, local, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 100 ms while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload(nx, ny, nz, nvol, seed=5):
+    """Seeded synthetic time points (drift 0.2 px/frame, 1 %/frame bleaching)."""
+    from cudasirecon_gb300 import synthetic as syn
+    o = syn.Optics()
+    vols = []
+    for t in range(nvol):
+        a = syn.simulate(nx, ny, nz, o, seed=seed, drift_px=0.2 * t, bleach=0.99 ** t, noise_seed=1000 + t,
+                         scene_seed=seed, mod_seed=seed + 1)
+        vols.append(a.raw)
+    otf = syn.ra_otf(o, nx_psf=128, nz_psf=64)
+    return vols, otf, syn.config_text(o)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary (or None)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            return json.load(f).get(kernel)
+    except Exception:
+        return None
+
+
+def cpu_baseline(vol, otf, cfg, nx, ny, nz):
+    """FP64 oracle on a bounded sample: a 128 x 128 lateral crop of the same stack."""
+    import warnings
+    from oracle.sirecon_oracle import SIMReconOracle
+    c = 128
+    crop = vol.reshape(3, nz, 5, ny, nx)[:, :, :, :c, :c].reshape(-1, c, c)
+    t = time.perf_counter()
+    o = SIMReconOracle(c, c, crop.shape[0], cfg, otf)
+    o.set_raw(crop)
+    o.load_and_rescale(0)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        o.process()
+    dt = time.perf_counter() - t
+    outvox = o.result.size
+    return {"value": outvox / dt / 1e6, "unit": "Mvoxels/s", "cores": 1, "kind": "port",
+            "sample": f"FP64 numpy restatement, full pipeline incl. k0 search, on a {c}x{c}x{nz}x15 lateral crop "
+                      f"of the workload ({dt:.1f} s)"}
+
+
+def run_gb300(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
+    import cudasirecon_gb300 as sr
+    sr.load_library()
+    nimg = vols[0].shape[0]
+    r = sr.Reconstructor(nx, ny, nimg, cfg, otf)
+    r.set_ntimes(1 << 14)
+    # time 0: k0 search (untimed)
+    r.set_raw(vols[0])
+    r.load_and_rescale(0, 0)
+    r.set_cur_time(0)
+    r.process()
+    reuse = args.workload.startswith("timeseries")
+    t_idx = 1 if reuse else 0
+    # ---- device-resident value
+    r.set_raw(vols[1 % len(vols)])
+    r.set_cur_time(t_idx)
+    r.bench_device(args.warmup)
+    r.set_profiling(True)
+    r.reset_profile()
+    l0 = r.kernel_launches()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    barrier(dist)
+    dev_ms = r.bench_device(args.steps)
+    barrier(dist)
+    clk = clocks.stop()
+    launches = r.kernel_launches() - l0
+    prof = r.profile()
+    r.set_profiling(False)
+    dev_ms = max_over_ranks(dist, dev_ms)
+    value = world * args.steps * outvox / (dev_ms / 1e3) / 1e6
+    # ---- end to end through the C ABI from pinned host memory
+    host = [np.ascontiguousarray(v) for v in vols]
+    out = np.empty(r.out_shape, np.float32)
+    for h in host:
+        sr.pin(h)
+    sr.pin(out)
+    for i in range(args.warmup):
+        r.set_raw(host[i % len(host)])
+        r.load_and_rescale(t_idx, 0)
+        r.set_cur_time(t_idx)
+        r.process()
+        r.result(out)
+    barrier(dist)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        r.set_raw(host[i % len(host)])
+        r.load_and_rescale(t_idx, 0)
+        r.set_cur_time(t_idx)
+        r.process()
+        r.result(out)
+    barrier(dist)
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    for h in host:
+        sr.unpin(h)
+    sr.unpin(out)
+    e2e = world * args.steps * outvox / e2e_s / 1e6
+    # ---- roofline of the dominant kernel
+    kern = prof.get("kernels", {})
+    top = max(kern.items(), key=lambda kv: kv[1]["ms"]) if kern else None
+    peak, peak_kind = peaks()
+    roof = None
+    if top:
+        name, st = top
+        ach = st["alg_bytes"] / (st["ms"] / 1e3) / 1e9
+        tr = ncu_traffic(name)
+        roof = {"kernel": name, "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(ach / peak, 4), "peak_source": peak_kind,
+                "traffic": tr, "alg_bytes_per_launch": st["alg_bytes"] / max(1, st["launches"]),
+                "avg_launch_ms": st["ms"] / max(1, st["launches"]),
+                "share_of_step": round(st["ms"] / max(dev_ms, 1e-9), 4)}
+    line = {
+        "metric": "Recon output Mvoxels/s (SIM 3-beam, 512x512x48x15 -> 1024x1024x48)",
+        "value": round(value, 1), "unit": "Mvoxels/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded beads+filaments, "
+        "widefield PSF, Poisson noise)",
+        "config": {"workload": args.workload, "nx": nx, "ny": ny, "nz": nz, "images_per_volume": nimg,
+                   "output": list(r.out_shape), "k0": "fitted at t=0, reused" if reuse else "searched every step",
+                   "l2": "flushed between steps (256 MiB write); raw stack 377 MB > L2",
+                   "description": WORKLOADS[args.workload][3]},
+        "e2e": {"value": round(e2e, 1), "unit": "Mvoxels/s",
+                "h2d_bytes_per_step": int(host[0].nbytes), "d2h_bytes_per_step": int(out.nbytes)},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "roofline": roof,
+        "kernels": {k: {"ms_per_step": round(v["ms"] / args.steps, 4), "launches_per_step": v["launches"] / args.steps,
+                        "GB_per_s": round(v["alg_bytes"] / (v["ms"] / 1e3) / 1e9, 1) if v["ms"] > 0 else None}
+                    for k, v in kern.items()},
+        "stages_ms_per_step": {k: round(v["ms"] / args.steps, 4) for k, v in prof.get("stages", {}).items()},
+    }
+    r.close()
+    return line
+
+
+def run_reference(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
+    from oracle import build_ref
+    lib = build_ref.build()
+    if lib is None:
+        return {"impl": "reference", "unavailable": "reference CUDA build could not be compiled here"}
+    from oracle.refharness import RefRecon
+    nimg = vols[0].shape[0]
+    fl = [v.astype(np.float32) for v in vols]
+    r = RefRecon(nx, ny, nimg, cfg, otf)
+    r.set_ntimes(1 << 14)
+    r.set_raw(fl[0])
+    r.load_and_rescale(0)
+    r.set_cur_time(0)
+    r.process()
+    reuse = args.workload.startswith("timeseries")
+    t_idx = 1 if reuse else 0
+    out = np.empty(r.out_shape, np.float32)
+
+    def step(i):
+        r.set_raw(fl[i % len(fl)])
+        r.load_and_rescale(t_idx)
+        r.set_cur_time(t_idx)
+        r.process()
+        out[...] = r.result()
+
+    import ctypes
+    ctypes.CDLL(None).fflush(None)
+    devnull = os.open(os.devnull, os.O_WRONLY)
+    saved = os.dup(1)
+    os.dup2(devnull, 1)  # the reference prints progress on stdout
+    try:
+        for i in range(args.warmup):
+            step(i)
+        clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+        clocks.start()
+        barrier(dist)
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            step(i)
+        barrier(dist)
+        dt = max_over_ranks(dist, time.perf_counter() - t0)
+        clk = clocks.stop()
+    finally:
+        import ctypes
+        ctypes.CDLL(None).fflush(None)  # flush the reference's C stdio before restoring stdout
+        sys.stdout.flush()
+        os.dup2(saved, 1)
+        os.close(devnull)
+    value = world * args.steps * outvox / dt / 1e6
+    r.close()
+    return {
+        "impl": "reference",
+        "metric": "Recon output Mvoxels/s (SIM 3-beam, 512x512x48x15 -> 1024x1024x48)",
+        "value": round(value, 1), "unit": "Mvoxels/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "nx": nx, "ny": ny, "nz": nz, "images_per_volume": nimg},
+        "e2e": {"value": round(value, 1), "unit": "Mvoxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cpu_baseline": {"value": round(value, 1), "unit": "Mvoxels/s", "cores": 1, "kind": "reference",
+                         "sample": "the reference's own CUDA build (gpuFunctionsImpl.cu kernels + cuFFT, host "
+                                   "orchestration restated from cudaSirecon.cpp) through its SR_* flow on the full "
+                                   "workload; one host thread drives it"},
+        "clocks": clk,
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=list(WORKLOADS), default="timeseries_512x512x48")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    rank, world, local, dist = dist_init()
+    if args.impl == "reference" and rank != 0:
+        return
+    if args.impl == "reference":
+        world, dist = 1, None
+    nx, ny, nz, _ = WORKLOADS[args.workload]
+    vols, otf, cfg = make_workload(nx, ny, nz, 2)
+    outvox = 4 * nx * ny * nz
+    if args.impl == "reference":
+        line = run_reference(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox)
+    else:
+        line = run_gb300(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox)
+        if rank == 0 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(vols[0], otf, cfg, nx, ny, nz)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

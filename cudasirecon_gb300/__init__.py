@@ -74,6 +74,10 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.SRX_resetProfile.argtypes = [vp]
     lib.SRX_kernelLaunches.restype = C.c_longlong
     lib.SRX_kernelLaunches.argtypes = [vp]
+    lib.SRX_pinHost.restype = ip
+    lib.SRX_pinHost.argtypes = [vp, C.c_size_t]
+    lib.SRX_unpinHost.restype = ip
+    lib.SRX_unpinHost.argtypes = [vp]
     _lib = lib
     return lib
 
@@ -257,3 +261,15 @@ class Reconstructor:
 
     def kernel_launches(self) -> int:
         return int(self.lib.SRX_kernelLaunches(self.h))
+
+
+def pin(array: np.ndarray) -> None:
+    """Page-lock a numpy array's memory (SRX_pinHost)."""
+    lib = load_library()
+    if lib.SRX_pinHost(array.ctypes.data, array.nbytes) != 0:
+        raise SIReconError(_err(lib))
+
+
+def unpin(array: np.ndarray) -> None:
+    lib = load_library()
+    lib.SRX_unpinHost(array.ctypes.data)

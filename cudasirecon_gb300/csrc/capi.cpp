@@ -2,6 +2,8 @@
 // reference) plus the additions declared in include/cudasirecon.h.  No C++
 // exception crosses this boundary and nothing here calls exit(): failures are
 // recorded as a thread-local message for SR_getLastError.
+#include <cuda_runtime.h>
+
 #include <cstring>
 #include <stdexcept>
 #include <string>
@@ -188,5 +190,25 @@ void SRX_resetProfile(SIM_Reconstructor* sr)
 }
 
 long long SRX_kernelLaunches(SIM_Reconstructor* sr) { return need(sr) ? sr->launches() : -1; }
+
+int SRX_pinHost(void* ptr, size_t bytes)
+{
+  cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+  if (e != cudaSuccess) {
+    g_last_error = std::string("cudaHostRegister: ") + cudaGetErrorString(e);
+    return (int)e;
+  }
+  return 0;
+}
+
+int SRX_unpinHost(void* ptr)
+{
+  cudaError_t e = cudaHostUnregister(ptr);
+  if (e != cudaSuccess) {
+    g_last_error = std::string("cudaHostUnregister: ") + cudaGetErrorString(e);
+    return (int)e;
+  }
+  return 0;
+}
 
 }  // extern "C"

@@ -206,6 +206,11 @@ void SRX_resetProfile(SIM_Reconstructor* sr);
 /* Number of this library's kernels launched since the handle was created. */
 long long SRX_kernelLaunches(SIM_Reconstructor* sr);
 
+/* Page-lock (pin) / unpin a caller's host buffer so that SR_setRaw* and
+ * SR_getResult copies run at full host-link bandwidth.  Return 0 on success. */
+int SRX_pinHost(void* ptr, size_t bytes);
+int SRX_unpinHost(void* ptr);
+
 #ifdef __cplusplus
 }
 #endif
