@@ -124,16 +124,28 @@ class ClockSampler:
 
 
 def make_workload(nx, ny, nz, nvol, seed=5):
-    """Seeded synthetic time points (drift 0.2 px/frame, 1 %/frame bleaching)."""
+    """Seeded synthetic time points (drift 0.2 px/frame, 1 %/frame bleaching).
+
+    With SIRECON_BENCH_CACHE set to a folder, the stacks are cached there.
+    """
     from cudasirecon_gb300 import synthetic as syn
     o = syn.Optics()
+    cache = os.environ.get("SIRECON_BENCH_CACHE")
+    cpath = os.path.join(cache, f"bench_{nx}x{ny}x{nz}_{nvol}_{seed}.npz") if cache else None
+    if cpath and os.path.exists(cpath):
+        z = np.load(cpath)
+        return [z[f"v{i}"] for i in range(nvol)], z["otf"], str(z["cfg"])
     vols = []
     for t in range(nvol):
         a = syn.simulate(nx, ny, nz, o, seed=seed, drift_px=0.2 * t, bleach=0.99 ** t, noise_seed=1000 + t,
                          scene_seed=seed, mod_seed=seed + 1)
         vols.append(a.raw)
     otf = syn.ra_otf(o, nx_psf=128, nz_psf=64)
-    return vols, otf, syn.config_text(o)
+    cfg = syn.config_text(o)
+    if cpath:
+        os.makedirs(cache, exist_ok=True)
+        np.savez(cpath, otf=otf, cfg=cfg, **{f"v{i}": v for i, v in enumerate(vols)})
+    return vols, otf, cfg
 
 
 def peaks():

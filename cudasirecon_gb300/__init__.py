@@ -74,6 +74,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.SRX_resetProfile.argtypes = [vp]
     lib.SRX_kernelLaunches.restype = C.c_longlong
     lib.SRX_kernelLaunches.argtypes = [vp]
+    lib.SRX_fftSelfTest.restype = ip
+    lib.SRX_fftSelfTest.argtypes = [fp, ip, ip, ip, ip]
     lib.SRX_pinHost.restype = ip
     lib.SRX_pinHost.argtypes = [vp, C.c_size_t]
     lib.SRX_unpinHost.restype = ip
@@ -273,3 +275,15 @@ def pin(array: np.ndarray) -> None:
 def unpin(array: np.ndarray) -> None:
     lib = load_library()
     lib.SRX_unpinHost(array.ctypes.data)
+
+
+def fft_selftest(x: np.ndarray, inverse: bool = False, columns: bool = False) -> np.ndarray:
+    """Run the library's FFT engine on lines x[nlines][n] (complex64)."""
+    lib = load_library()
+    a = np.ascontiguousarray(x, np.complex64).copy()
+    nl, n = a.shape
+    rc = lib.SRX_fftSelfTest(a.view(np.float32).ctypes.data_as(C.POINTER(C.c_float)), n, nl, int(inverse),
+                             int(columns))
+    if rc != 0:
+        raise SIReconError(_err(lib) or f"fft self test failed ({rc})")
+    return a

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcudasirecon.so")
 CLI = os.path.join(HERE, "bin", "cudasirecon")
-SOURCES = ["fft_plan.cu", "k_ingest.cu", "k_fit.cu", "k_assemble.cu", "reconstructor.cu",
+SOURCES = ["fft_plan.cu", "k_selftest.cu", "k_ingest.cu", "k_fit.cu", "k_assemble.cu", "reconstructor.cu",
            "params.cpp", "image_io.cpp", "capi.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

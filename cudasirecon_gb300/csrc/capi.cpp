@@ -191,6 +191,23 @@ void SRX_resetProfile(SIM_Reconstructor* sr)
 
 long long SRX_kernelLaunches(SIM_Reconstructor* sr) { return need(sr) ? sr->launches() : -1; }
 
+int SRX_fftSelfTest(float* data, int n, int nlines, int inverse, int columns)
+{
+  int rc = -1;
+  guarded([&] {
+    size_t bytes = (size_t)n * nlines * 2 * sizeof(float);
+    float2* d = nullptr;
+    if (cudaMalloc(&d, bytes) != cudaSuccess) throw std::runtime_error("cudaMalloc failed");
+    cudaMemcpy(d, data, bytes, cudaMemcpyHostToDevice);
+    rc = simrecon::launch_fft_selftest(d, n, nlines, inverse, columns, 0);
+    cudaMemcpy(data, d, bytes, cudaMemcpyDeviceToHost);
+    cudaError_t e = cudaDeviceSynchronize();
+    cudaFree(d);
+    if (e != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e));
+  });
+  return rc;
+}
+
 int SRX_pinHost(void* ptr, size_t bytes)
 {
   cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);

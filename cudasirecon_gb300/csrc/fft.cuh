@@ -6,7 +6,7 @@
 //   * "columns" (ldl == 1): lines are interleaved, W consecutive columns of a
 //     strided axis staged as an [n][W] tile (y / z transforms), so that the
 //     global loads and stores of a tile are 8*W-byte coalesced segments.
-// The transform is an autosorting Stockham sequence of radix-2/3/4/5/7/8
+// The transform is an autosorting Stockham sequence of radix-2/3/4/5/7/8/16/32
 // stages ping-ponging between two shared buffers of the same layout.  Twiddles come from a per-length
 // table tw[k] = exp(-2 pi i k / n) computed in double precision on the host.
 //
@@ -164,6 +164,58 @@ __device__ __forceinline__ void dft8(float2* v)
   v[7] = o[3];
 }
 
+// exp(DIR * 2 pi i m / 32) for a compile-time m
+__device__ __forceinline__ float2 w32c(int m, int dir)
+{
+  constexpr float c[32] = {1.000000000e+00f, 9.807852804e-01f, 9.238795325e-01f, 8.314696123e-01f, 7.071067812e-01f, 5.555702330e-01f, 3.826834324e-01f, 1.950903220e-01f, 6.123233996e-17f, -1.950903220e-01f, -3.826834324e-01f, -5.555702330e-01f, -7.071067812e-01f, -8.314696123e-01f, -9.238795325e-01f, -9.807852804e-01f, -1.000000000e+00f, -9.807852804e-01f, -9.238795325e-01f, -8.314696123e-01f, -7.071067812e-01f, -5.555702330e-01f, -3.826834324e-01f, -1.950903220e-01f, -1.836970199e-16f, 1.950903220e-01f, 3.826834324e-01f, 5.555702330e-01f, 7.071067812e-01f, 8.314696123e-01f, 9.238795325e-01f, 9.807852804e-01f};
+  constexpr float s[32] = {0.000000000e+00f, 1.950903220e-01f, 3.826834324e-01f, 5.555702330e-01f, 7.071067812e-01f, 8.314696123e-01f, 9.238795325e-01f, 9.807852804e-01f, 1.000000000e+00f, 9.807852804e-01f, 9.238795325e-01f, 8.314696123e-01f, 7.071067812e-01f, 5.555702330e-01f, 3.826834324e-01f, 1.950903220e-01f, 1.224646799e-16f, -1.950903220e-01f, -3.826834324e-01f, -5.555702330e-01f, -7.071067812e-01f, -8.314696123e-01f, -9.238795325e-01f, -9.807852804e-01f, -1.000000000e+00f, -9.807852804e-01f, -9.238795325e-01f, -8.314696123e-01f, -7.071067812e-01f, -5.555702330e-01f, -3.826834324e-01f, -1.950903220e-01f};
+  return make_float2(c[m & 31], dir < 0 ? -s[m & 31] : s[m & 31]);
+}
+
+// radix 16 = 4 x 4: inner DFT4 over x[i + 4j], twiddle W16^(i k1), outer DFT4 over i
+template <int DIR>
+__device__ __forceinline__ void dft16(float2* v)
+{
+  float2 a[16];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    float2 t[4] = {v[i], v[i + 4], v[i + 8], v[i + 12]};
+    dft4<DIR>(t);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) a[i * 4 + k1] = (i * k1 == 0) ? t[k1] : cmul(t[k1], w32c(2 * i * k1, DIR));
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    float2 u[4] = {a[k1], a[4 + k1], a[8 + k1], a[12 + k1]};
+    dft4<DIR>(u);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = u[k2];
+  }
+}
+
+// radix 32 = 4 x 8: inner DFT8 over x[i + 4j], twiddle W32^(i k1), outer DFT4 over i
+template <int DIR>
+__device__ __forceinline__ void dft32(float2* v)
+{
+  float2 a[32];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    float2 t[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) t[j] = v[i + 4 * j];
+    dft8<DIR>(t);
+#pragma unroll
+    for (int k1 = 0; k1 < 8; ++k1) a[i * 8 + k1] = (i * k1 == 0) ? t[k1] : cmul(t[k1], w32c(i * k1, DIR));
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < 8; ++k1) {
+    float2 u[4] = {a[k1], a[8 + k1], a[16 + k1], a[24 + k1]};
+    dft4<DIR>(u);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) v[k1 + 8 * k2] = u[k2];
+  }
+}
+
 template <int R, int DIR>
 __device__ __forceinline__ void dftR(float2* v)
 {
@@ -173,32 +225,41 @@ __device__ __forceinline__ void dftR(float2* v)
   else if (R == 5) dft5<DIR>(v);
   else if (R == 7) dft7<DIR>(v);
   else if (R == 8) dft8<DIR>(v);
+  else if (R == 16) dft16<DIR>(v);
+  else if (R == 32) dft32<DIR>(v);
 }
+
+// q = t / d for t, d < 2^16 with m = floor((2^32 - 1) / d) + 1 (exact in that range)
+__device__ __forceinline__ unsigned magic_of(unsigned d) { return d == 1 ? 0u : 0xFFFFFFFFu / d + 1u; }
+__device__ __forceinline__ unsigned fdiv(unsigned t, unsigned d, unsigned m) { return d == 1 ? t : __umulhi(t, m); }
 
 // One Stockham stage of radix R over nl lines, reading `src` and writing
 // `dst` (ping-pong shared buffers of identical layout), then a barrier.
+// Index arithmetic uses multiply-high division (all indices < 2^16).
 template <int R, int DIR>
 __device__ __forceinline__ void stockham_stage(const float2* __restrict__ src, float2* __restrict__ dst, int n,
                                                int nl, int ldl, int ldi, int Ns, const float2* __restrict__ tw)
 {
-  const int m = n / R;  // butterflies per line
-  const int total = m * nl;
+  const unsigned m = n / R;  // butterflies per line
+  const unsigned total = m * nl;
   const int twstep = n / (Ns * R);
   const bool rows = (ldi == 1);
-  for (int t = threadIdx.x; t < total; t += blockDim.x) {
-    int l, j;
+  const unsigned mm = magic_of(m), mnl = magic_of(nl), mns = magic_of(Ns);
+  for (unsigned t = threadIdx.x; t < total; t += blockDim.x) {
+    unsigned l, j;
     if (rows) {
-      l = t / m;
+      l = fdiv(t, m, mm);
       j = t - l * m;
     } else {
-      j = t / nl;
+      j = fdiv(t, nl, mnl);
       l = t - j * nl;
     }
     float2 v[R];
     const float2* s = src + l * ldl;
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = s[(j + r * m) * ldi];
-    const int k = j % Ns;
+    const unsigned jq = fdiv(j, Ns, mns);
+    const unsigned k = j - jq * Ns;
     if (Ns > 1) {
 #pragma unroll
       for (int r = 1; r < R; ++r) {
@@ -208,7 +269,7 @@ __device__ __forceinline__ void stockham_stage(const float2* __restrict__ src, f
       }
     }
     dftR<R, DIR>(v);
-    float2* d = dst + l * ldl + ((j / Ns) * Ns * R + k) * ldi;
+    float2* d = dst + l * ldl + (jq * Ns * R + k) * ldi;
 #pragma unroll
     for (int r = 0; r < R; ++r) d[r * Ns * ldi] = v[r];
   }
@@ -233,7 +294,9 @@ __device__ float2* fft_lines(float2* a, float2* b, const FFTPlan& p, int nl, int
       case 4: stockham_stage<4, DIR>(src, dst, p.n, nl, ldl, ldi, Ns, p.tw); break;
       case 5: stockham_stage<5, DIR>(src, dst, p.n, nl, ldl, ldi, Ns, p.tw); break;
       case 7: stockham_stage<7, DIR>(src, dst, p.n, nl, ldl, ldi, Ns, p.tw); break;
-      default: stockham_stage<8, DIR>(src, dst, p.n, nl, ldl, ldi, Ns, p.tw); break;
+      case 8: stockham_stage<8, DIR>(src, dst, p.n, nl, ldl, ldi, Ns, p.tw); break;
+      case 16: stockham_stage<16, DIR>(src, dst, p.n, nl, ldl, ldi, Ns, p.tw); break;
+      default: stockham_stage<32, DIR>(src, dst, p.n, nl, ldl, ldi, Ns, p.tw); break;
     }
     Ns *= R;
     float2* t = src;

@@ -25,18 +25,14 @@ bool factor(int n, std::vector<int>& radix)
     m /= 2;
     ++p2;
   }
-  // powers of two as radix 8 / 4 (a lone factor 2 only when n is 2)
-  int k8 = p2 / 3, rem = p2 % 3;
-  if (rem == 1 && k8 >= 1) {
-    --k8;
-    radix.push_back(4);
-    radix.push_back(4);
-  } else if (rem == 1) {
-    radix.push_back(2);
-  } else if (rem == 2) {
-    radix.push_back(4);
-  }
-  for (int i = 0; i < k8; ++i) radix.push_back(8);
+  // powers of two in as few stages as possible: radix 32 / 16 / 8 / 4 / 2
+  // (e.g. 1024 = 32*32, 512 = 32*16, 256 = 16*16, 128 = 16*8, 64 = 8*8)
+  static const int plan2[14][3] = {{0, 0, 0},  {2, 0, 0},   {4, 0, 0},   {8, 0, 0},   {16, 0, 0},
+                                   {32, 0, 0}, {8, 8, 0},   {16, 8, 0},  {16, 16, 0}, {32, 16, 0},
+                                   {32, 32, 0}, {16, 16, 8}, {16, 16, 16}, {32, 16, 16}};
+  if (p2 > 13) return false;
+  for (int i = 0; i < 3; ++i)
+    if (plan2[p2][i]) radix.push_back(plan2[p2][i]);
   for (int r : {3, 5, 7})
     while (m % r == 0) {
       m /= r;

@@ -118,6 +118,9 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches);
 int launch_ramp_tables(const float2* k0 /* device [ndirs] */, int ndirs, int norders, int X, int Y, float dxyz,
                        float fact, float2* ex, float2* ey, cudaStream_t s, long long* launches);
 
+// FFT-engine self test on `nlines` lines of length n (in place, device memory)
+int launch_fft_selftest(float2* data, int n, int nlines, int inverse, int columns, cudaStream_t s);
+
 // L2 flush helper for timing
 int launch_fill(float* buf, size_t n, float v, cudaStream_t s, long long* launches);
 

@@ -209,6 +209,12 @@ long long SRX_kernelLaunches(SIM_Reconstructor* sr);
 /* Page-lock (pin) / unpin a caller's host buffer so that SR_setRaw* and
  * SR_getResult copies run at full host-link bandwidth.  Return 0 on success. */
 int SRX_pinHost(void* ptr, size_t bytes);
+/* Test hook: transform `nlines` complex lines of length n (interleaved
+ * float pairs, in place) with the library's FFT engine; inverse != 0 for
+ * e^{+i}; columns != 0 stages the lines interleaved (strided-axis layout).
+ * Unnormalised, like cuFFT.  Returns 0 on success. */
+int SRX_fftSelfTest(float* data, int n, int nlines, int inverse, int columns);
+
 int SRX_unpinHost(void* ptr);
 
 #ifdef __cplusplus
