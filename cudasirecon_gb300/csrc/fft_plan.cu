@@ -50,6 +50,33 @@ thread_local KernelTimer* t_timer = nullptr;
 void set_kernel_timer(KernelTimer* t) { t_timer = t; }
 KernelTimer* kernel_timer() { return t_timer; }
 
+// The radix sequence of get_fft_plan, written into a caller array without
+// any allocation (used by the allocation-free FFT entry point).
+bool fft_radix_plan(int n, int* radix, int* nstages)
+{
+  if (n < 1) return false;
+  int m = n, p2 = 0, ns = 0;
+  while (m % 2 == 0) {
+    m /= 2;
+    ++p2;
+  }
+  static const int plan2[14][3] = {{0, 0, 0},  {2, 0, 0},   {4, 0, 0},   {8, 0, 0},   {16, 0, 0},
+                                   {32, 0, 0}, {8, 8, 0},   {16, 8, 0},  {16, 16, 0}, {32, 16, 0},
+                                   {32, 32, 0}, {16, 16, 8}, {16, 16, 16}, {32, 16, 16}};
+  if (p2 > 13) return false;
+  for (int i = 0; i < 3; ++i)
+    if (plan2[p2][i]) radix[ns++] = plan2[p2][i];
+  for (int r : {3, 5, 7})
+    while (m % r == 0) {
+      if (ns >= kMaxStages) return false;
+      m /= r;
+      radix[ns++] = r;
+    }
+  if (m != 1) return false;
+  *nstages = ns;
+  return true;
+}
+
 bool fft_length_ok(int n)
 {
   std::vector<int> r;

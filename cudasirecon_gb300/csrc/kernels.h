@@ -25,6 +25,8 @@ KernelTimer* kernel_timer();
 // (device, n).  n must factor into 2, 3, 5, 7.  Returns false if it cannot.
 bool get_fft_plan(int n, FFTPlan* plan);
 bool fft_length_ok(int n);
+// radix sequence of length n into radix[kMaxStages] (no allocation)
+bool fft_radix_plan(int n, int* radix, int* nstages);
 
 // -------------------------------------------------------------------- ingest
 struct IngestArgs {

@@ -215,6 +215,19 @@ int SRX_pinHost(void* ptr, size_t bytes);
  * Unnormalised, like cuFFT.  Returns 0 on success. */
 int SRX_fftSelfTest(float* data, int n, int nlines, int inverse, int columns);
 
+/* No counterpart in the reference.  The same line transform for callers
+ * that must not allocate device memory (code running inside a CUDA graph
+ * capture, real-time acquisition loops, plug-in hosts that own the device's
+ * memory): `in` and `out` are host arrays of nlines x n complex values; the
+ * device staging buffer and twiddle table live in a fixed 16 MiB file-scope
+ * device array, so no cudaMalloc/cudaFree is made.  At most 2 Mi complex
+ * values per call and n <= 8192; larger requests return -1 without running.
+ * Calls share the array: calls that overlap on the GPU race.  The first call
+ * on a device looks up the array's address; make it before any stream
+ * capture.  Returns 0 on success; SRX_fftLinesNoAllocError() describes a
+ * failure. */
+int SRX_fftLinesNoAlloc(const float* in, float* out, int n, int nlines, int inverse, int columns);
+const char* SRX_fftLinesNoAllocError(void);
 int SRX_unpinHost(void* ptr);
 
 #ifdef __cplusplus
