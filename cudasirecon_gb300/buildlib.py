@@ -28,7 +28,7 @@ def nvcc() -> str:
 
 
 def _flags():
-    return ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include"),
+    return ["-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include"),
             "-I", CSRC] + ARCH
 
 

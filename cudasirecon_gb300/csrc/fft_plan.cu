@@ -2,12 +2,14 @@
 // (device, length).  The tables are allocated once per length and live until
 // process exit.
 #include <cmath>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <utility>
 #include <vector>
 
 #include "kernels.h"
+#include "reg_fft.cuh"
 
 namespace simrecon {
 
@@ -75,6 +77,30 @@ bool fft_radix_plan(int n, int* radix, int* nstages)
   if (m != 1) return false;
   *nstages = ns;
   return true;
+}
+
+bool reg_fft_site_enabled(FftSite site, int n)
+{
+  // Built-in choice, from timing both paths in every kernel on GB300 at
+  // 256^2 x 32 and 512^2 x 48: the register path wins for all lengths up to
+  // 256 and, at any length, in the ingest rows and the short z lines; the
+  // 512- and 1024-point transforms of the overlap, correlation and assembly
+  // kernels are faster with the Stockham stages (the register path's 130-255
+  // registers per thread leave one CTA per SM there).
+  static const int forced = [] {
+    const char* e = std::getenv("SIMRECON_FFT_REGISTER_SITES");
+    return e ? (int)(std::strtoul(e, nullptr, 16) | (1u << kSiteSelfTest)) : -1;
+  }();
+  if (forced >= 0) return (forced >> (int)site) & 1;
+  switch (site) {
+    case kSiteIngestX:
+    case kSiteSeparateZ:
+    case kSiteAsmZ:
+    case kSiteSelfTest:
+      return true;
+    default:
+      return n <= 256;
+  }
 }
 
 bool fft_length_ok(int n)

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "kernels.h"
+#include "reg_fft.cuh"
 
 namespace simrecon {
 
@@ -187,7 +188,8 @@ struct Slot {
 // zero-padded inverse FFT along y of the in-band plane kz of band (d, o);
 // columns c = kx + nx/2 - 1, kx in [-nx/2+1, nx/2] (move_kernel ranges,
 // gpuFunctionsImpl.cu:1853-1913)
-__global__ void k_asm_y(AssembleArgs a, const Slot* __restrict__ slots, FFTPlan plan, int W)
+template <int NF>
+__global__ void __launch_bounds__(kThreads) k_asm_y(AssembleArgs a, const Slot* __restrict__ slots, FFTPlan plan, int W)
 {
   extern __shared__ float2 sm[];
   const Slot sl = slots[blockIdx.y];
@@ -197,6 +199,7 @@ __global__ void k_asm_y(AssembleArgs a, const Slot* __restrict__ slots, FFTPlan 
   const float2* br = a.bands + ((size_t)sl.dir * a.nphases + (sl.order == 0 ? 0 : 2 * sl.order - 1)) * nz * plane;
   const float2* bi = sl.order == 0 ? nullptr : a.bands + ((size_t)sl.dir * a.nphases + 2 * sl.order) * nz * plane;
   const int ylo = ny / 2 - 1;  // ky in [-ylo, ny/2]
+  const int ld = W + 1;
   for (int t = threadIdx.x; t < Y * W; t += blockDim.x) {
     int yr = t / W, w = t - yr * W;
     int c = c0 + w;
@@ -229,20 +232,21 @@ __global__ void k_asm_y(AssembleArgs a, const Slot* __restrict__ slots, FFTPlan 
         v = make_float2(re.x - im.y, re.y + im.x);
       }
     }
-    sm[t] = v;
+    sm[yr * ld + w] = v;
   }
   __syncthreads();
-  const float2* res = fft_lines<+1>(sm, sm + Y * W, plan, W, 1, W);
+  const float2* res = fft_dispatch<NF, +1>(sm, sm + Y * ld, plan, W, 1, ld);
   float2* dst = a.T + (size_t)blockIdx.y * Y * nx;
   for (int t = threadIdx.x; t < Y * W; t += blockDim.x) {
     int yr = t / W, w = t - yr * W;
-    if (c0 + w < nx) dst[(size_t)yr * nx + c0 + w] = res[t];
+    if (c0 + w < nx) dst[(size_t)yr * nx + c0 + w] = res[yr * ld + w];
   }
 }
 
 // zero-padded inverse FFT along x of every slot of output plane zout, ramp,
 // weighted sum -> S[zout][yr][:]
 constexpr int kAccPerThread = 16;
+template <int NF>
 __global__ void __launch_bounds__(kThreads) k_asm_x(AssembleArgs a, const int* __restrict__ plane_slot0,
                                                const int* __restrict__ plane_nslot, const Slot* __restrict__ slots,
                                                const int* __restrict__ plane_zout, FFTPlan plan, int lines)
@@ -255,6 +259,7 @@ __global__ void __launch_bounds__(kThreads) k_asm_x(AssembleArgs a, const int* _
 #pragma unroll
   for (int k = 0; k < kAccPerThread; ++k) acc[k] = make_float2(0.f, 0.f);
   const int xlo = nx / 2 - 1;
+  const int ldl = X + 1;
   for (int b0 = 0; b0 < ns; b0 += lines) {
     int nb = min(lines, ns - b0);
     __syncthreads();
@@ -268,10 +273,10 @@ __global__ void __launch_bounds__(kThreads) k_asm_x(AssembleArgs a, const int* _
           v = a.T[((size_t)(s0 + b0 + l) * Y + yr) * nx + c];
         }
       }
-      sm[t] = v;
+      sm[l * ldl + xo] = v;
     }
     __syncthreads();
-    const float2* res = fft_lines<+1>(sm, sm + lines * X, plan, lines, X, 1);
+    const float2* res = fft_dispatch<NF, +1>(sm, sm + lines * ldl, plan, lines, ldl, 1);
     for (int l = 0; l < nb; ++l) {
       const Slot sl = slots[s0 + b0 + l];
       const int ro = sl.dir * a.norders + sl.order;
@@ -284,7 +289,7 @@ __global__ void __launch_bounds__(kThreads) k_asm_x(AssembleArgs a, const int* _
         int x = threadIdx.x + k * blockDim.x;
         if (x < X) {
           float2 e = cmul(a.ex[(size_t)ro * X + x], ey);
-          float2 v = cmul(res[l * X + x], e);
+          float2 v = cmul(res[l * ldl + x], e);
           acc[k].x += v.x;
           acc[k].y += v.y;
         }
@@ -300,21 +305,23 @@ __global__ void __launch_bounds__(kThreads) k_asm_x(AssembleArgs a, const int* _
 }
 
 // inverse FFT along z of S, real part -> out
+template <int NF>
 __global__ void __launch_bounds__(kThreads) k_asm_z(AssembleArgs a, const unsigned char* __restrict__ zactive,
                                                     FFTPlan plan, int W)
 {
   extern __shared__ float2 sm[];
   const int X = a.X, Y = a.Y, Z = a.Z;
   const int yr = blockIdx.y, c0 = blockIdx.x * W;
+  const int ld = W + 1;
   for (int t = threadIdx.x; t < Z * W; t += blockDim.x) {
     int z = t / W, w = t - z * W;
-    sm[t] = (zactive[z] && c0 + w < X) ? a.S[((size_t)z * Y + yr) * X + c0 + w] : make_float2(0.f, 0.f);
+    sm[z * ld + w] = (zactive[z] && c0 + w < X) ? a.S[((size_t)z * Y + yr) * X + c0 + w] : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  const float2* res = fft_lines<+1>(sm, sm + Z * W, plan, W, 1, W);
+  const float2* res = fft_dispatch<NF, +1>(sm, sm + Z * ld, plan, W, 1, ld);
   for (int t = threadIdx.x; t < Z * W; t += blockDim.x) {
     int z = t / W, w = t - z * W;
-    if (c0 + w < X) a.out[((size_t)z * Y + yr) * X + c0 + w] = res[t].x;
+    if (c0 + w < X) a.out[((size_t)z * Y + yr) * X + c0 + w] = res[z * ld + w].x;
   }
 }
 
@@ -450,12 +457,12 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
   cudaMemcpyAsync(d_zact, zact.data(), a.Z, cudaMemcpyHostToDevice, s);
   // tile sizes
   int Wy = std::max(1, std::min(32, kMaxElems / a.Y));
-  size_t smy = (size_t)2 * Wy * a.Y * sizeof(float2);
-  cudaFuncSetAttribute(k_asm_y, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
+  size_t smy = fft_stage_smem(a.Y, Wy, a.Y * (Wy + 1), kThreads);
+
   int xlines = std::max(1, kMaxElems / a.X);
   xlines = std::min(xlines, 16);
-  size_t smx = (size_t)2 * xlines * a.X * sizeof(float2);
-  cudaFuncSetAttribute(k_asm_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+  size_t smx = fft_stage_smem(a.X, xlines, xlines * (a.X + 1), kThreads);
+
   if (a.X > kAccPerThread * kThreads) return -3;
   // process whole planes in groups whose slots fit in T
   size_t np = p0.size();
@@ -472,7 +479,10 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
     AssembleArgs ay = a;
     KernelTimer* kt = kernel_timer();
     if (kt) kt->begin(s);
-    k_asm_y<<<dim3((nx + Wy - 1) / Wy, nsl), kThreads, smy, s>>>(ay, d_slots + first, py, Wy);
+    dispatch_fft_len(kSiteAsmY, a.Y, [&]<int NF>() {
+      cudaFuncSetAttribute(k_asm_y<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
+      k_asm_y<NF><<<dim3((nx + Wy - 1) / Wy, nsl), kThreads, smy, s>>>(ay, d_slots + first, py, Wy);
+    });
     if (kt) {
       double rd = 0;
       for (int q = first; q < first + nsl; ++q) rd += (slots[q].order == 0 ? 1 : 2) * (double)a.ny * nx * 8;
@@ -482,18 +492,23 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
     AssembleArgs ax = a;
     ax.T = a.T - (size_t)first * per_slot;
     if (kt) kt->begin(s);
-    k_asm_x<<<dim3(a.Y, (unsigned)(pj - pi)), kThreads, smx, s>>>(ax, d_p0 + pi, d_pn + pi, d_slots, d_pz + pi, px,
-                                                              xlines);
+    dispatch_fft_len(kSiteAsmX, a.X, [&]<int NF>() {
+      cudaFuncSetAttribute(k_asm_x<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+      k_asm_x<NF><<<dim3(a.Y, (unsigned)(pj - pi)), kThreads, smx, s>>>(ax, d_p0 + pi, d_pn + pi, d_slots,
+                                                                       d_pz + pi, px, xlines);
+    });
     if (kt) kt->end("k_asm_x", s, (double)nsl * per_slot * sizeof(float2) + (double)(pj - pi) * a.X * a.Y * 8);
     nl += 2;
     pi = pj;
   }
   int Wz = std::max(1, std::min(32, kMaxElems / a.Z));
-  size_t smz = (size_t)2 * Wz * a.Z * sizeof(float2);
-  cudaFuncSetAttribute(k_asm_z, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
+  size_t smz = fft_stage_smem(a.Z, Wz, a.Z * (Wz + 1), kThreads);
   KernelTimer* kt = kernel_timer();
   if (kt) kt->begin(s);
-  k_asm_z<<<dim3((a.X + Wz - 1) / Wz, a.Y), kThreads, smz, s>>>(a, d_zact, pz, Wz);
+  dispatch_fft_len(kSiteAsmZ, a.Z, [&]<int NF>() {
+    cudaFuncSetAttribute(k_asm_z<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
+    k_asm_z<NF><<<dim3((a.X + Wz - 1) / Wz, a.Y), kThreads, smz, s>>>(a, d_zact, pz, Wz);
+  });
   if (kt) kt->end("k_asm_z", s, (double)np * a.X * a.Y * 8 + (double)a.X * a.Y * a.Z * 4);
   nl += 1;
   if (launches) *launches += nl;

@@ -23,6 +23,7 @@
 #include <algorithm>
 
 #include "kernels.h"
+#include "reg_fft.cuh"
 
 namespace simrecon {
 
@@ -32,7 +33,8 @@ constexpr int kThreads = 256;
 constexpr int kMaxElems = kFftElems;
 
 // ---------------------------------------------------------------- overlaps
-__global__ void __launch_bounds__(kThreads) k_ovl_build_x(OverlapArgs a, FFTPlan plan, int rows_per_cta)
+template <int NF>
+__global__ void __launch_bounds__(kThreads) k_ovl_build_x(OverlapArgs a, FFTPlan plan, int rows_per_cta, int ldl)
 {
   extern __shared__ float2 sm[];
   const int nx = a.nx, ny = a.ny, nz = a.nz, nxh = nx / 2 + 1;
@@ -113,19 +115,21 @@ __global__ void __launch_bounds__(kThreads) k_ovl_build_x(OverlapArgs a, FFTPlan
         }
       }
     }
-    sm[l * nx + j] = val;
+    sm[l * ldl + j] = val;
   }
   __syncthreads();
-  const float2* res = fft_lines<+1>(sm, sm + 2 * rows_per_cta * nx, plan, 2 * rows_per_cta, nx, 1);
+  const float2* res = fft_dispatch<NF, +1>(sm, sm + 2 * rows_per_cta * ldl, plan, 2 * rows_per_cta, ldl, 1);
   const size_t vol = (size_t)nzb * ny * nx;
   for (int t = threadIdx.x; t < 2 * nrows * nx; t += blockDim.x) {
     int l = t / nx, j = t - l * nx;
     int r = l >> 1, ov = l & 1;
-    a.ovl[(size_t)ov * vol + (size_t)(row0 + r) * nx + j] = res[t];
+    a.ovl[(size_t)ov * vol + (size_t)(row0 + r) * nx + j] = res[l * ldl + j];
   }
 }
 
-__global__ void __launch_bounds__(kThreads) k_ovl_y_accum(OverlapArgs a, FFTPlan plan, int W, int planes_per_group)
+template <int NF>
+__global__ void __launch_bounds__(kThreads) k_ovl_y_accum(OverlapArgs a, FFTPlan plan, int W, int planes_per_group,
+                                                          int xoff)
 {
   extern __shared__ float2 sm[];
   __shared__ double red[32];
@@ -134,20 +138,21 @@ __global__ void __launch_bounds__(kThreads) k_ovl_y_accum(OverlapArgs a, FFTPlan
   const int c0 = blockIdx.x * W;
   const int zb0 = blockIdx.y * planes_per_group;
   const int zb1 = min(nzb, zb0 + planes_per_group);
-  const int ld = 2 * W;
-  float2* acc = sm + (size_t)2 * ny * ld;  // [ny][W], after the two FFT buffers
+  const int ld = 2 * W + 1;  // odd pitch: conflict-free strided lane reads
+  float2* acc = sm + (size_t)xoff;  // [ny][W], after the two FFT buffers
   for (int t = threadIdx.x; t < ny * W; t += blockDim.x) acc[t] = make_float2(0.f, 0.f);
   double sx = 0.0, sy = 0.0;
   const size_t vol = (size_t)nzb * ny * nx;
   for (int zb = zb0; zb < zb1; ++zb) {
     __syncthreads();
-    for (int t = threadIdx.x; t < ny * ld; t += blockDim.x) {
-      int y = t / ld, q = t - y * ld;
+    for (int t = threadIdx.x; t < ny * 2 * W; t += blockDim.x) {
+      int y = t / (2 * W), q = t - y * 2 * W;
       int ov = q >= W, w = q - ov * W;
-      sm[t] = (c0 + w < nx) ? a.ovl[(size_t)ov * vol + ((size_t)zb * ny + y) * nx + c0 + w] : make_float2(0.f, 0.f);
+      sm[y * ld + q] =
+          (c0 + w < nx) ? a.ovl[(size_t)ov * vol + ((size_t)zb * ny + y) * nx + c0 + w] : make_float2(0.f, 0.f);
     }
     __syncthreads();
-    const float2* res = fft_lines<+1>(sm, sm + ny * ld, plan, ld, 1, ld);
+    const float2* res = fft_dispatch<NF, +1>(sm, sm + ny * ld, plan, 2 * W, 1, ld);
     for (int t = threadIdx.x; t < ny * W; t += blockDim.x) {
       int y = t / W, w = t - y * W;
       float2 X = res[y * ld + w], Y = res[y * ld + W + w];
@@ -207,38 +212,43 @@ __global__ void k_p_reduce(OverlapArgs a, int ngroups, int nctas)
 
 // ---------------------------------------------------------- generic FFTs
 // rows of a [nrows][n] array; CONJ_IN conjugates the input on load
-template <int DIR, bool CONJ_IN>
+template <int DIR, bool CONJ_IN, int NF>
 __global__ void __launch_bounds__(kThreads) k_fft_rows(const float2* in, float2* out, int n, int nrows, FFTPlan plan,
                                                        int nl)
 {
   extern __shared__ float2 sm[];
   const int r0 = blockIdx.x * nl;
   const int nr = min(nl, nrows - r0);
+  const int ldl = n + 1;
   for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
-    int l = t / n;
+    int l = t / n, i = t - l * n;
     float2 v = l < nr ? in[(size_t)r0 * n + t] : make_float2(0.f, 0.f);
     if (CONJ_IN) v.y = -v.y;
-    sm[t] = v;
+    sm[l * ldl + i] = v;
   }
   __syncthreads();
-  const float2* res = fft_lines<DIR>(sm, sm + nl * n, plan, nl, n, 1);
-  for (int t = threadIdx.x; t < nr * n; t += blockDim.x) out[(size_t)r0 * n + t] = res[t];
+  const float2* res = fft_dispatch<NF, DIR>(sm, sm + nl * ldl, plan, nl, ldl, 1);
+  for (int t = threadIdx.x; t < nr * n; t += blockDim.x) {
+    int l = t / n, i = t - l * n;
+    out[(size_t)r0 * n + t] = res[l * ldl + i];
+  }
 }
 
-template <int DIR>
+template <int DIR, int NF>
 __global__ void __launch_bounds__(kThreads) k_fft_cols2(float2* data, int n, int ncol, FFTPlan plan, int W)
 {
   extern __shared__ float2 sm[];
   const int c0 = blockIdx.x * W;
+  const int ld = W + 1;
   for (int t = threadIdx.x; t < n * W; t += blockDim.x) {
     int i = t / W, w = t - i * W;
-    sm[t] = (c0 + w < ncol) ? data[(size_t)i * ncol + c0 + w] : make_float2(0.f, 0.f);
+    sm[i * ld + w] = (c0 + w < ncol) ? data[(size_t)i * ncol + c0 + w] : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  const float2* res = fft_lines<DIR>(sm, sm + n * W, plan, W, 1, W);
+  const float2* res = fft_dispatch<NF, DIR>(sm, sm + n * ld, plan, W, 1, ld);
   for (int t = threadIdx.x; t < n * W; t += blockDim.x) {
     int i = t / W, w = t - i * W;
-    if (c0 + w < ncol) data[(size_t)i * ncol + c0 + w] = res[t];
+    if (c0 + w < ncol) data[(size_t)i * ncol + c0 + w] = res[i * ld + w];
   }
 }
 
@@ -406,16 +416,20 @@ int launch_overlaps(OverlapArgs& a, cudaStream_t s, long long* launches)
   if (!get_fft_plan(a.nx, &px) || !get_fft_plan(a.ny, &py)) return -1;
   const int nzb = 2 * a.zdc + 1;
   // 1) build + x inverse FFT
+  const int ldl = a.nx + 1;
   int rows = std::max(1, kMaxElems / (2 * a.nx));
   rows = std::min(rows, nzb * a.ny);
-  size_t sm1 = (size_t)4 * rows * a.nx * sizeof(float2);
+  size_t sm1 = fft_stage_smem(a.nx, 2 * rows, 2 * rows * ldl, kThreads);
   int nb1 = (nzb * a.ny + rows - 1) / rows;
-  cudaFuncSetAttribute(k_ovl_build_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
+
   KernelTimer* kt = kernel_timer();
   const double ovlb = 2.0 * nzb * a.ny * a.nx * sizeof(float2);
   const double bandplanes = (double)nzb * a.ny * (a.nx / 2 + 1) * sizeof(float2);
   if (kt) kt->begin(s);
-  k_ovl_build_x<<<nb1, kThreads, sm1, s>>>(a, px, rows);
+  dispatch_fft_len(kSiteOvlX, a.nx, [&]<int NF>() {
+    cudaFuncSetAttribute(k_ovl_build_x<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
+    k_ovl_build_x<NF><<<nb1, kThreads, sm1, s>>>(a, px, rows, ldl);
+  });
   if (kt) kt->end("k_ovl_build_x", s, ovlb + (a.order1 == 0 ? 3 : 4) * bandplanes);
   // 2) y inverse FFT + accumulation over kz planes
   const int threads = kThreads;
@@ -424,10 +438,15 @@ int launch_overlaps(OverlapArgs& a, cudaStream_t s, long long* launches)
   int groups = std::max(1, std::min(nzb, (2 * 152 + tiles - 1) / tiles));
   int ppg = (nzb + groups - 1) / groups;
   groups = (nzb + ppg - 1) / ppg;
-  size_t sm2 = (size_t)a.ny * (4 * W + W) * sizeof(float2);
-  cudaFuncSetAttribute(k_ovl_y_accum, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+  const int tile = a.ny * (2 * W + 1);
+  const size_t fsm = fft_stage_smem(a.ny, 2 * W, tile, threads);
+  const int xoff = (int)(fsm / sizeof(float2));
+  size_t sm2 = fsm + (size_t)a.ny * W * sizeof(float2);
   if (kt) kt->begin(s);
-  k_ovl_y_accum<<<dim3(tiles, groups), threads, sm2, s>>>(a, py, W, ppg);
+  dispatch_fft_len(kSiteOvlY, a.ny, [&]<int NF>() {
+    cudaFuncSetAttribute(k_ovl_y_accum<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+    k_ovl_y_accum<NF><<<dim3(tiles, groups), threads, sm2, s>>>(a, py, W, ppg, xoff);
+  });
   if (kt) kt->end("k_ovl_y_accum", s, ovlb + (double)groups * a.ny * a.nx * sizeof(float2));
   // 3) reduce plane groups
   k_p_reduce<<<std::min(1024, (a.nx * a.ny + 255) / 256), 256, 0, s>>>(a, groups, tiles * groups);
@@ -441,13 +460,17 @@ int launch_crosscorr_peak(const float2* pmap, float2* cc, int nx, int ny, float*
   FFTPlan px, py;
   if (!get_fft_plan(nx, &px) || !get_fft_plan(ny, &py)) return -1;
   int nl = std::max(1, std::min(ny, kMaxElems / nx));
-  size_t sm1 = (size_t)2 * nl * nx * sizeof(float2);
-  cudaFuncSetAttribute(k_fft_rows<-1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
-  k_fft_rows<-1, true><<<(ny + nl - 1) / nl, kThreads, sm1, s>>>(pmap, cc, nx, ny, px, nl);
+  size_t sm1 = fft_stage_smem(nx, nl, nl * (nx + 1), kThreads);
+  dispatch_fft_len(kSiteCorrRows, nx, [&]<int NF>() {
+    cudaFuncSetAttribute(k_fft_rows<-1, true, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
+    k_fft_rows<-1, true, NF><<<(ny + nl - 1) / nl, kThreads, sm1, s>>>(pmap, cc, nx, ny, px, nl);
+  });
   int W = std::max(1, std::min(32, kMaxElems / ny));
-  size_t sm2 = (size_t)2 * W * ny * sizeof(float2);
-  cudaFuncSetAttribute(k_fft_cols2<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
-  k_fft_cols2<-1><<<(nx + W - 1) / W, kThreads, sm2, s>>>(cc, ny, nx, py, W);
+  size_t sm2 = fft_stage_smem(ny, W, (W + 1) * ny, kThreads);
+  dispatch_fft_len(kSiteCorrCols, ny, [&]<int NF>() {
+    cudaFuncSetAttribute(k_fft_cols2<-1, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+    k_fft_cols2<-1, NF><<<(nx + W - 1) / W, kThreads, sm2, s>>>(cc, ny, nx, py, W);
+  });
   int nb = 256;
   k_argmax_partial<<<nb, 256, 0, s>>>(cc, nx * ny, blockval, blockidx);
   k_argmax_final<<<1, 256, 0, s>>>(cc, nx, ny, blockval, blockidx, nb, peak);

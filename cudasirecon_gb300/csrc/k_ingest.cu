@@ -14,6 +14,7 @@
 #include <algorithm>
 
 #include "kernels.h"
+#include "reg_fft.cuh"
 
 namespace simrecon {
 
@@ -37,9 +38,32 @@ __device__ __forceinline__ float flat(const T* __restrict__ plane, const IngestA
   return (v - bg - a.bgextra) * sl * a.inscale;
 }
 
+// VEC consecutive raw pixels of row y starting at x (x % VEC == 0), as floats
+template <typename T, int VEC>
+__device__ __forceinline__ void load_vec(const T* __restrict__ plane, int nx, int y, int x, float* out)
+{
+  const T* src = plane + (size_t)y * nx + x;
+  if constexpr (sizeof(T) == 2 && VEC == 8) {
+    uint4 u = __ldg((const uint4*)src);
+    const unsigned short* h = (const unsigned short*)&u;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) out[i] = (float)h[i];
+  } else if constexpr (sizeof(T) == 4 && VEC == 4) {
+    float4 f = __ldg((const float4*)src);
+    out[0] = f.x;
+    out[1] = f.y;
+    out[2] = f.z;
+    out[3] = f.w;
+  } else {
+#pragma unroll
+    for (int i = 0; i < VEC; ++i) out[i] = (float)src[i];
+  }
+}
+
 // One CTA: `nl` complex lines = 2*nl rows [y0, y0 + 2 nl) of plane `pl`.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_ingest_x(IngestArgs a, FFTPlan plan, int nl)
+// Line l (rows y0+2l, y0+2l+1 as real / imaginary parts) sits at sm[l*ldl].
+template <typename T, int VEC, int NF>
+__global__ void __launch_bounds__(kThreads) k_ingest_x(IngestArgs a, FFTPlan plan, int nl, int ldl)
 {
   extern __shared__ float2 sm[];
   __shared__ float diffr[2 * 256];
@@ -50,31 +74,48 @@ __global__ void __launch_bounds__(kThreads) k_ingest_x(IngestArgs a, FFTPlan pla
   const int p = dp % a.nphases, d = dp / a.nphases;
   const int y0 = blockIdx.x * 2 * nl;
   const T* plane = (const T*)a.raw + (size_t)raw_section(d, p, z, a.nz, a.ndirs, a.nphases, a.fastSI) * nx * ny;
-  float* smr = (float*)sm;  // real view: row r at x -> smr[2*((r>>1)*nx + x) + (r&1)]
+  float* smr = (float*)sm;  // row r at x -> smr[2*((r>>1)*ldl + x) + (r&1)]
   const int napo = a.napodize;
   const int nrows = 2 * nl;
-  // 1) flat-field + top/bottom edge blend (apodize_x_kernel)
-  for (int t = threadIdx.x; t < nrows * nx; t += blockDim.x) {
-    int r = t / nx, x = t - r * nx;
-    int y = y0 + r;
-    float v = 0.f;
+  const int nchunk = nx / VEC;
+  const bool plainbg = !a.bg && !a.slope;
+  // 1) flat-field + top/bottom edge blend (apodize_x_kernel), VEC pixels per thread
+  for (int t = threadIdx.x; t < nrows * nchunk; t += blockDim.x) {
+    const int r = t / nchunk, x0 = (t - r * nchunk) * VEC;
+    const int y = y0 + r;
+    float v[VEC];
     if (y < ny) {
-      v = flat(plane, a, y, x);
-      bool top = y < napo, bot = (ny - 1 - y) < napo;
-      if (top || bot) {
-        float diff = (flat(plane, a, ny - 1, x) - flat(plane, a, 0, x)) / 2.0f;
-        if (top) v += diff * a.apofact[y];
-        if (bot) v -= diff * a.apofact[ny - 1 - y];
+      if (plainbg) {
+        load_vec<T, VEC>(plane, nx, y, x0, v);
+#pragma unroll
+        for (int i = 0; i < VEC; ++i) v[i] = (v[i] - a.bgconst - a.bgextra) * 1.0f * a.inscale;
+      } else {
+#pragma unroll
+        for (int i = 0; i < VEC; ++i) v[i] = flat(plane, a, y, x0 + i);
       }
+      const bool top = y < napo, bot = (ny - 1 - y) < napo;
+      if (top || bot) {
+#pragma unroll
+        for (int i = 0; i < VEC; ++i) {
+          float diff = (flat(plane, a, ny - 1, x0 + i) - flat(plane, a, 0, x0 + i)) / 2.0f;
+          if (top) v[i] += diff * a.apofact[y];
+          if (bot) v[i] -= diff * a.apofact[ny - 1 - y];
+        }
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < VEC; ++i) v[i] = 0.f;
     }
-    smr[2 * ((r >> 1) * nx + x) + (r & 1)] = v;
+    float* dst = smr + 2 * ((r >> 1) * ldl + x0) + (r & 1);
+#pragma unroll
+    for (int i = 0; i < VEC; ++i) dst[2 * i] = v[i];
   }
   __syncthreads();
   // 2) left/right edge blend (apodize_y_kernel) using the blended row ends
   if (napo > 0) {
     for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
-      float e0 = smr[2 * ((r >> 1) * nx + 0) + (r & 1)];
-      float e1 = smr[2 * ((r >> 1) * nx + nx - 1) + (r & 1)];
+      float e0 = smr[2 * ((r >> 1) * ldl + 0) + (r & 1)];
+      float e1 = smr[2 * ((r >> 1) * ldl + nx - 1) + (r & 1)];
       diffr[r] = (e1 - e0) / 2.0f;
     }
     __syncthreads();
@@ -84,44 +125,46 @@ __global__ void __launch_bounds__(kThreads) k_ingest_x(IngestArgs a, FFTPlan pla
       int x = q < napo ? q : nx - 1 - (q - napo);
       int l = q < napo ? q : q - napo;
       float f = diffr[r] * a.apofact[l];
-      float* e = &smr[2 * ((r >> 1) * nx + x) + (r & 1)];
+      float* e = &smr[2 * ((r >> 1) * ldl + x) + (r & 1)];
       if (q < napo) *e += f;
       else *e -= f;
     }
   }
   __syncthreads();
   // 3) forward FFT along x of the packed lines
-  const float2* res = fft_lines<-1>(sm, sm + nl * nx, plan, nl, nx, 1);
+  const float2* res = fft_dispatch<NF, -1>(sm, sm + nl * ldl, plan, nl, ldl, 1);
   // 4) split the two real transforms, keep kx in [0, nx/2]
+  float2* dst = a.spec + (size_t)pl * ny * nxh;
   for (int t = threadIdx.x; t < nl * nxh; t += blockDim.x) {
     int l = t / nxh, k = t - l * nxh;
-    float2 zk = res[l * nx + k];
-    float2 zn = res[l * nx + (nx - k) % nx];
+    float2 zk = res[l * ldl + k];
+    float2 zn = res[l * ldl + (nx - k) % nx];
     float2 A = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
     float2 B = make_float2(0.5f * (zk.y + zn.y), -0.5f * (zk.x - zn.x));
     int y = y0 + 2 * l;
-    float2* dst = a.spec + (size_t)pl * ny * nxh;
     if (y < ny) dst[(size_t)y * nxh + k] = A;
     if (y + 1 < ny) dst[(size_t)(y + 1) * nxh + k] = B;
   }
 }
 
 // Forward/inverse FFT along the middle axis of [nplanes][n][ncol], in place.
-template <int DIR>
+// Tile [n][W] with pitch W+1 (odd: conflict-free strided lane reads).
+template <int DIR, int NF>
 __global__ void __launch_bounds__(kThreads) k_fft_cols(float2* data, int n, int ncol, FFTPlan plan, int W)
 {
   extern __shared__ float2 sm[];
   const int c0 = blockIdx.x * W;
+  const int ld = W + 1;
   float2* base = data + (size_t)blockIdx.y * n * ncol;
   for (int t = threadIdx.x; t < n * W; t += blockDim.x) {
     int i = t / W, w = t - i * W;
-    sm[t] = (c0 + w < ncol) ? base[(size_t)i * ncol + c0 + w] : make_float2(0.f, 0.f);
+    sm[i * ld + w] = (c0 + w < ncol) ? base[(size_t)i * ncol + c0 + w] : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  const float2* res = fft_lines<DIR>(sm, sm + n * W, plan, W, 1, W);
+  const float2* res = fft_dispatch<NF, DIR>(sm, sm + n * ld, plan, W, 1, ld);
   for (int t = threadIdx.x; t < n * W; t += blockDim.x) {
     int i = t / W, w = t - i * W;
-    if (c0 + w < ncol) base[(size_t)i * ncol + c0 + w] = res[t];
+    if (c0 + w < ncol) base[(size_t)i * ncol + c0 + w] = res[i * ld + w];
   }
 }
 
@@ -145,6 +188,7 @@ __global__ void k_rescale(const float2* __restrict__ spec, int ny, int nxh, int 
 
 // Separation + forward z FFT.  One CTA = (ky, W columns of kx) of one
 // direction; shared tile [z][band][w].
+template <int NF>
 __global__ void __launch_bounds__(kThreads) k_separate(float2* spec, const float* __restrict__ scale,
                                                        const float* __restrict__ sepmat, int ny, int nxh, int nz,
                                                        int nph, FFTPlan plan, int W)
@@ -157,7 +201,7 @@ __global__ void __launch_bounds__(kThreads) k_separate(float2* spec, const float
   const size_t plane = (size_t)ny * nxh;
   float2* dbase = spec + (size_t)d * nph * nz * plane + (size_t)ky * nxh + c0;
   const float* dscale = scale + d * nph * nz;
-  const int ld = nph * W;
+  const int ld = nph * W + 1;  // odd pitch
   for (int t = threadIdx.x; t < nz * W; t += blockDim.x) {
     int z = t / W, w = t - z * W;
     float2 in[kMaxPhases];
@@ -179,15 +223,18 @@ __global__ void __launch_bounds__(kThreads) k_separate(float2* spec, const float
   }
   __syncthreads();
   const float2* res = sm;
-  if (nz > 1) res = fft_lines<-1>(sm, sm + nz * ld, plan, nph * W, 1, ld);
-  for (int t = threadIdx.x; t < nz * nph * W; t += blockDim.x) {
-    int z = t / ld, r = t - z * ld;
+  if (nz > 1) res = fft_dispatch<NF, -1>(sm, sm + nz * ld, plan, nph * W, 1, ld);
+  const int lw = nph * W;
+  for (int t = threadIdx.x; t < nz * lw; t += blockDim.x) {
+    int z = t / lw, r = t - z * lw;
     int b = r / W, w = r - b * W;
-    if (c0 + w < nxh) dbase[((size_t)b * nz + z) * plane + w] = res[t];
+    if (c0 + w < nxh) dbase[((size_t)b * nz + z) * plane + w] = res[z * ld + r];
   }
 }
 
 }  // namespace
+
+static size_t fft_smem(int n, int lines, int elems) { return fft_stage_smem(n, lines, elems, kThreads); }
 
 int launch_ingest(const IngestArgs& a, cudaStream_t s, long long* launches)
 {
@@ -195,27 +242,42 @@ int launch_ingest(const IngestArgs& a, cudaStream_t s, long long* launches)
   if (!get_fft_plan(a.nx, &px) || !get_fft_plan(a.ny, &py)) return -1;
   const int nxh = a.nx / 2 + 1;
   const int nplanes = a.ndirs * a.nphases * a.nz;
+  const int ldl = a.nx + 1;
   int nl = std::max(1, std::min(kMaxElems / a.nx, 256));
   nl = std::min(nl, (a.ny + 1) / 2);
-  size_t smx = (size_t)2 * nl * a.nx * sizeof(float2);
+  size_t smx = fft_smem(a.nx, nl, nl * ldl);
   dim3 gx((a.ny + 2 * nl - 1) / (2 * nl), nplanes);
   KernelTimer* kt = kernel_timer();
   const double specb = (double)nplanes * a.ny * nxh * sizeof(float2);
   if (kt) kt->begin(s);
-  if (a.raw_is_u16) {
-    cudaFuncSetAttribute(k_ingest_x<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
-    k_ingest_x<uint16_t><<<gx, kThreads, smx, s>>>(a, px, nl);
-  } else {
-    cudaFuncSetAttribute(k_ingest_x<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
-    k_ingest_x<float><<<gx, kThreads, smx, s>>>(a, px, nl);
-  }
+  dispatch_fft_len(kSiteIngestX, a.nx, [&]<int NF>() {
+    if (a.raw_is_u16) {
+      if (a.nx % 8 == 0) {
+        cudaFuncSetAttribute(k_ingest_x<uint16_t, 8, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+        k_ingest_x<uint16_t, 8, NF><<<gx, kThreads, smx, s>>>(a, px, nl, ldl);
+      } else {
+        cudaFuncSetAttribute(k_ingest_x<uint16_t, 1, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+        k_ingest_x<uint16_t, 1, 0><<<gx, kThreads, smx, s>>>(a, px, nl, ldl);
+      }
+    } else {
+      if (a.nx % 4 == 0) {
+        cudaFuncSetAttribute(k_ingest_x<float, 4, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+        k_ingest_x<float, 4, NF><<<gx, kThreads, smx, s>>>(a, px, nl, ldl);
+      } else {
+        cudaFuncSetAttribute(k_ingest_x<float, 1, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+        k_ingest_x<float, 1, 0><<<gx, kThreads, smx, s>>>(a, px, nl, ldl);
+      }
+    }
+  });
   if (kt) kt->end("k_ingest_x", s, (double)nplanes * a.nx * a.ny * (a.raw_is_u16 ? 2 : 4) + specb);
   int W = std::max(1, std::min(32, kMaxElems / a.ny));
-  size_t smy = (size_t)2 * W * a.ny * sizeof(float2);
+  size_t smy = fft_smem(a.ny, W, a.ny * (W + 1));
   dim3 gy((nxh + W - 1) / W, nplanes);
-  cudaFuncSetAttribute(k_fft_cols<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
   if (kt) kt->begin(s);
-  k_fft_cols<-1><<<gy, kThreads, smy, s>>>(a.spec, a.ny, nxh, py, W);
+  dispatch_fft_len(kSiteIngestY, a.ny, [&]<int NF>() {
+    cudaFuncSetAttribute(k_fft_cols<-1, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
+    k_fft_cols<-1, NF><<<gy, kThreads, smy, s>>>(a.spec, a.ny, nxh, py, W);
+  });
   if (kt) kt->end("k_fft_y", s, 2 * specb);
   if (launches) *launches += 2;
   return (int)cudaGetLastError();
@@ -237,13 +299,15 @@ int launch_separate(float2* spec, const float* scale, const float* sepmat, int n
   if (nphases > kMaxPhases) return -1;
   const int nxh = nx / 2 + 1;
   int W = 32;
-  while (W > 1 && nphases * W * nz > kMaxElems) W >>= 1;
-  size_t sm = (size_t)2 * nphases * W * nz * sizeof(float2);
+  while (W > 1 && (nphases * W + 1) * nz > kMaxElems) W >>= 1;
+  size_t sm = fft_smem(nz, nphases * W, (nphases * W + 1) * nz);
   dim3 g((nxh + W - 1) / W, ny, ndirs);
-  cudaFuncSetAttribute(k_separate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   KernelTimer* kt = kernel_timer();
   if (kt) kt->begin(s);
-  k_separate<<<g, kThreads, sm, s>>>(spec, scale, sepmat, ny, nxh, nz, nphases, pz, W);
+  dispatch_fft_len(kSiteSeparateZ, nz, [&]<int NF>() {
+    cudaFuncSetAttribute(k_separate<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_separate<NF><<<g, kThreads, sm, s>>>(spec, scale, sepmat, ny, nxh, nz, nphases, pz, W);
+  });
   if (kt) kt->end("k_separate", s, 2.0 * ndirs * nphases * nz * (double)ny * nxh * sizeof(float2));
   if (launches) *launches += 1;
   return (int)cudaGetLastError();

@@ -6,26 +6,34 @@
 
 #include "cudasirecon.h"
 #include "kernels.h"
+#include "reg_fft.cuh"
 
 namespace simrecon {
 
 namespace {
-template <int DIR>
+template <int DIR, int NF>
 __global__ void k_fft_selftest(float2* data, int n, int nl, int columns, FFTPlan plan)
 {
   extern __shared__ float2 sm[];
   float2* base = data + (size_t)blockIdx.x * nl * n;
+  const int ldc = nl + 1, ldr = n + 1;  // odd pitches, as the reconstruction kernels use
   for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
     int l = t / n, i = t - l * n;
-    sm[columns ? i * nl + l : t] = base[t];
+    sm[columns ? i * ldc + l : l * ldr + i] = base[t];
   }
   __syncthreads();
-  const float2* res = columns ? fft_lines<DIR>(sm, sm + nl * n, plan, nl, 1, nl)
-                              : fft_lines<DIR>(sm, sm + nl * n, plan, nl, n, 1);
+  const int elems = columns ? n * ldc : nl * ldr;
+  const float2* res = columns ? fft_dispatch<NF, DIR>(sm, sm + elems, plan, nl, 1, ldc)
+                              : fft_dispatch<NF, DIR>(sm, sm + elems, plan, nl, ldr, 1);
   for (int t = threadIdx.x; t < nl * n; t += blockDim.x) {
     int l = t / n, i = t - l * n;
-    base[t] = res[columns ? i * nl + l : t];
+    base[t] = res[columns ? i * ldc + l : l * ldr + i];
   }
+}
+size_t selftest_smem(int n, int nl, int columns)
+{
+  int elems = columns ? n * (nl + 1) : nl * (n + 1);
+  return fft_stage_smem(n, nl, elems, kFftThreads);
 }
 }  // namespace
 
@@ -33,16 +41,18 @@ int launch_fft_selftest(float2* data, int n, int nlines, int inverse, int column
 {
   FFTPlan p;
   if (!get_fft_plan(n, &p)) return -1;
-  int nl = std::max(1, std::min(nlines, kFftElems / n));
+  int nl = std::max(1, std::min(nlines, kFftElems / (n + 1)));
   while (nlines % nl) --nl;
-  size_t sm = (size_t)2 * nl * n * sizeof(float2);
-  if (inverse) {
-    cudaFuncSetAttribute(k_fft_selftest<+1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_fft_selftest<+1><<<nlines / nl, kFftThreads, sm, s>>>(data, n, nl, columns, p);
-  } else {
-    cudaFuncSetAttribute(k_fft_selftest<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_fft_selftest<-1><<<nlines / nl, kFftThreads, sm, s>>>(data, n, nl, columns, p);
-  }
+  size_t sm = selftest_smem(n, nl, columns);
+  dispatch_fft_len(kSiteSelfTest, n, [&]<int NF>() {
+    if (inverse) {
+      cudaFuncSetAttribute(k_fft_selftest<+1, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      k_fft_selftest<+1, NF><<<nlines / nl, kFftThreads, sm, s>>>(data, n, nl, columns, p);
+    } else {
+      cudaFuncSetAttribute(k_fft_selftest<-1, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      k_fft_selftest<-1, NF><<<nlines / nl, kFftThreads, sm, s>>>(data, n, nl, columns, p);
+    }
+  });
   return (int)cudaGetLastError();
 }
 
@@ -155,16 +165,18 @@ extern "C" int SRX_fftLinesNoAlloc(const float* in, float* out, int n, int nline
   k_noalloc_twiddles<<<(n + 255) / 256, 256>>>(tw, n);
   e = cudaMemcpy(data, in, bytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return noalloc_fail("SRX_fftLinesNoAlloc: input copy", e);
-  int nl = std::max(1, std::min(nlines, kFftElems / n));
+  int nl = std::max(1, std::min(nlines, kFftElems / (n + 1)));
   while (nlines % nl) --nl;
-  size_t sm = (size_t)2 * nl * n * sizeof(float2);
-  if (inverse) {
-    cudaFuncSetAttribute(k_fft_selftest<+1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_fft_selftest<+1><<<nlines / nl, kFftThreads, sm>>>(data, n, nl, columns, p);
-  } else {
-    cudaFuncSetAttribute(k_fft_selftest<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_fft_selftest<-1><<<nlines / nl, kFftThreads, sm>>>(data, n, nl, columns, p);
-  }
+  size_t sm = selftest_smem(n, nl, columns);
+  dispatch_fft_len(kSiteSelfTest, n, [&]<int NF>() {
+    if (inverse) {
+      cudaFuncSetAttribute(k_fft_selftest<+1, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      k_fft_selftest<+1, NF><<<nlines / nl, kFftThreads, sm>>>(data, n, nl, columns, p);
+    } else {
+      cudaFuncSetAttribute(k_fft_selftest<-1, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      k_fft_selftest<-1, NF><<<nlines / nl, kFftThreads, sm>>>(data, n, nl, columns, p);
+    }
+  });
   e = cudaGetLastError();
   if (e != cudaSuccess) return noalloc_fail("SRX_fftLinesNoAlloc: launch", e);
   e = cudaMemcpy(out, data, bytes, cudaMemcpyDeviceToHost);

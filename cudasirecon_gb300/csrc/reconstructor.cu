@@ -832,6 +832,10 @@ void SIM_Reconstructor::fitk0andmodamps(int d)
   float deltaangle = 0.001;
   float deltamag = 0.1 / (std::max(nx_, ny_) * opt.ip.dxy);
   const int K = 12;
+  // Upper bound on each climb (the reference's loops have none): 4096 steps
+  // is 4 rad of angle or 400 frequency pixels of magnitude, far past any
+  // physical maximum, so it only ends a climb whose amplitude never peaks.
+  constexpr int kMaxClimbSteps = 4096;
   // both directions of the angle search in one batch
   prefetch_line(fitorder1, fitorder2, true, k0mag, k0angle, deltaangle, K, +1);
   prefetch_line(fitorder1, fitorder2, true, k0mag, k0angle, deltaangle, K, -1);
@@ -841,7 +845,7 @@ void SIM_Reconstructor::fitk0andmodamps(int d)
   float amp1 = 0, x1 = 0.0, a;
   int steps = 0;
   if (amp3 > amp2) {
-    while (amp3 > amp2) {
+    while (amp3 > amp2 && steps < kMaxClimbSteps) {
       amp1 = amp2;
       x1 = x2;
       amp2 = amp3;
@@ -859,7 +863,7 @@ void SIM_Reconstructor::fitk0andmodamps(int d)
     a = x3;
     x3 = x2;
     x2 = a;
-    while (amp3 > amp2) {
+    while (amp3 > amp2 && steps < kMaxClimbSteps) {
       amp1 = amp2;
       x1 = x2;
       amp2 = amp3;
@@ -884,7 +888,7 @@ void SIM_Reconstructor::fitk0andmodamps(int d)
   amp3 = getmodamp(d, angle, mag, fitorder1, fitorder2, redoarrays, &modamp);
   steps = 0;
   if (amp3 > amp2) {
-    while (amp3 > amp2) {
+    while (amp3 > amp2 && steps < kMaxClimbSteps) {
       amp1 = amp2;
       x1 = x2;
       amp2 = amp3;
@@ -902,7 +906,7 @@ void SIM_Reconstructor::fitk0andmodamps(int d)
     a = x3;
     x3 = x2;
     x2 = a;
-    while (amp3 > amp2) {
+    while (amp3 > amp2 && steps < kMaxClimbSteps) {
       amp1 = amp2;
       x1 = x2;
       amp2 = amp3;
