@@ -80,6 +80,10 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.SRX_pinHost.argtypes = [vp, C.c_size_t]
     lib.SRX_unpinHost.restype = ip
     lib.SRX_unpinHost.argtypes = [vp]
+    lib.SRX_makeOTF.restype = ip
+    lib.SRX_makeOTF.argtypes = [fp, ip, ip, ip, ip, C.POINTER(C.c_char_p), fp, C.c_size_t, C.POINTER(C.c_int)]
+    lib.SRX_makeotfMain.restype = ip
+    lib.SRX_makeotfMain.argtypes = [ip, C.POINTER(C.c_char_p)]
     _lib = lib
     return lib
 
@@ -131,6 +135,37 @@ def write_tiff_float(path: str, pages: np.ndarray) -> None:
         out += pages[p].tobytes()
     with open(path, "wb") as f:
         f.write(out)
+
+
+def read_tiff_float(path: str) -> np.ndarray:
+    """Read an uncompressed little-endian 32-bit float multi-page TIFF (any
+    strip layout) into float32 [depth][height][width]."""
+    import struct
+    with open(path, "rb") as f:
+        buf = f.read()
+    if buf[:4] != b"II*\x00":
+        raise ValueError("not a little-endian classic TIFF")
+    (off,) = struct.unpack_from("<I", buf, 4)
+    pages = []
+    while off:
+        (n,) = struct.unpack_from("<H", buf, off)
+        tags = {}
+        for i in range(n):
+            tag, typ, cnt, val = struct.unpack_from("<HHII", buf, off + 2 + 12 * i)
+            size = {3: 2, 4: 4}.get(typ, 4)
+            if cnt * size <= 4:
+                fmt = "<" + ("H" if typ == 3 else "I") * cnt
+                vals = list(struct.unpack_from(fmt, buf, off + 2 + 12 * i + 8))
+            else:
+                vals = list(struct.unpack_from("<" + ("H" if typ == 3 else "I") * cnt, buf, val))
+            tags[tag] = vals
+        w, h = tags[256][0], tags[257][0]
+        if tags.get(258, [32])[0] != 32 or tags.get(259, [1])[0] != 1 or tags.get(339, [3])[0] != 3:
+            raise ValueError("only uncompressed float32 TIFF pages are supported")
+        data = b"".join(buf[o:o + c] for o, c in zip(tags[273], tags[279]))
+        pages.append(np.frombuffer(data, "<f4", count=w * h).reshape(h, w))
+        (off,) = struct.unpack_from("<I", buf, off + 2 + 12 * n)
+    return np.stack(pages).astype(np.float32)
 
 
 def _err(lib) -> str:
@@ -287,3 +322,37 @@ def fft_selftest(x: np.ndarray, inverse: bool = False, columns: bool = False) ->
     if rc != 0:
         raise SIReconError(_err(lib) or f"fft self test failed ({rc})")
     return a
+
+
+def make_otf(psf: np.ndarray, args: list[str] | tuple = ()) -> np.ndarray:
+    """makeotf on the GPU (SRX_makeOTF): PSF stack float [nz*nphases][ny][nx]
+    (phase fastest) and makeotf switches -> the OTF file's float array
+    [bands][nx/2+1][2*nz] ([bands][1][2*(nx/2+1)] for a 2D PSF)."""
+    lib = load_library()
+    p = np.ascontiguousarray(psf, np.float32)
+    nsec, ny, nx = p.shape
+    args = list(args)
+    argv = (C.c_char_p * max(1, len(args)))(*[a.encode() for a in args])
+    nph = int(args[args.index("-nphases") + 1]) if "-nphases" in args else 5
+    nz = max(1, nsec // max(1, nph))
+    nb = nph if "-5bands" in args else (nph + 1) // 2
+    shape = (nb, nx // 2 + 1, 2 * nz) if nz > 1 else (nb, 1, 2 * (nx // 2 + 1))
+    out = np.empty(shape, np.float32)
+    dims = (C.c_int * 3)()
+    f32p = C.POINTER(C.c_float)
+    if lib.SRX_makeOTF(p.ctypes.data_as(f32p), nx, ny, nsec, len(args), argv, out.ctypes.data_as(f32p), out.size,
+                       dims) != 0:
+        raise SIReconError(_err(lib))
+    if (dims[2], dims[1], dims[0]) != out.shape:
+        raise SIReconError(f"unexpected OTF shape {tuple(dims)}")
+    return out
+
+
+def makeotf_main(argv: list[str]) -> None:
+    """The makeotf program (SRX_makeotfMain) in-process: argv without the
+    program name, e.g. ["psf.tif", "otf.tif", "-angle", "-0.8", ...]."""
+    lib = load_library()
+    full = ["makeotf"] + list(argv)
+    arr = (C.c_char_p * len(full))(*[a.encode() for a in full])
+    if lib.SRX_makeotfMain(len(full), arr) != 0:
+        raise SIReconError(_err(lib))

@@ -4,6 +4,7 @@ All CUDA code is compiled for sm_103a only.  Translation units are compiled
 in parallel into cudasirecon_gb300/_build/; outputs:
   cudasirecon_gb300/libcudasirecon.so
   cudasirecon_gb300/bin/cudasirecon
+  cudasirecon_gb300/bin/makeotf
 """
 from __future__ import annotations
 
@@ -18,8 +19,9 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcudasirecon.so")
 CLI = os.path.join(HERE, "bin", "cudasirecon")
+MAKEOTF = os.path.join(HERE, "bin", "makeotf")
 SOURCES = ["fft_plan.cu", "k_selftest.cu", "k_ingest.cu", "k_fit.cu", "k_assemble.cu", "reconstructor.cu",
-           "params.cpp", "image_io.cpp", "capi.cpp"]
+           "makeotf.cu", "params.cpp", "image_io.cpp", "makeotf_io.cpp", "capi.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -28,8 +30,10 @@ def nvcc() -> str:
 
 
 def _flags():
-    return ["-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include"),
-            "-I", CSRC] + ARCH
+    # host code: no contraction into FMA, so float decisions (makeotf's radial
+    # bins, the filter radii) round the same on x86-64 and aarch64 hosts
+    return ["-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+            "-I", os.path.join(ROOT, "include"), "-I", CSRC] + ARCH
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
@@ -63,14 +67,15 @@ def build(force: bool = False, verbose: bool = False) -> str:
         r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stdout.decode(errors="replace"))
-    cli_src = os.path.join(CSRC, "cli_main.cpp")
-    if force or not os.path.exists(CLI) or os.path.getmtime(CLI) < max(os.path.getmtime(LIB),
-                                                                         os.path.getmtime(cli_src)):
-        cmd = [nvcc(), "-x", "c++", cli_src, "-o", CLI, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
-               "-L", HERE, "-lcudasirecon", "-Xlinker", "-rpath=$ORIGIN/.."]
-        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
-        if r.returncode != 0:
-            raise RuntimeError("CLI build failed:\n" + r.stdout.decode(errors="replace"))
+    for exe, main_src in ((CLI, "cli_main.cpp"), (MAKEOTF, "makeotf_main.cpp")):
+        src = os.path.join(CSRC, main_src)
+        if force or not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(LIB),
+                                                                             os.path.getmtime(src)):
+            cmd = [nvcc(), "-x", "c++", src, "-o", exe, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+                   "-L", HERE, "-lcudasirecon", "-Xlinker", "-rpath=$ORIGIN/.."]
+            r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+            if r.returncode != 0:
+                raise RuntimeError(main_src + " build failed:\n" + r.stdout.decode(errors="replace"))
     return LIB
 
 

@@ -9,7 +9,12 @@
 #include <string>
 
 #include "cudasirecon.h"
+#include "makeotf.h"
 #include "reconstructor.h"
+
+namespace simrecon {
+int makeotf_main(int argc, const char* const* argv, std::string* err);
+}
 
 namespace {
 thread_local std::string g_last_error;
@@ -204,6 +209,54 @@ int SRX_fftSelfTest(float* data, int n, int nlines, int inverse, int columns)
     cudaError_t e = cudaDeviceSynchronize();
     cudaFree(d);
     if (e != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e));
+  });
+  return rc;
+}
+
+int SRX_makeOTF(const float* psf, int nx, int ny, int nsections, int nargs, const char* const* args, float* out,
+                size_t out_floats, int* dims)
+{
+  int rc = -1;
+  guarded([&] {
+    simrecon::MakeOtfOptions o;
+    std::string err;
+    if (!psf || nx <= 0 || ny <= 0 || nsections <= 0 || nargs < 0 || (nargs > 0 && !args)) {
+      g_last_error = "SRX_makeOTF: invalid arguments";
+      return;
+    }
+    if (!simrecon::makeotf_parse_switches(nargs, args, &o, &err)) {
+      g_last_error = err;
+      return;
+    }
+    simrecon::OtfResult r;
+    if (!simrecon::makeotf_run(psf, nx, ny, nsections, o, &r, &err)) {
+      g_last_error = err;
+      return;
+    }
+    if (dims) {
+      dims[0] = r.width;
+      dims[1] = r.height;
+      dims[2] = r.depth;
+    }
+    if (out) {
+      if (out_floats < r.data.size()) {
+        g_last_error = "SRX_makeOTF: output buffer too small (" + std::to_string(r.data.size()) + " floats needed)";
+        return;
+      }
+      std::memcpy(out, r.data.data(), r.data.size() * sizeof(float));
+    }
+    rc = 0;
+  });
+  return rc;
+}
+
+int SRX_makeotfMain(int argc, char** argv)
+{
+  int rc = -1;
+  guarded([&] {
+    std::string err;
+    rc = simrecon::makeotf_main(argc, argv, &err);
+    if (rc != 0) g_last_error = err;
   });
   return rc;
 }

@@ -171,6 +171,50 @@ def simulate(nx: int, ny: int, nz: int, optics: Optics | None = None, seed: int 
     return Acquisition(raw=raw, modamps=m)
 
 
+def bead_psf_stack(nx: int, ny: int, nz: int, optics: Optics | None = None, nphases: int | None = None,
+                   peak_photons: float = 1e5, background: float = 100.0, seed: int = 4,
+                   offset_px: tuple = (0.3, -0.2, 0.15), pattern_phase: float = 0.3,
+                   m1: float = 0.9, m2: float = 0.8) -> np.ndarray:
+    """SIM PSF stack of one sub-resolution bead: the input of makeotf.
+
+    float32 [nz * nphases][ny][nx], sections phase-fastest (section =
+    z * nphases + phase).  The bead sits at the stack centre plus a
+    sub-pixel offset (x, y, z in pixels) and the pattern moves with the
+    focal plane, so with pattern phase phi0 at the bead the section at
+    phase p is
+      3D (nz > 1, 3-beam):  det0 (1 + m2 cos(2 phi_p + 2 phi0)) + m1 cos(phi_p + phi0) det1
+      2D (nz = 1, 2-beam):  det0 (1 + m1 cos(phi_p + phi0))
+    with det0 the widefield PSF at the bead and det1 the PSF times
+    cos(2 pi kz1 (z - z_bead)).  Poisson noise on a constant background.
+    """
+    optics = optics or Optics()
+    nph = nphases or optics.nphases
+    rng = np.random.default_rng(seed)
+    psf = widefield_psf(nx, ny, nz, optics).astype(np.float64)
+    fx = np.fft.fftfreq(nx)[None, None, :]
+    fy = np.fft.fftfreq(ny)[None, :, None]
+    fz = np.fft.fftfreq(nz)[:, None, None]
+    cz = (nz // 2 + offset_px[2]) if nz > 1 else 0.0
+    shift = np.exp(-2j * np.pi * (fx * (nx // 2 + offset_px[0]) + fy * (ny // 2 + offset_px[1]) + fz * cz))
+    det0 = np.real(np.fft.ifftn(np.fft.fftn(psf) * shift))
+    stack = np.empty((nz, nph, ny, nx), np.float64)
+    if nz > 1:
+        zs = np.fft.fftfreq(nz, d=1.0 / nz) * optics.dz
+        psf1 = psf * np.cos(2 * np.pi * optics.kz1() * zs)[:, None, None]
+        det1 = np.real(np.fft.ifftn(np.fft.fftn(psf1) * shift))
+        for p in range(nph):
+            phi = 2 * np.pi * p / nph
+            stack[:, p] = det0 * (1.0 + m2 * np.cos(2 * phi + 2 * pattern_phase)) + \
+                m1 * np.cos(phi + pattern_phase) * det1
+    else:
+        for p in range(nph):
+            phi = 2 * np.pi * p / nph
+            stack[:, p] = det0 * (1.0 + m1 * np.cos(phi + pattern_phase))
+    stack *= peak_photons / max(float(stack.max()), 1e-30)
+    noisy = rng.poisson(np.maximum(stack, 0.0)).astype(np.float64) + background
+    return noisy.reshape(nz * nph, ny, nx).astype(np.float32)
+
+
 def ra_otf(optics: Optics, nx_psf: int = 128, nz_psf: int = 64, dz_psf: float | None = None,
            norders: int = 3, twod: bool = False) -> np.ndarray:
     """Rotationally averaged OTF pages in the layout of an OTF TIFF.

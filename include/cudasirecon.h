@@ -230,6 +230,26 @@ int SRX_fftLinesNoAlloc(const float* in, float* out, int n, int nlines, int inve
 const char* SRX_fftLinesNoAllocError(void);
 int SRX_unpinHost(void* ptr);
 
+/* makeotf.  The reference's makeotf is a program, not a library call
+ * (src/otf/radialft.cpp:82-434); these replace it:
+ *
+ * SRX_makeotfMain: the program itself, with the reference's command line
+ * (radialft.cpp:1381-1553: `makeotf psf otf [switches]`, TIFF or MRC/DV in,
+ * the same format out).  Returns 0 on success, else -1 with the message in
+ * SR_getLastError().
+ *
+ * SRX_makeOTF: the same computation on a PSF stack in host memory, float
+ * [nsections][ny][nx] with the phase fastest (section = z*nphases + phase).
+ * `args` are makeotf's switches without file names (e.g. "-angle", "-0.8",
+ * "-ls", "0.2035", "-xyres", "0.08", "-zres", "0.125").  The result is the
+ * float array the program writes to its OTF TIFF, [dims[2]][dims[1]][dims[0]]
+ * with dims = {width = 2*nz, height = nx/2+1, depth = number of bands}
+ * (width 2*(nx/2+1), height 1 for a 2D PSF).  out may be NULL to query dims;
+ * out_floats is its capacity.  Returns 0 on success, -1 on error. */
+int SRX_makeotfMain(int argc, char** argv);
+int SRX_makeOTF(const float* psf, int nx, int ny, int nsections, int nargs, const char* const* args, float* out,
+                size_t out_floats, int* dims);
+
 #ifdef __cplusplus
 }
 #endif

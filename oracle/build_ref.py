@@ -121,7 +121,86 @@ def build(force: bool = False, verbose: bool = False) -> str | None:
     return LIB
 
 
+# ---------------------------------------------------------------------------
+# makeotf (src/otf/radialft.cpp) reference program, host only
+# ---------------------------------------------------------------------------
+MO_LIB = os.path.join(OUT, "libmakeotf_ref.so")
+MO_STAGED = ["src/otf/radialft.cpp", "src/cudaSirecon/CImg.h"]
+
+MO_CIMG_SHIM = """// include shim for radialft.cpp: the real CImg.h without libtiff; the TIFF
+// calls radialft.cpp makes itself are declared here and defined by the
+// harness, and CImg's save_tiff is routed to its own raw .cimg writer
+#undef cimg_use_tiff
+#include "tiffio_stub.h"
+#include "../src/src/cudaSirecon/CImg.h"
+#define save_tiff save_cimg
+"""
+
+MO_TIFF_STUB = """#pragma once
+#include <cstdarg>
+typedef struct tiff TIFF;
+typedef void (*TIFFErrorHandler)(const char*, const char*, va_list);
+extern "C" {
+TIFFErrorHandler TIFFSetWarningHandler(TIFFErrorHandler);
+TIFFErrorHandler TIFFSetErrorHandler(TIFFErrorHandler);
+TIFF* TIFFOpen(const char*, const char*);
+void TIFFClose(TIFF*);
+}
+"""
+
+MO_FFTW_SHIM = """// the four FFTW3f declarations radialft.cpp uses (radialft.cpp:339-348)
+#pragma once
+typedef float fftwf_complex[2];
+typedef struct fftwf_plan_s* fftwf_plan;
+#define FFTW_ESTIMATE (1U << 6)
+extern "C" {
+void fftwf_plan_with_nthreads(int nthreads);
+fftwf_plan fftwf_plan_dft_r2c_3d(int n0, int n1, int n2, float* in, fftwf_complex* out, unsigned flags);
+void fftwf_execute_dft_r2c(const fftwf_plan p, float* in, fftwf_complex* out);
+void fftwf_destroy_plan(fftwf_plan p);
+}
+"""
+
+
+def build_makeotf(force: bool = False) -> str | None:
+    """Compile the reference makeotf program with the harness into
+    oracle/_ref/libmakeotf_ref.so (g++, the reference's Release flags)."""
+    if os.path.isdir(REF_ROOT):
+        for rel in MO_STAGED:
+            src = os.path.join(REF_ROOT, rel)
+            dst = os.path.join(STAGE, rel)
+            os.makedirs(os.path.dirname(dst), exist_ok=True)
+            if not os.path.exists(dst) or os.path.getmtime(dst) < os.path.getmtime(src):
+                shutil.copyfile(src, dst)
+    if not all(os.path.exists(os.path.join(STAGE, f)) for f in MO_STAGED):
+        return None
+    shim = os.path.join(OUT, "mo_shim")
+    os.makedirs(shim, exist_ok=True)
+    for name, text in (("CImg.h", MO_CIMG_SHIM), ("tiffio_stub.h", MO_TIFF_STUB), ("fftw3.h", MO_FFTW_SHIM)):
+        path = os.path.join(shim, name)
+        if not os.path.exists(path) or open(path).read() != text:
+            with open(path, "w") as f:
+                f.write(text)
+    harness = os.path.join(HERE, "ref_harness", "makeotf_harness.cpp")
+    srcs = [os.path.join(STAGE, "src/otf/radialft.cpp"), harness]
+    if os.path.exists(MO_LIB) and not force:
+        if os.path.getmtime(MO_LIB) >= max(os.path.getmtime(s) for s in srcs):
+            return MO_LIB
+    gxx = shutil.which("g++")
+    if not gxx:
+        return None
+    cmd = [gxx, "-std=c++17", "-O3", "-DNDEBUG", "-Dcimg_display=0", "-Dmain=radialft_reference_main",
+           "-fPIC", "-shared", "-w", "-I", shim, "-o", MO_LIB] + srcs + ["-lpthread", "-Wl,--no-undefined"]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    if r.returncode != 0:
+        sys.stderr.write(" ".join(cmd) + "\n" + r.stdout.decode(errors="replace")[-4000:] + "\n")
+        return None
+    return MO_LIB
+
+
 if __name__ == "__main__":
     lib = build(force="--force" in sys.argv, verbose="-v" in sys.argv)
     print(lib if lib else "reference harness not built")
-    sys.exit(0 if lib else 1)
+    mo = build_makeotf(force="--force" in sys.argv)
+    print(mo if mo else "reference makeotf not built")
+    sys.exit(0 if lib and mo else 1)

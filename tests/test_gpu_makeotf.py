@@ -1,0 +1,87 @@
+"""GPU makeotf (SRX_makeOTF / bin/makeotf) against the reference program's
+outputs (tests/golden/mo_*.npz) and the oracle."""
+import glob
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+pytestmark = pytest.mark.gpu
+
+FIXTURES = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "mo_*.npz")))
+# float32 FFT on the GPU against the reference run with a float64 DFT; the
+# OTF is normalised to 1 at the origin
+REL_L2 = 2e-5
+MAX_ABS = 2e-5
+
+
+def load(path):
+    z = np.load(path)
+    return z["psf"].astype(np.float32), [str(a) for a in z["args"]], z["otf"]
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import cudasirecon_gb300 as cs
+    cs.load_library()
+    return cs
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=[os.path.basename(p)[3:-4] for p in FIXTURES])
+def test_makeotf_matches_reference_program(lib, path):
+    psf, args, ref = load(path)
+    got = lib.make_otf(psf, args)
+    assert got.shape == ref.shape
+    d = got - ref
+    assert np.linalg.norm(d) / np.linalg.norm(ref) <= REL_L2
+    assert np.abs(d).max() <= MAX_ABS
+
+
+def test_makeotf_matches_oracle_fresh_input(lib):
+    import makeotf_oracle as mo
+    from cudasirecon_gb300.synthetic import Optics, bead_psf_stack
+    psf = bead_psf_stack(96, 96, 40, Optics(), peak_photons=5e4, seed=21, offset_px=(0.45, 0.1, -0.35))
+    args = ["-angle", "0.2388", "-ls", "0.21", "-xyres", "0.08", "-zres", "0.125", "-na", "1.42", "-nimm", "1.515",
+            "-wavelength", "528", "-fixorigin", "3", "20"]
+    got = lib.make_otf(psf, args)
+    want = mo.makeotf(psf, mo.MakeOTFOptions.from_args(args))
+    d = got - want
+    assert np.linalg.norm(d) / np.linalg.norm(want) <= REL_L2
+    assert np.abs(d).max() <= MAX_ABS
+
+
+def test_makeotf_deterministic(lib):
+    psf, args, _ = load(FIXTURES[0])
+    a = lib.make_otf(psf, args)
+    b = lib.make_otf(psf, args)
+    assert np.array_equal(a, b)
+
+
+def test_makeotf_cli_tiff_roundtrip(lib, tmp_path):
+    psf, args, ref = load(os.path.join(ROOT, "tests", "golden", "mo_mo3d_64.npz"))
+    ipath, opath = str(tmp_path / "psf.tif"), str(tmp_path / "otf.tif")
+    lib.write_tiff_float(ipath, psf)
+    exe = os.path.join(ROOT, "cudasirecon_gb300", "bin", "makeotf")
+    r = subprocess.run([exe, ipath, opath] + args, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    got = lib.read_tiff_float(opath)
+    assert got.shape == ref.shape
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= REL_L2
+    view = lib.read_tiff_float(str(tmp_path / "otf_OnlyForViewing.tif"))
+    c = got[..., 0::2] + 1j * got[..., 1::2]
+    assert np.allclose(view, np.sqrt(np.abs(c)), rtol=1e-6, atol=1e-7)
+
+
+def test_makeotf_rejects_bad_input(lib):
+    psf, args, _ = load(FIXTURES[0])
+    with pytest.raises(lib.SIReconError):  # sections smaller than the 20-pixel background border
+        lib.make_otf(np.zeros((5, 10, 10), np.float32), args)
+    with pytest.raises(lib.SIReconError):  # wider than high
+        lib.make_otf(np.zeros((5, 32, 48), np.float32), args)
+    with pytest.raises(lib.SIReconError):
+        lib.make_otf(psf, args + ["-2lenses"])
