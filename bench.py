@@ -157,13 +157,21 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary (or None)."""
+def ncu_traffic(kernel, workload, alg_bytes_per_launch):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary
+    (profiles/ncu_traffic.json), or None.  A capture taken on a smaller
+    workload is scaled to this launch by its algorithmic bytes (the kernel's
+    traffic grows in proportion to the slots it processes)."""
     try:
         with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
-            return json.load(f).get(kernel)
+            e = json.load(f).get(kernel)
     except Exception:
         return None
+    if not e:
+        return None
+    if e.get("workload") == workload:
+        return e["dram_bytes_per_launch"]
+    return round(e["dram_bytes_per_launch"] / e["alg_bytes_per_launch"] * alg_bytes_per_launch)
 
 
 def cpu_baseline(vol, otf, cfg, nx, ny, nz):
@@ -251,7 +259,7 @@ def run_gb300(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
     if top:
         name, st = top
         ach = st["alg_bytes"] / (st["ms"] / 1e3) / 1e9
-        tr = ncu_traffic(name)
+        tr = ncu_traffic(name, args.workload, st["alg_bytes"] / max(1, st["launches"]))
         roof = {"kernel": name, "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "peak_source": peak_kind,
                 "traffic": tr, "alg_bytes_per_launch": st["alg_bytes"] / max(1, st["launches"]),
