@@ -181,6 +181,10 @@ __global__ void __launch_bounds__(kThreads) k_filter(FilterArgs a)
   b2[ind] = im;
 }
 
+// One transformed plane: band (dir, order) at signed kz, summed into output
+// plane zout.  dir < 0 marks the order-0 slot of a plane: the order-0 bands
+// of all directions summed before the transforms (their phase ramps are all
+// 1, so the sum commutes with the inverse FFTs).
 struct Slot {
   int dir, order, kz, zout;
 };
@@ -196,8 +200,10 @@ __global__ void __launch_bounds__(kThreads) k_asm_y(AssembleArgs a, const Slot* 
   const int nx = a.nx, ny = a.ny, nz = a.nz, nxh = nx / 2 + 1, Y = a.Y;
   const int c0 = blockIdx.x * W;
   const size_t plane = (size_t)ny * nxh;
-  const float2* br = a.bands + ((size_t)sl.dir * a.nphases + (sl.order == 0 ? 0 : 2 * sl.order - 1)) * nz * plane;
-  const float2* bi = sl.order == 0 ? nullptr : a.bands + ((size_t)sl.dir * a.nphases + 2 * sl.order) * nz * plane;
+  const int d0 = sl.dir < 0 ? 0 : sl.dir;
+  const float2* br = a.bands + ((size_t)d0 * a.nphases + (sl.order == 0 ? 0 : 2 * sl.order - 1)) * nz * plane;
+  const float2* bi = sl.order == 0 ? nullptr : a.bands + ((size_t)d0 * a.nphases + 2 * sl.order) * nz * plane;
+  const size_t dstride = (size_t)a.nphases * nz * plane;  // next direction's band 0
   const int ylo = ny / 2 - 1;  // ky in [-ylo, ny/2]
   const int ld = W + 1;
   for (int t = threadIdx.x; t < Y * W; t += blockDim.x) {
@@ -222,6 +228,12 @@ __global__ void __launch_bounds__(kThreads) k_asm_y(AssembleArgs a, const Slot* 
       size_t indin = (size_t)z * plane + (size_t)y * nxh + x;
       if (sl.order == 0) {
         v = br[indin];
+        if (sl.dir < 0)
+          for (int d = 1; d < a.ndirs; ++d) {
+            float2 u = br[d * dstride + indin];
+            v.x += u.x;
+            v.y += u.y;
+          }
         if (conj) v.y = -v.y;
       } else {
         float2 re = br[indin], im = bi[indin];
@@ -279,6 +291,17 @@ __global__ void __launch_bounds__(kThreads) k_asm_x(AssembleArgs a, const int* _
     const float2* res = fft_dispatch<NF, +1>(sm, sm + lines * ldl, plan, lines, ldl, 1);
     for (int l = 0; l < nb; ++l) {
       const Slot sl = slots[s0 + b0 + l];
+      if (sl.dir < 0) {  // summed order-0 slot: ramp 1, weight 1
+#pragma unroll
+        for (int k = 0; k < kAccPerThread; ++k) {
+          int x = threadIdx.x + k * blockDim.x;
+          if (x < X) {
+            acc[k].x += res[l * ldl + x].x;
+            acc[k].y += res[l * ldl + x].y;
+          }
+        }
+        continue;
+      }
       const int ro = sl.dir * a.norders + sl.order;
       const float w = sl.order == 0 ? 1.f : 2.f;
       float2 ey = a.ey[(size_t)ro * Y + yr];
@@ -301,6 +324,83 @@ __global__ void __launch_bounds__(kThreads) k_asm_x(AssembleArgs a, const int* _
   for (int k = 0; k < kAccPerThread; ++k) {
     int x = threadIdx.x + k * blockDim.x;
     if (x < X) dst[x] = acc[k];
+  }
+}
+
+// Warp-level variant of k_asm_x for the zoomed row lengths with a register
+// path: each group of P lanes owns one output row yr of plane pidx and runs,
+// for every slot of the plane, the zero-padded inverse FFT of the slot's T row
+// in registers (one warp-private exchange, no CTA barrier), the phase ramp
+// and the weighted sum; the row of S is written once.
+template <int X>
+struct XwLanes {
+  static constexpr int P = X == 1024 ? 32 : (X == 512 || X == 256 ? 16 : 0);
+};
+constexpr int kXwWarps = 4;
+
+template <int X>
+__global__ void __launch_bounds__(kXwWarps * 32, 3) k_asm_xw(AssembleArgs a, const int* __restrict__ plane_slot0,
+                                                          const int* __restrict__ plane_nslot,
+                                                          const Slot* __restrict__ slots,
+                                                          const int* __restrict__ plane_zout,
+                                                          const float2* __restrict__ tw)
+{
+  constexpr int P = XwLanes<X>::P, E = X / P, G = 32 / P;
+  constexpr int XB = (P + 1) * E + 1;
+  __shared__ float2 xs[kXwWarps * G * XB];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane / P, p = lane - g * P;
+  const int yr = (blockIdx.x * kXwWarps + warp) * G + g;
+  const bool act = yr < a.Y;
+  const int pidx = blockIdx.y;
+  const int s0 = plane_slot0[pidx], ns = plane_nslot[pidx], zout = plane_zout[pidx];
+  const int nx = a.nx, Y = a.Y, xlo = nx / 2 - 1;
+  float2* xb = xs + (warp * G + g) * XB;
+  float2 acc[E];
+#pragma unroll
+  for (int i = 0; i < E; ++i) acc[i] = make_float2(0.f, 0.f);
+  for (int si = 0; si < ns; ++si) {  // same trip count for every lane of the warp
+    const Slot sl = slots[s0 + si];
+    const float2* trow = a.T + ((size_t)(s0 + si) * Y + (act ? yr : 0)) * nx;
+    float2 v[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int x = p + P * e;
+      const bool in = act && (x <= nx / 2 || x >= X - xlo);
+      v[e] = in ? __ldg(trow + (x <= nx / 2 ? x : x - X) + xlo) : make_float2(0.f, 0.f);
+    }
+    reg_line<X, P, +1>(v, p, xb, tw, true);
+    if (sl.dir < 0) {
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        acc[i].x += v[i].x;
+        acc[i].y += v[i].y;
+      }
+    } else {
+      const int ro = sl.dir * a.norders + sl.order;
+      const float w = sl.order == 0 ? 1.f : 2.f;
+      float2 ey = act ? __ldg(a.ey + (size_t)ro * Y + yr) : make_float2(0.f, 0.f);
+      ey.x *= w;
+      ey.y *= w;
+      const float2* exr = a.ex + (size_t)ro * X;
+#pragma unroll
+      for (int m = 0; m < E / P; ++m)
+#pragma unroll
+        for (int k2 = 0; k2 < P; ++k2) {
+          const int i = m * P + k2;
+          const float2 e = cmul(__ldg(exr + p + P * m + E * k2), ey);
+          const float2 t = cmul(v[i], e);
+          acc[i].x += t.x;
+          acc[i].y += t.y;
+        }
+    }
+  }
+  if (act) {
+    float2* dst = a.S + ((size_t)zout * Y + yr) * X;
+#pragma unroll
+    for (int m = 0; m < E / P; ++m)
+#pragma unroll
+      for (int k2 = 0; k2 < P; ++k2) dst[p + P * m + E * k2] = acc[m * P + k2];
   }
 }
 
@@ -419,15 +519,13 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
   std::vector<unsigned char> zact(a.Z, 0);
   for (int kz : kzs) {
     int start = (int)slots.size();
+    const int az = kz < 0 ? -kz : kz;
+    int zo = kz;
+    if (zo < 0) zo += a.Z;
+    if (az <= a.zdc[0]) slots.push_back(Slot{-1, 0, kz, zo});  // order 0 of all directions, summed
     for (int d = 0; d < a.ndirs; ++d)
-      for (int o = 0; o < a.norders; ++o) {
-        int az = kz < 0 ? -kz : kz;
-        if (az <= a.zdc[o]) {
-          int zo = kz;
-          if (zo < 0) zo += a.Z;
-          slots.push_back(Slot{d, o, kz, zo});
-        }
-      }
+      for (int o = 1; o < a.norders; ++o)
+        if (az <= a.zdc[o]) slots.push_back(Slot{d, o, kz, zo});
     int cnt = (int)slots.size() - start;
     if (cnt > 0) {
       int zo = kz < 0 ? kz + a.Z : kz;
@@ -485,18 +583,29 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
     });
     if (kt) {
       double rd = 0;
-      for (int q = first; q < first + nsl; ++q) rd += (slots[q].order == 0 ? 1 : 2) * (double)a.ny * nx * 8;
+      for (int q = first; q < first + nsl; ++q)
+        rd += (slots[q].dir < 0 ? a.ndirs : (slots[q].order == 0 ? 1 : 2)) * (double)a.ny * nx * 8;
       kt->end("k_asm_y", s, rd + (double)nsl * per_slot * sizeof(float2));
     }
     // k_asm_x reads T[(slot - first)]: pass a shifted T base
     AssembleArgs ax = a;
     ax.T = a.T - (size_t)first * per_slot;
     if (kt) kt->begin(s);
-    dispatch_fft_len(kSiteAsmX, a.X, [&]<int NF>() {
-      cudaFuncSetAttribute(k_asm_x<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
-      k_asm_x<NF><<<dim3(a.Y, (unsigned)(pj - pi)), kThreads, smx, s>>>(ax, d_p0 + pi, d_pn + pi, d_slots,
-                                                                       d_pz + pi, px, xlines);
-    });
+    auto launch_xw = [&]<int XN>() {
+      constexpr int G = 32 / XwLanes<XN>::P;
+      const int rows_per_cta = kXwWarps * G;
+      k_asm_xw<XN><<<dim3((a.Y + rows_per_cta - 1) / rows_per_cta, (unsigned)(pj - pi)), kXwWarps * 32, 0, s>>>(
+          ax, d_p0 + pi, d_pn + pi, d_slots, d_pz + pi, px.tw);
+    };
+    if (a.X == 1024) launch_xw.template operator()<1024>();
+    else if (a.X == 512) launch_xw.template operator()<512>();
+    else if (a.X == 256) launch_xw.template operator()<256>();
+    else
+      dispatch_fft_len(kSiteAsmX, a.X, [&]<int NF>() {
+        cudaFuncSetAttribute(k_asm_x<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+        k_asm_x<NF><<<dim3(a.Y, (unsigned)(pj - pi)), kThreads, smx, s>>>(ax, d_p0 + pi, d_pn + pi, d_slots,
+                                                                         d_pz + pi, px, xlines);
+      });
     if (kt) kt->end("k_asm_x", s, (double)nsl * per_slot * sizeof(float2) + (double)(pj - pi) * a.X * a.Y * 8);
     nl += 2;
     pi = pj;

@@ -410,9 +410,13 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
   const size_t nspec = (size_t)ndirs_ * nph_ * nz_ * ny_ * nxh_;
   const int nzb = 2 * zdc_ovl_ + 1;
   const size_t nxy = (size_t)nx_ * ny_;
-  // assembly scratch: at least all slots of one plane, up to 64 MiB
+  // assembly scratch: every slot of the volume (at most nz planes of
+  // 1 + ndirs*(norders-1) slots) when that fits in 2 GiB, else as many as do
+  // (at least one plane's worth); the slots are processed in plane groups
   const size_t per_slot = (size_t)Y_ * nx_;
-  size_t want_slots = std::max<size_t>((size_t)ndirs_ * norders_, (64ull << 20) / (per_slot * sizeof(float2)));
+  const size_t all_slots = (size_t)nz_ * (1 + (size_t)ndirs_ * (norders_ - 1));
+  size_t want_slots = std::max<size_t>(1 + (size_t)ndirs_ * (norders_ - 1),
+                                       std::min<size_t>(all_slots, (size_t)(2ull << 30) / (per_slot * sizeof(float2))));
   tcap_ = want_slots * per_slot + 65536;
   struct Req {
     void** ptr;
