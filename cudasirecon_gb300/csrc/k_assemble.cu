@@ -35,7 +35,7 @@ __device__ __forceinline__ float dev_suppress(float x)
 {
   float x6 = x * x * x;
   x6 *= x6;
-  return 1.0 / (1 + 20000 / (x6 + 20));
+  return 1.f / (1 + 20000 / (x6 + 20));  // float division: correctly rounded, like the double one rounded
 }
 
 __device__ __forceinline__ float dev_order0damping(float radius, float zindex, float rlimit, int zlimit)
@@ -45,58 +45,100 @@ __device__ __forceinline__ float dev_order0damping(float radius, float zindex, f
   return rfraction * rfraction + zfraction * zfraction * zfraction;
 }
 
-// Wiener scale of pixel (x1, y1, z0) of band (dir, order), the body of
+// Per-launch constants derived on the host from FilterArgs (reciprocals and
+// products the per-term arithmetic would otherwise recompute per element).
+struct FilterK {
+  float termw[kMaxDirs * kMaxOrders];  // |amp|^2 / noisevar (order 0: 1 / noisevar)
+  float rnv[kMaxDirs * kMaxOrders];    // 1 / noisevar
+  float kxo[kMaxDirs * kMaxOrders];    // order * k0x of each direction
+  float kyo[kMaxDirs * kMaxOrders];
+  float rdkrotf;                       // 1 / dkrotf
+  float min_dkr, rmin_dkr, supp_r;     // suppression radius (1/um) and its unit
+  float rrcut;                         // 1 / rdistcutoff
+};
+
+// bilinear RA-OTF lookup at radius kr (otf_lookup's arithmetic with
+// krindex = kr * (1/dkrotf))
+__device__ __forceinline__ float2 otf_lookup_rr(const float2* __restrict__ otf, const OTFView& v, float krindex,
+                                               const OtfKz& z)
+{
+  int ir = (int)floorf(krindex);
+  float ar = krindex - ir;
+  int last = v.nxotf * v.nzotf - 1;
+  int i00 = min(max(ir * v.nzotf + z.iz, 0), last);
+  int i01 = min(max(ir * v.nzotf + z.izp, 0), last);
+  int i10 = min(max((ir + 1) * v.nzotf + z.iz, 0), last);
+  int i11 = min(max((ir + 1) * v.nzotf + z.izp, 0), last);
+  float2 a = __ldg(otf + i00), b = __ldg(otf + i01), c = __ldg(otf + i10), d = __ldg(otf + i11);
+  const float az = z.az;
+  float2 r;
+  r.x = (1 - ar) * (a.x * (1 - az) + b.x * az) + ar * (c.x * (1 - az) + d.x * az);
+  r.y = (1 - ar) * (a.y * (1 - az) + b.y * az) + ar * (c.y * (1 - az) + d.y * az);
+  return r;
+}
+
+// Wiener scale of pixel (x1f, y1f, z0) of band (dir, order): the body of
 // filterbands_kernel1 (gpuFunctionsImpl.cu:1504-1592) without the final
-// conjamp factor.
-__device__ float2 filter_scale(const FilterArgs& a, int order, int x1, int y1, int z0, float rdist1, float x1f,
+// conjamp factor.  ND/NO: compile-time direction and order counts (0: use
+// the runtime values).
+template <int ND, int NO>
+__device__ __forceinline__ float2 filter_scale(const FilterArgs& a, const FilterK& k, int order, int z0, float rdist1, float x1f,
                                float y1f)
 {
-  const int dir = a.dir, no = a.norders;
-  const float kx = order * a.k0[dir].x, ky = order * a.k0[dir].y;
-  const float min_dkr = a.dkx < a.dky ? a.dkx : a.dky;
-  const float suppRadius = a.supp_radius * min_dkr;
-  float xabs = x1f + kx, yabs = y1f + ky;
-  float rdistabs = sqrtf(xabs * xabs + yabs * yabs);
-  float2 otf1 = otf_lookup(a.otf.otf[order], a.otf, x1f, y1f, z0);
+  const int dir = a.dir;
+  const int nd = ND ? ND : a.ndirs, no = NO ? NO : a.norders;
+  const float xabs = x1f + k.kxo[dir * no + order], yabs = y1f + k.kyo[dir * no + order];
+  const OtfKz kzi = otf_kz(a.otf, z0);
+  // order-0 damping's axial part |z0 / zdc0|^3, the same for every term
+  const float zf = fabsf(z0 / (float)a.zdc[0]);
+  const float zf3 = zf * zf * zf;
+  float2 otf1 = otf_lookup_rr(a.otf.otf[order], a.otf, rdist1 * k.rdkrotf, kzi);
   float weight = otf1.x * otf1.x + otf1.y * otf1.y;
   if (order != 0) weight *= a.ampmag2[dir * no + order];
-  float dampfact = 1. / a.noisevar[dir * no + order];
-  if (a.suppress && order != 0 && rdist1 <= suppRadius)
-    dampfact *= dev_suppress(rdist1 / min_dkr);
-  else if (!a.dampen0 && a.suppress && order == 0 && rdist1 <= suppRadius)
-    dampfact *= dev_suppress(rdist1 / min_dkr);
-  else if (a.dampen0 && order == 0)
-    dampfact *= dev_order0damping(rdist1, z0, a.rdistcutoff, a.zdc[0]);
+  float dampfact = k.rnv[dir * no + order];
+  if (a.suppress && order != 0 && rdist1 <= k.supp_r)
+    dampfact *= dev_suppress(rdist1 * k.rmin_dkr);
+  else if (!a.dampen0 && a.suppress && order == 0 && rdist1 <= k.supp_r)
+    dampfact *= dev_suppress(rdist1 * k.rmin_dkr);
+  else if (a.dampen0 && order == 0) {
+    const float rf = rdist1 * k.rrcut;
+    dampfact *= rf * rf + zf3;
+  }
   if (order == 0 && z0 == 0 && a.nokz0) dampfact = 0;
   weight *= dampfact;
   float sumweight = weight;
-  for (int dir2 = 0; dir2 < a.ndirs; dir2++) {
+#pragma unroll
+  for (int dir2 = 0; dir2 < nd; dir2++) {
+#pragma unroll
     for (int order2 = -(no - 1); order2 < no; order2++) {
       if (dir2 == dir && order2 == order) continue;
       if (!a.filteroverlaps && !(order2 == 0 && order == 0)) continue;
-      int ao2 = order2 < 0 ? -order2 : order2;
-      float amp2mag2 = a.ampmag2[dir2 * no + ao2];
-      float kx2 = order2 * a.k0[dir2].x, ky2 = order2 * a.k0[dir2].y;
-      float x2 = xabs - kx2, y2 = yabs - ky2;
-      float rdist2 = sqrtf(x2 * x2 + y2 * y2);
+      const int ao2 = order2 < 0 ? -order2 : order2;
+      const float sx = order2 < 0 ? -k.kxo[dir2 * no + ao2] : k.kxo[dir2 * no + ao2];
+      const float sy = order2 < 0 ? -k.kyo[dir2 * no + ao2] : k.kyo[dir2 * no + ao2];
+      const float x2 = xabs - sx, y2 = yabs - sy;
+      const float rdist2 = sqrtf(x2 * x2 + y2 * y2);
       if (rdist2 < a.rdistcutoff) {
-        float2 otf2 = otf_lookup(a.otf.otf[ao2], a.otf, x2, y2, z0);
-        float w = (otf2.x * otf2.x + otf2.y * otf2.y) / a.noisevar[dir2 * no + ao2];
-        if (order2 != 0) w *= amp2mag2;
-        if (a.suppress && order2 != 0 && rdist2 <= suppRadius)
-          w *= dev_suppress(rdist2 / min_dkr);
-        else if (!a.dampen0 && a.suppress && order2 == 0 && rdist2 <= suppRadius)
-          w *= dev_suppress(rdist2 / min_dkr);
-        else if (a.dampen0 && order2 == 0)
-          w *= dev_order0damping(rdist2, z0, a.rdistcutoff, a.zdc[0]);
+        const float2 otf2 = otf_lookup_rr(a.otf.otf[ao2], a.otf, rdist2 * k.rdkrotf, kzi);
+        float w = (otf2.x * otf2.x + otf2.y * otf2.y) * k.termw[dir2 * no + ao2];
+        if (a.suppress && order2 != 0 && rdist2 <= k.supp_r)
+          w *= dev_suppress(rdist2 * k.rmin_dkr);
+        else if (!a.dampen0 && a.suppress && order2 == 0 && rdist2 <= k.supp_r)
+          w *= dev_suppress(rdist2 * k.rmin_dkr);
+        else if (a.dampen0 && order2 == 0) {
+          const float rf = rdist2 * k.rrcut;
+          w *= rf * rf + zf3;
+        }
         if (a.nokz0 && order2 == 0 && z0 == 0) w = 0.0f;
         sumweight += w;
       }
     }
   }
   sumweight += a.wiener2;
-  float2 scale = make_float2(dampfact * otf1.x / sumweight, dampfact * (-otf1.y) / sumweight);
+  const float f = dampfact / sumweight;
+  float2 scale = make_float2(otf1.x * f, -otf1.y * f);
   if (a.apodizeoutput) {
+    float rdistabs = sqrtf(xabs * xabs + yabs * yabs);
     float rho;
     float zdistabs = abs(z0);
     if (a.zapocutoff > 0)
@@ -106,7 +148,7 @@ __device__ float2 filter_scale(const FilterArgs& a, int order, int x1, int y1, i
       rho = sqrtf((rdistabs / a.apocutoff) * (rdistabs / a.apocutoff));
     if (rho > 1.f) rho = 1.0f;
     float apofact = 1.f;
-    if (a.apodizeoutput == 1) apofact = cosf((M_PI * 0.5f) * rho);
+    if (a.apodizeoutput == 1) apofact = cosf(1.57079632679f * rho);
     else if (a.apodizeoutput == 2) apofact = 1.0f - rho;
     scale.x *= apofact;
     scale.y *= apofact;
@@ -132,7 +174,8 @@ __device__ __forceinline__ void apply_side(float2& re, float2& im, float2 scale,
   }
 }
 
-__global__ void __launch_bounds__(kThreads) k_filter(FilterArgs a)
+template <int ND, int NO>
+__global__ void __launch_bounds__(kThreads) k_filter(const __grid_constant__ FilterArgs a, const __grid_constant__ FilterK k)
 {
   const int nx = a.nx, ny = a.ny, nz = a.nz, nxh = nx / 2 + 1;
   const int order = blockIdx.z, iz = blockIdx.y;
@@ -161,7 +204,7 @@ __global__ void __launch_bounds__(kThreads) k_filter(FilterArgs a)
     if (b2) b2[ind] = make_float2(0.f, 0.f);
     return;
   }
-  float2 s1 = filter_scale(a, order, x1, y1, z0, rdist1, x1f, y1f);
+  float2 s1 = filter_scale<ND, NO>(a, k, order, z0, rdist1, x1f, y1f);
   if (order == 0) {
     b1[ind] = cmul(b1[ind], s1);
     return;
@@ -174,7 +217,7 @@ __global__ void __launch_bounds__(kThreads) k_filter(FilterArgs a)
     const int x2 = -jin;
     float x2f = x2 * a.dkx, y2f = y2 * a.dky;
     float rdist2 = sqrtf(x2f * x2f + y2f * y2f);
-    float2 s2 = filter_scale(a, order, x2, y2, -z0, rdist2, x2f, y2f);
+    float2 s2 = filter_scale<ND, NO>(a, k, order, -z0, rdist2, x2f, y2f);
     apply_side(re, im, cmul(s2, a.conjamp[order]), true);
   }
   b1[ind] = re;
@@ -466,9 +509,26 @@ int launch_filter(const FilterArgs& a, cudaStream_t s, long long* launches)
 {
   const int nxh = a.nx / 2 + 1;
   dim3 g((a.ny * nxh + kThreads - 1) / kThreads, a.nz, a.norders);
+  FilterK k{};
+  const int no = a.norders;
+  for (int d = 0; d < a.ndirs; ++d)
+    for (int o = 0; o < no; ++o) {
+      const int i = d * no + o;
+      k.rnv[i] = 1.f / a.noisevar[i];
+      k.termw[i] = o == 0 ? k.rnv[i] : a.ampmag2[i] / a.noisevar[i];
+      k.kxo[i] = o * a.k0[d].x;
+      k.kyo[i] = o * a.k0[d].y;
+    }
+  k.rdkrotf = 1.f / a.otf.dkrotf;
+  k.min_dkr = a.dkx < a.dky ? a.dkx : a.dky;
+  k.rmin_dkr = 1.f / k.min_dkr;
+  k.supp_r = a.supp_radius * k.min_dkr;
+  k.rrcut = 1.f / a.rdistcutoff;
   KernelTimer* kt = kernel_timer();
   if (kt) kt->begin(s);
-  k_filter<<<g, kThreads, 0, s>>>(a);
+  if (a.ndirs == 3 && a.norders == 3) k_filter<3, 3><<<g, kThreads, 0, s>>>(a, k);
+  else if (a.ndirs == 3 && a.norders == 2) k_filter<3, 2><<<g, kThreads, 0, s>>>(a, k);
+  else k_filter<0, 0><<<g, kThreads, 0, s>>>(a, k);
   // every element of the 2*norders-1 bands of this direction is read (in
   // band) or only written (cleared)
   double planeb = (double)a.ny * nxh * sizeof(float2);

@@ -69,13 +69,15 @@ __global__ void __launch_bounds__(kThreads) k_ovl_build_x(OverlapArgs a, FFTPlan
       int zin = ((conj ? -z0 : z0) + nz) % nz;
       size_t indin = (size_t)zin * bplane + (size_t)iin * nxh + jin;
       bool skip = (z0 == 0 && a.nokz0);
+      const OtfKz kzi = otf_kz(a.otf, z0);
       if (!skip && ov == 0 && rdist1 <= cut) {
         // makeOverlaps0Kernel, gpuFunctionsImpl.cu:677-778
         float x12 = x1f - a.kx, y12 = y1f - a.ky;
-        if (sqrtf(x12 * x12 + y12 * y12) <= cut) {
-          float2 o1 = otf_lookup(otfA, a.otf, x1f, y1f, z0);
+        float r12 = sqrtf(x12 * x12 + y12 * y12);
+        if (r12 <= cut) {
+          float2 o1 = otf_lookup_rk(otfA, a.otf, rdist1, kzi);
           if (sqrtf(cmag2(o1)) > a.otfcutoff) {
-            float2 o12 = otf_lookup(otfB, a.otf, x12, y12, z0);
+            float2 o12 = otf_lookup_rk(otfB, a.otf, r12, kzi);
             if (sqrtf(cmag2(o12)) * a.order0_2_factor > a.otfcutoff) {
               float root = sqrtf(cmag2(o1) + cmag2(o12));
               float2 fact = make_float2(o12.x / root, o12.y / root);
@@ -94,10 +96,11 @@ __global__ void __launch_bounds__(kThreads) k_ovl_build_x(OverlapArgs a, FFTPlan
       } else if (!skip && ov == 1 && rdist1 < cut) {
         // makeOverlaps1Kernel, gpuFunctionsImpl.cu:780-872
         float x21 = x1f + a.kx, y21 = y1f + a.ky;
-        if (sqrtf(x21 * x21 + y21 * y21) <= cut) {
-          float2 o2 = otf_lookup(otfB, a.otf, x1f, y1f, z0);
+        float r21 = sqrtf(x21 * x21 + y21 * y21);
+        if (r21 <= cut) {
+          float2 o2 = otf_lookup_rk(otfB, a.otf, rdist1, kzi);
           if (sqrtf(cmag2(o2)) * a.order0_2_factor > a.otfcutoff) {
-            float2 o21 = otf_lookup(otfA, a.otf, x21, y21, z0);
+            float2 o21 = otf_lookup_rk(otfA, a.otf, r21, kzi);
             if (sqrtf(cmag2(o21)) > a.otfcutoff) {
               float root = sqrtf(cmag2(o2) + cmag2(o21));
               float2 fact = make_float2(o21.x / root, o21.y / root);
@@ -153,6 +156,9 @@ __global__ void __launch_bounds__(kThreads) k_ovl_y_accum(OverlapArgs a, FFTPlan
     }
     __syncthreads();
     const float2* res = fft_dispatch<NF, +1>(sm, sm + ny * ld, plan, 2 * W, 1, ld);
+    // this plane's |X|^2 and |Y|^2 in float (ny*W/blockDim terms per
+    // thread), added to the double totals once per plane
+    float px = 0.f, py = 0.f;
     for (int t = threadIdx.x; t < ny * W; t += blockDim.x) {
       int y = t / W, w = t - y * W;
       float2 X = res[y * ld + w], Y = res[y * ld + W + w];
@@ -161,9 +167,11 @@ __global__ void __launch_bounds__(kThreads) k_ovl_y_accum(OverlapArgs a, FFTPlan
       p.x += X.x * Y.x + X.y * Y.y;
       p.y += X.x * Y.y - X.y * Y.x;
       acc[t] = p;
-      sx += (double)cmag2(X);
-      sy += (double)cmag2(Y);
+      px += cmag2(X);
+      py += cmag2(Y);
     }
+    sx += (double)px;
+    sy += (double)py;
   }
   __syncthreads();
   float2* dst = a.ppart + (size_t)blockIdx.y * ny * nx;

@@ -50,6 +50,42 @@ __device__ __forceinline__ float2 otf_lookup(const float2* __restrict__ otf, con
   return r;
 }
 
+// kz part of otf_lookup, shared by every lookup at one kz
+struct OtfKz {
+  int iz, izp;
+  float az;
+};
+__device__ __forceinline__ OtfKz otf_kz(const OTFView& v, int kz)
+{
+  float kzindex = kz * v.kzscale;
+  if (kzindex < 0) kzindex += v.nzotf;
+  OtfKz r;
+  r.iz = (int)floorf(kzindex);
+  r.az = kzindex - r.iz;
+  r.izp = (r.iz == v.nzotf - 1) ? 0 : r.iz + 1;
+  return r;
+}
+// otf_lookup with the radius |k| already known and the kz part precomputed
+// (same arithmetic: krindex = |k| / dkrotf)
+__device__ __forceinline__ float2 otf_lookup_rk(const float2* __restrict__ otf, const OTFView& v, float kr,
+                                               const OtfKz& z)
+{
+  float krindex = kr / v.dkrotf;
+  int ir = (int)floorf(krindex);
+  float ar = krindex - ir;
+  int last = v.nxotf * v.nzotf - 1;
+  int i00 = min(max(ir * v.nzotf + z.iz, 0), last);
+  int i01 = min(max(ir * v.nzotf + z.izp, 0), last);
+  int i10 = min(max((ir + 1) * v.nzotf + z.iz, 0), last);
+  int i11 = min(max((ir + 1) * v.nzotf + z.izp, 0), last);
+  float2 a = __ldg(otf + i00), b = __ldg(otf + i01), c = __ldg(otf + i10), d = __ldg(otf + i11);
+  const float az = z.az;
+  float2 r;
+  r.x = (1 - ar) * (a.x * (1 - az) + b.x * az) + ar * (c.x * (1 - az) + d.x * az);
+  r.y = (1 - ar) * (a.y * (1 - az) + b.y * az) + ar * (c.y * (1 - az) + d.y * az);
+  return r;
+}
+
 __device__ __forceinline__ float cmag2(float2 a) { return a.x * a.x + a.y * a.y; }
 
 // Block-wide sum of a double (all threads must call).  Result valid in thread 0.
