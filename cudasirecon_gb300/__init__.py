@@ -80,6 +80,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.SRX_pinHost.argtypes = [vp, C.c_size_t]
     lib.SRX_unpinHost.restype = ip
     lib.SRX_unpinHost.argtypes = [vp]
+    lib.SRX_processSeries.restype = ip
+    lib.SRX_processSeries.argtypes = [vp, C.POINTER(vp), ip, C.POINTER(vp), ip, ip]
     lib.SRX_makeOTF.restype = ip
     lib.SRX_makeOTF.argtypes = [fp, ip, ip, ip, ip, C.POINTER(C.c_char_p), fp, C.c_size_t, C.POINTER(C.c_int)]
     lib.SRX_makeotfMain.restype = ip
@@ -298,6 +300,26 @@ class Reconstructor:
 
     def kernel_launches(self) -> int:
         return int(self.lib.SRX_kernelLaunches(self.h))
+
+    def process_series(self, raws, outs, t0: int = 0) -> None:
+        """SRX_processSeries: raws[i] (uint16 or float32 stacks of the setRaw
+        shape) -> outs[i] (float32 result arrays), volume i at time t0+i, with
+        uploads and downloads overlapped with the computation."""
+        n = len(raws)
+        if len(outs) != n:
+            raise ValueError("raws and outs differ in length")
+        u16 = raws[0].dtype == np.uint16
+        for r in raws:
+            if r.dtype != raws[0].dtype or not r.flags.c_contiguous or r.size != raws[0].size:
+                raise ValueError("raw stacks must share dtype and size and be C-contiguous")
+        for o in outs:
+            if o.dtype != np.float32 or not o.flags.c_contiguous or o.size != self.out_shape[0] * self.out_shape[1] * \
+                    self.out_shape[2]:
+                raise ValueError("outputs must be C-contiguous float32 arrays of the result shape")
+        rp = (C.c_void_p * n)(*[r.ctypes.data for r in raws])
+        op = (C.c_void_p * n)(*[o.ctypes.data for o in outs])
+        if self.lib.SRX_processSeries(self.h, rp, int(u16), op, n, t0) != 0:
+            raise SIReconError(_err(self.lib))
 
 
 def pin(array: np.ndarray) -> None:

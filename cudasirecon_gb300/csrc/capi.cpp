@@ -213,6 +213,18 @@ int SRX_fftSelfTest(float* data, int n, int nlines, int inverse, int columns)
   return rc;
 }
 
+int SRX_processSeries(SIM_Reconstructor* sr, const void* const* raws, int raw_is_u16, float* const* outs, int n,
+                      int t0)
+{
+  int rc = -1;
+  if (need(sr))
+    guarded([&] {
+      sr->process_series(raws, raw_is_u16 != 0, outs, n, t0);
+      rc = 0;
+    });
+  return rc;
+}
+
 int SRX_makeOTF(const float* psf, int nx, int ny, int nsections, int nargs, const char* const* args, float* out,
                 size_t out_floats, int* dims)
 {

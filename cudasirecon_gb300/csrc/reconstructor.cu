@@ -482,6 +482,15 @@ SIM_Reconstructor::~SIM_Reconstructor()
     cudaEventDestroy(pd.b);
   }
   if (stream_) cudaStreamSynchronize(stream_);
+  if (h2d_stream_) cudaStreamSynchronize(h2d_stream_);
+  if (d2h_stream_) cudaStreamSynchronize(d2h_stream_);
+  for (int b = 0; b < 2; ++b)
+    for (cudaEvent_t e : {ev_raw_ready_[b], ev_raw_free_[b], ev_out_ready_[b], ev_out_free_[b]})
+      if (e) cudaEventDestroy(e);
+  if (h2d_stream_) cudaStreamDestroy(h2d_stream_);
+  if (d2h_stream_) cudaStreamDestroy(d2h_stream_);
+  if (d_raw_alt_) cudaFree(d_raw_alt_);
+  if (d_out_extra_) cudaFree(d_out_extra_);
   if (arena_) cudaFree(arena_);
   if (d_flush_) cudaFree(d_flush_);
   if (h_pinned_) cudaFreeHost(h_pinned_);
@@ -1154,6 +1163,73 @@ void SIM_Reconstructor::get_fit(float* k0, float* amps) const
         amps[2 * (d * norders_ + o) + 1] = amp_[d][o].y;
       }
   }
+}
+
+void SIM_Reconstructor::process_series(const void* const* raws, bool u16, float* const* outs, int n, int t0)
+{
+  if (n <= 0) return;
+  if (!raws || !outs) throw std::runtime_error("processSeries: null buffer list");
+  const size_t raw_bytes = (size_t)nimg_ * nx_ * ny_ * (u16 ? 2 : 4);
+  const size_t out_bytes = out_elems() * sizeof(float);
+  if (!d_raw_alt_) {
+    check(cudaMalloc(&d_raw_alt_, (size_t)nimg_ * nx_ * ny_ * sizeof(float)), "series raw buffer");
+    check(cudaMalloc((void**)&d_out_extra_, out_bytes), "series output buffer");
+    d_out_alt_ = d_out_extra_;
+    check(cudaStreamCreateWithFlags(&h2d_stream_, cudaStreamNonBlocking), "series stream");
+    check(cudaStreamCreateWithFlags(&d2h_stream_, cudaStreamNonBlocking), "series stream");
+    for (int b = 0; b < 2; ++b)
+      for (cudaEvent_t* e : {&ev_raw_ready_[b], &ev_raw_free_[b], &ev_out_ready_[b], &ev_out_free_[b]})
+        check(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "series event");
+  }
+  void* raw_buf[2] = {d_raw_, d_raw_alt_};
+  float* out_buf[2] = {d_out_, d_out_alt_};
+  for (int b = 0; b < 2; ++b) {  // both buffers start free
+    check(cudaEventRecord(ev_raw_free_[b], stream_), "series event");
+    check(cudaEventRecord(ev_out_free_[b], stream_), "series event");
+  }
+  auto upload = [&](int i) {
+    const int b = i & 1;
+    check(cudaStreamWaitEvent(h2d_stream_, ev_raw_free_[b], 0), "series wait");
+    check(cudaMemcpyAsync(raw_buf[b], raws[i], raw_bytes, cudaMemcpyHostToDevice, h2d_stream_), "series upload");
+    check(cudaEventRecord(ev_raw_ready_[b], h2d_stream_), "series event");
+  };
+  upload(0);
+  if (n > 1) upload(1);
+  raw_u16_ = u16;
+  try {
+    for (int i = 0; i < n; ++i) {
+      const int b = i & 1;
+      check(cudaStreamWaitEvent(stream_, ev_raw_ready_[b], 0), "series wait");
+      d_raw_ = raw_buf[b];
+      have_raw_ = true;
+      ingest();  // returns after the ingest kernels finished: raw buffer b is free
+      check(cudaEventRecord(ev_raw_free_[b], stream_), "series event");
+      if (i + 2 < n) upload(i + 2);
+      load_and_rescale(t0 + i, 0);
+      set_cur_time(t0 + i);
+      check(cudaStreamWaitEvent(stream_, ev_out_free_[b], 0), "series wait");
+      d_out_ = out_buf[b];
+      process_one_volume();
+      check(cudaEventRecord(ev_out_ready_[b], stream_), "series event");
+      check(cudaStreamWaitEvent(d2h_stream_, ev_out_ready_[b], 0), "series wait");
+      check(cudaMemcpyAsync(outs[i], out_buf[b], out_bytes, cudaMemcpyDeviceToHost, d2h_stream_), "series download");
+      check(cudaEventRecord(ev_out_free_[b], d2h_stream_), "series event");
+    }
+  } catch (...) {
+    cudaStreamSynchronize(h2d_stream_);
+    cudaStreamSynchronize(d2h_stream_);
+    d_raw_ = raw_buf[0];
+    d_out_ = out_buf[0];
+    d_out_alt_ = out_buf[1];
+    throw;
+  }
+  check(cudaStreamSynchronize(h2d_stream_), "series upload");
+  check(cudaStreamSynchronize(d2h_stream_), "series download");
+  // getResult after the series returns the last volume; keep the arena's raw
+  // buffer as the one setRaw uses
+  d_raw_ = raw_buf[0];
+  d_out_ = out_buf[(n - 1) & 1];
+  d_out_alt_ = out_buf[((n - 1) & 1) ^ 1];
 }
 
 // getResult (cudaSirecon.cpp:1620-1634)

@@ -32,6 +32,13 @@ class SIM_Reconstructor {
   void set_cur_time(int it) { opt.ip.curTimeIdx = (unsigned short)it; }
   int process_one_volume();
   void get_result(float* out);
+  // n volumes: per volume i the same as setRaw(raws[i]) ->
+  // loadAndRescaleImage(t0+i) -> setCurTimeIdx(t0+i) -> processOneVolume ->
+  // getResult(outs[i]), with the upload of volume i+1 and the download of
+  // volume i-1 overlapped with the computation of volume i (double-buffered
+  // device raw/output buffers, separate copy streams; page-locked host
+  // buffers make the copies asynchronous)
+  void process_series(const void* const* raws, bool u16, float* const* outs, int n, int t0);
   void set_file(int it, int iw);
   void write_result(int it, int iw);
   void close_files();
@@ -114,6 +121,14 @@ class SIM_Reconstructor {
   float* d_out_ = nullptr;
   float* d_flush_ = nullptr;
   size_t flush_n_ = 0;
+  // second raw and output buffers, copy streams and events of process_series
+  // (allocated on first use)
+  void* d_raw_alt_ = nullptr;
+  float* d_out_alt_ = nullptr;   // the output buffer not holding the last result
+  float* d_out_extra_ = nullptr;  // the allocation behind the second output buffer
+  cudaStream_t h2d_stream_ = nullptr, d2h_stream_ = nullptr;
+  cudaEvent_t ev_raw_ready_[2] = {nullptr, nullptr}, ev_raw_free_[2] = {nullptr, nullptr};
+  cudaEvent_t ev_out_ready_[2] = {nullptr, nullptr}, ev_out_free_[2] = {nullptr, nullptr};
   double* h_pinned_ = nullptr;  // small pinned host buffer for results of the fit
 
   // host-side state (ReconData equivalents)

@@ -230,6 +230,19 @@ int SRX_fftLinesNoAlloc(const float* in, float* out, int n, int nlines, int inve
 const char* SRX_fftLinesNoAllocError(void);
 int SRX_unpinHost(void* ptr);
 
+/* No counterpart in the reference.  Reconstruct n volumes of a time series:
+ * for volume i the same as SR_setRaw(raws[i]) (SR_setRawU16 when
+ * raw_is_u16), SR_loadAndRescaleImage(t0+i, 0), SR_setCurTimeIdx(t0+i),
+ * SR_processOneVolume, SR_getResult(outs[i]) -- the results are identical --
+ * but the upload of volume i+1 and the download of volume i-1 run on their
+ * own streams while volume i is computed.  raws[i] and outs[i] are host
+ * buffers of the SR_setRaw / SR_getResult sizes; page-lock them
+ * (SRX_pinHost) for the copies to overlap.  Entries may repeat, except that
+ * an output buffer must not be reused within two consecutive volumes.
+ * Returns 0 on success, -1 on error (SR_getLastError). */
+int SRX_processSeries(SIM_Reconstructor* sr, const void* const* raws, int raw_is_u16, float* const* outs, int n,
+                      int t0);
+
 /* makeotf.  The reference's makeotf is a program, not a library call
  * (src/otf/radialft.cpp:82-434); these replace it:
  *
