@@ -251,14 +251,22 @@ def run_gb300(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
         r.result(out)
     barrier(dist)
     t0 = time.perf_counter()
+    lat = []
     for i in range(args.steps):
+        ts = time.perf_counter()
         r.set_raw(host[i % len(host)])
         r.load_and_rescale(t_idx, 0)
         r.set_cur_time(t_idx)
         r.process()
         r.result(out)
+        lat.append(time.perf_counter() - ts)
     barrier(dist)
     e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    # per-volume latency of the plain calls: stack submitted -> result in host memory
+    lat_ms = np.sort(np.array(lat)) * 1e3
+    latency = {"p50_ms": round(float(np.percentile(lat_ms, 50)), 3), "p99_ms": round(float(np.percentile(lat_ms, 99)), 3),
+               "max_ms": round(float(lat_ms[-1]), 3), "n": len(lat),
+               "what": "plain SR_* sequence per volume, stack in pinned host memory -> result in host memory"}
     for h in host + outs2:
         sr.unpin(h)
     sr.unpin(out)
@@ -291,7 +299,7 @@ def run_gb300(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
         "e2e": {"value": round(e2e, 1), "unit": "Mvoxels/s",
                 "h2d_bytes_per_step": int(host[0].nbytes), "d2h_bytes_per_step": int(out.nbytes),
                 "api": "SRX_processSeries (uploads/downloads overlapped with computation), pinned host buffers",
-                "plain_value": round(e2e_plain, 1),
+                "plain_value": round(e2e_plain, 1), "plain_latency": latency,
                 "plain_api": "SR_setRawU16 -> SR_loadAndRescaleImage -> SR_processOneVolume -> SR_getResult"},
         "gpu_launches": int(launches),
         "clocks": clk,

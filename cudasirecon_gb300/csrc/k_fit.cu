@@ -33,22 +33,86 @@ constexpr int kThreads = 256;
 constexpr int kMaxElems = kFftElems;
 
 // ---------------------------------------------------------------- overlaps
+// Element (j) of overlap `ov` on row (zb, i) before the x transform:
+// makeOverlaps0Kernel (ov 0, gpuFunctionsImpl.cu:677-778) / makeOverlaps1Kernel
+// (ov 1, 780-872): the order-1/order-2 band value times the partner OTF over
+// sqrt(|OTF1|^2 + |OTF2|^2) inside both supports, merged re + i im.
+__device__ __forceinline__ float2 ovl_value(const OverlapArgs& a, int ov, int zb, int i, int j)
+{
+  const int nx = a.nx, ny = a.ny, nz = a.nz, nxh = nx / 2 + 1;
+  const size_t bplane = (size_t)ny * nxh;
+  const float cut = a.rdistcutoff;
+  int z0 = zb - a.zdc;
+  float x1f = (float)j, y1f = (float)i;
+  if (x1f > nx / 2) x1f -= nx;
+  if (y1f > ny / 2) y1f -= ny;
+  x1f *= a.dkx;
+  y1f *= a.dky;
+  float rdist1 = sqrtf(x1f * x1f + y1f * y1f);
+  bool conj = j > nx / 2;
+  int jin = conj ? nx - j : j;
+  int iin = conj ? (ny - i) % ny : i;
+  int zin = ((conj ? -z0 : z0) + nz) % nz;
+  size_t indin = (size_t)zin * bplane + (size_t)iin * nxh + jin;
+  if (z0 == 0 && a.nokz0) return make_float2(0.f, 0.f);
+  const OtfKz kzi = otf_kz(a.otf, z0);
+  if (ov == 0 && rdist1 <= cut) {
+    float x12 = x1f - a.kx, y12 = y1f - a.ky;
+    float r12 = sqrtf(x12 * x12 + y12 * y12);
+    if (r12 <= cut) {
+      float2 o1 = otf_lookup_rk(a.otf.otf[a.order1], a.otf, rdist1, kzi);
+      if (sqrtf(cmag2(o1)) > a.otfcutoff) {
+        float2 o12 = otf_lookup_rk(a.otf.otf[a.order2], a.otf, r12, kzi);
+        if (sqrtf(cmag2(o12)) * a.order0_2_factor > a.otfcutoff) {
+          float root = sqrtf(cmag2(o1) + cmag2(o12));
+          float2 fact = make_float2(o12.x / root, o12.y / root);
+          const float2* b1re = a.order1 == 0 ? a.bands : a.bands + (size_t)(2 * a.order1 - 1) * nz * bplane;
+          float2 vre = b1re[indin];
+          float2 vim = a.order1 == 0 ? make_float2(0.f, 0.f) : a.bands[(size_t)(2 * a.order1) * nz * bplane + indin];
+          if (conj) {
+            vre.y = -vre.y;
+            vim.y = -vim.y;
+          }
+          vre = cmul(vre, fact);
+          vim = cmul(vim, fact);
+          return make_float2(vre.x - vim.y, vre.y + vim.x);
+        }
+      }
+    }
+  } else if (ov == 1 && rdist1 < cut) {
+    float x21 = x1f + a.kx, y21 = y1f + a.ky;
+    float r21 = sqrtf(x21 * x21 + y21 * y21);
+    if (r21 <= cut) {
+      float2 o2 = otf_lookup_rk(a.otf.otf[a.order2], a.otf, rdist1, kzi);
+      if (sqrtf(cmag2(o2)) * a.order0_2_factor > a.otfcutoff) {
+        float2 o21 = otf_lookup_rk(a.otf.otf[a.order1], a.otf, r21, kzi);
+        if (sqrtf(cmag2(o21)) > a.otfcutoff) {
+          float root = sqrtf(cmag2(o2) + cmag2(o21));
+          float2 fact = make_float2(o21.x / root, o21.y / root);
+          float2 vre = a.bands[(size_t)(2 * a.order2 - 1) * nz * bplane + indin];
+          float2 vim = a.bands[(size_t)(2 * a.order2) * nz * bplane + indin];
+          if (conj) {
+            vre.y = -vre.y;
+            vim.y = -vim.y;
+          }
+          vre = cmul(vre, fact);
+          vim = cmul(vim, fact);
+          return make_float2(vre.x - vim.y, vre.y + vim.x);
+        }
+      }
+    }
+  }
+  return make_float2(0.f, 0.f);
+}
+
 template <int NF>
 __global__ void __launch_bounds__(kThreads) k_ovl_build_x(OverlapArgs a, FFTPlan plan, int rows_per_cta, int ldl)
 {
   extern __shared__ float2 sm[];
-  const int nx = a.nx, ny = a.ny, nz = a.nz, nxh = nx / 2 + 1;
+  const int nx = a.nx, ny = a.ny;
   const int nzb = 2 * a.zdc + 1;
   const int row0 = blockIdx.x * rows_per_cta;
   const int nrows = min(rows_per_cta, nzb * ny - row0);
-  const size_t bplane = (size_t)ny * nxh;
-  const float2* b1re = a.order1 == 0 ? a.bands : a.bands + (size_t)(2 * a.order1 - 1) * nz * bplane;
-  const float2* b1im = a.order1 == 0 ? nullptr : a.bands + (size_t)(2 * a.order1) * nz * bplane;
-  const float2* b2re = a.bands + (size_t)(2 * a.order2 - 1) * nz * bplane;
-  const float2* b2im = a.bands + (size_t)(2 * a.order2) * nz * bplane;
-  const float2* otfA = a.otf.otf[a.order1];
-  const float2* otfB = a.otf.otf[a.order2];
-  const float cut = a.rdistcutoff;
   for (int t = threadIdx.x; t < 2 * rows_per_cta * nx; t += blockDim.x) {
     int l = t / nx, j = t - l * nx;
     int r = l >> 1, ov = l & 1;
@@ -56,67 +120,7 @@ __global__ void __launch_bounds__(kThreads) k_ovl_build_x(OverlapArgs a, FFTPlan
     if (r < nrows) {
       int row = row0 + r;
       int zb = row / ny, i = row - zb * ny;
-      int z0 = zb - a.zdc;
-      float x1f = (float)j, y1f = (float)i;
-      if (x1f > nx / 2) x1f -= nx;
-      if (y1f > ny / 2) y1f -= ny;
-      x1f *= a.dkx;
-      y1f *= a.dky;
-      float rdist1 = sqrtf(x1f * x1f + y1f * y1f);
-      bool conj = j > nx / 2;
-      int jin = conj ? nx - j : j;
-      int iin = conj ? (ny - i) % ny : i;
-      int zin = ((conj ? -z0 : z0) + nz) % nz;
-      size_t indin = (size_t)zin * bplane + (size_t)iin * nxh + jin;
-      bool skip = (z0 == 0 && a.nokz0);
-      const OtfKz kzi = otf_kz(a.otf, z0);
-      if (!skip && ov == 0 && rdist1 <= cut) {
-        // makeOverlaps0Kernel, gpuFunctionsImpl.cu:677-778
-        float x12 = x1f - a.kx, y12 = y1f - a.ky;
-        float r12 = sqrtf(x12 * x12 + y12 * y12);
-        if (r12 <= cut) {
-          float2 o1 = otf_lookup_rk(otfA, a.otf, rdist1, kzi);
-          if (sqrtf(cmag2(o1)) > a.otfcutoff) {
-            float2 o12 = otf_lookup_rk(otfB, a.otf, r12, kzi);
-            if (sqrtf(cmag2(o12)) * a.order0_2_factor > a.otfcutoff) {
-              float root = sqrtf(cmag2(o1) + cmag2(o12));
-              float2 fact = make_float2(o12.x / root, o12.y / root);
-              float2 vre = b1re[indin];
-              float2 vim = b1im ? b1im[indin] : make_float2(0.f, 0.f);
-              if (conj) {
-                vre.y = -vre.y;
-                vim.y = -vim.y;
-              }
-              vre = cmul(vre, fact);
-              vim = cmul(vim, fact);
-              val = make_float2(vre.x - vim.y, vre.y + vim.x);
-            }
-          }
-        }
-      } else if (!skip && ov == 1 && rdist1 < cut) {
-        // makeOverlaps1Kernel, gpuFunctionsImpl.cu:780-872
-        float x21 = x1f + a.kx, y21 = y1f + a.ky;
-        float r21 = sqrtf(x21 * x21 + y21 * y21);
-        if (r21 <= cut) {
-          float2 o2 = otf_lookup_rk(otfB, a.otf, rdist1, kzi);
-          if (sqrtf(cmag2(o2)) * a.order0_2_factor > a.otfcutoff) {
-            float2 o21 = otf_lookup_rk(otfA, a.otf, r21, kzi);
-            if (sqrtf(cmag2(o21)) > a.otfcutoff) {
-              float root = sqrtf(cmag2(o2) + cmag2(o21));
-              float2 fact = make_float2(o21.x / root, o21.y / root);
-              float2 vre = b2re[indin];
-              float2 vim = b2im[indin];
-              if (conj) {
-                vre.y = -vre.y;
-                vim.y = -vim.y;
-              }
-              vre = cmul(vre, fact);
-              vim = cmul(vim, fact);
-              val = make_float2(vre.x - vim.y, vre.y + vim.x);
-            }
-          }
-        }
-      }
+      val = ovl_value(a, ov, zb, i, j);
     }
     sm[l * ldl + j] = val;
   }
@@ -127,6 +131,57 @@ __global__ void __launch_bounds__(kThreads) k_ovl_build_x(OverlapArgs a, FFTPlan
     int l = t / nx, j = t - l * nx;
     int r = l >> 1, ov = l & 1;
     a.ovl[(size_t)ov * vol + (size_t)(row0 + r) * nx + j] = res[l * ldl + j];
+  }
+}
+
+// Warp-level variant for the row lengths with a register configuration:
+// each warp owns 32/P consecutive overlap lines (line = 2 * row + ov), builds
+// their elements into a warp-private buffer, and each group of P lanes runs
+// its line's inverse x FFT in registers and stores it (no CTA barrier).
+template <int N>
+struct OvlLanes {
+  static constexpr int P = N == 1024 ? 32 : (N == 512 || N == 256 ? 16 : 0);
+};
+constexpr int kOvlWarps = 4;
+
+template <int N>
+__global__ void __launch_bounds__(kOvlWarps * 32, 3) k_ovl_build_xw(OverlapArgs a, const float2* __restrict__ tw)
+{
+  constexpr int P = OvlLanes<N>::P, E = N / P, G = 32 / P;
+  constexpr int XB = (P + 1) * E + 1;
+  constexpr int LB = N > XB ? N : XB;  // line buffer, reused as the exchange buffer
+  __shared__ float2 lines[kOvlWarps][G][LB];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane / P, p = lane - g * P;
+  const int ny = a.ny, nzb = 2 * a.zdc + 1;
+  const int nlines = 2 * nzb * ny;
+  const int l0 = (blockIdx.x * kOvlWarps + warp) * G;
+  // build the warp's G lines (all 32 lanes, consecutive j)
+  for (int t = lane; t < G * N; t += 32) {
+    const int gl = t / N, j = t - gl * N;
+    const int L = l0 + gl;
+    float2 v = make_float2(0.f, 0.f);
+    if (L < nlines) {
+      const int row = L >> 1, ov = L & 1;
+      const int zb = row / ny, i = row - zb * ny;
+      v = ovl_value(a, ov, zb, i, j);
+    }
+    lines[warp][gl][j] = v;
+  }
+  __syncwarp();
+  float2 v[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) v[e] = lines[warp][g][p + P * e];
+  __syncwarp();  // every lane has its values before the buffer becomes the exchange
+  reg_line<N, P, +1>(v, p, lines[warp][g], tw, true);
+  const int L = l0 + g;
+  if (L < nlines) {
+    const int row = L >> 1, ov = L & 1;
+    float2* dst = a.ovl + (size_t)ov * nzb * ny * N + (size_t)row * N;
+#pragma unroll
+    for (int m = 0; m < E / P; ++m)
+#pragma unroll
+      for (int k2 = 0; k2 < P; ++k2) dst[p + P * m + E * k2] = v[m * P + k2];
   }
 }
 
@@ -434,10 +489,20 @@ int launch_overlaps(OverlapArgs& a, cudaStream_t s, long long* launches)
   const double ovlb = 2.0 * nzb * a.ny * a.nx * sizeof(float2);
   const double bandplanes = (double)nzb * a.ny * (a.nx / 2 + 1) * sizeof(float2);
   if (kt) kt->begin(s);
-  dispatch_fft_len(kSiteOvlX, a.nx, [&]<int NF>() {
-    cudaFuncSetAttribute(k_ovl_build_x<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
-    k_ovl_build_x<NF><<<nb1, kThreads, sm1, s>>>(a, px, rows, ldl);
-  });
+  auto launch_w = [&]<int N>() {
+    constexpr int G = 32 / OvlLanes<N>::P;
+    const int nlines = 2 * nzb * a.ny;
+    const int per_cta = kOvlWarps * G;
+    k_ovl_build_xw<N><<<(nlines + per_cta - 1) / per_cta, kOvlWarps * 32, 0, s>>>(a, px.tw);
+  };
+  if (a.nx == 512) launch_w.template operator()<512>();
+  else if (a.nx == 1024) launch_w.template operator()<1024>();
+  else if (a.nx == 256) launch_w.template operator()<256>();
+  else
+    dispatch_fft_len(kSiteOvlX, a.nx, [&]<int NF>() {
+      cudaFuncSetAttribute(k_ovl_build_x<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
+      k_ovl_build_x<NF><<<nb1, kThreads, sm1, s>>>(a, px, rows, ldl);
+    });
   if (kt) kt->end("k_ovl_build_x", s, ovlb + (a.order1 == 0 ? 3 : 4) * bandplanes);
   // 2) y inverse FFT + accumulation over kz planes
   const int threads = kThreads;
