@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "col_fft.cuh"
 #include "kernels.h"
 #include "reg_fft.cuh"
 
@@ -370,6 +371,69 @@ __global__ void __launch_bounds__(kThreads) k_asm_x(AssembleArgs a, const int* _
   }
 }
 
+// Four-step variant of k_asm_y (col_fft.cuh) for zoomed column lengths with
+// a column configuration: 8 output columns of one slot per CTA, band values
+// loaded straight from HBM during the first stage.
+template <int Y>
+__global__ void __launch_bounds__(kThreads) k_asm_y4(AssembleArgs a, const Slot* __restrict__ slots,
+                                                    const float2* __restrict__ tw)
+{
+  constexpr int R1 = colfft_r1(Y), W = 8;
+  extern __shared__ float2 sm[];  // ColFft<Y, R1, W>::kSmemElems
+  const Slot sl = slots[blockIdx.y];
+  const int nx = a.nx, ny = a.ny, nz = a.nz, nxh = nx / 2 + 1;
+  const int c0 = blockIdx.x * W;
+  const size_t plane = (size_t)ny * nxh;
+  const int d0 = sl.dir < 0 ? 0 : sl.dir;
+  const float2* br = a.bands + ((size_t)d0 * a.nphases + (sl.order == 0 ? 0 : 2 * sl.order - 1)) * nz * plane;
+  const float2* bi = sl.order == 0 ? nullptr : a.bands + ((size_t)d0 * a.nphases + 2 * sl.order) * nz * plane;
+  const size_t dstride = (size_t)a.nphases * nz * plane;
+  const int ylo = ny / 2 - 1;  // ky in [-ylo, ny/2]
+  colfft_stage1<Y, R1, W, +1>(sm, tw, [&](int yr, int w) {
+    const int c = c0 + w;
+    float2 v = make_float2(0.f, 0.f);
+    int ky;
+    bool valid = c < nx;
+    if (yr <= ny / 2) ky = yr;
+    else if (yr >= Y - ylo) ky = yr - Y;
+    else valid = false;
+    if (valid) {
+      int x = c - (nx / 2 - 1), y = ky, z = sl.kz;
+      const bool conj = x < 0;
+      if (conj) {
+        x = -x;
+        y = -y;
+        z = -z;
+      }
+      if (y < 0) y += ny;
+      if (z < 0) z += nz;
+      const size_t indin = (size_t)z * plane + (size_t)y * nxh + x;
+      if (sl.order == 0) {
+        v = br[indin];
+        if (sl.dir < 0)
+          for (int d = 1; d < a.ndirs; ++d) {
+            float2 u = br[d * dstride + indin];
+            v.x += u.x;
+            v.y += u.y;
+          }
+        if (conj) v.y = -v.y;
+      } else {
+        float2 re = br[indin], im = bi[indin];
+        if (conj) {
+          re.y = -re.y;
+          im.y = -im.y;
+        }
+        v = make_float2(re.x - im.y, re.y + im.x);
+      }
+    }
+    return v;
+  });
+  float2* dst = a.T + (size_t)blockIdx.y * Y * nx + c0;
+  colfft_stage2<Y, R1, W, +1>(sm, [&](int yr, int w, float2 v) {
+    if (c0 + w < nx) dst[(size_t)yr * nx + w] = v;
+  });
+}
+
 // Warp-level variant of k_asm_x for the zoomed row lengths with a register
 // path: each group of P lanes owns one output row yr of plane pidx and runs,
 // for every slot of the plane, the zero-padded inverse FFT of the slot's T row
@@ -637,10 +701,21 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
     AssembleArgs ay = a;
     KernelTimer* kt = kernel_timer();
     if (kt) kt->begin(s);
-    dispatch_fft_len(kSiteAsmY, a.Y, [&]<int NF>() {
-      cudaFuncSetAttribute(k_asm_y<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
-      k_asm_y<NF><<<dim3((nx + Wy - 1) / Wy, nsl), kThreads, smy, s>>>(ay, d_slots + first, py, Wy);
-    });
+    if (colfft_r1(a.Y)) {
+      auto go = [&]<int YN>() {
+        const size_t bytes = ColFft<YN, colfft_r1(YN), 8>::kSmemElems * sizeof(float2);
+        cudaFuncSetAttribute(k_asm_y4<YN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        k_asm_y4<YN><<<dim3((nx + 7) / 8, nsl), kThreads, bytes, s>>>(ay, d_slots + first, py.tw);
+      };
+      if (a.Y == 1024) go.template operator()<1024>();
+      else if (a.Y == 512) go.template operator()<512>();
+      else go.template operator()<256>();
+    } else {
+      dispatch_fft_len(kSiteAsmY, a.Y, [&]<int NF>() {
+        cudaFuncSetAttribute(k_asm_y<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
+        k_asm_y<NF><<<dim3((nx + Wy - 1) / Wy, nsl), kThreads, smy, s>>>(ay, d_slots + first, py, Wy);
+      });
+    }
     if (kt) {
       double rd = 0;
       for (int q = first; q < first + nsl; ++q)

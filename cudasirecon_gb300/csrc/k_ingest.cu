@@ -13,6 +13,7 @@
 // (gpuFunctionsImpl.cu:214-291) and the z FFT (cudaSirecon.cpp:238-257).
 #include <algorithm>
 
+#include "col_fft.cuh"
 #include "kernels.h"
 #include "reg_fft.cuh"
 
@@ -168,6 +169,24 @@ __global__ void __launch_bounds__(kThreads) k_fft_cols(float2* data, int n, int 
   }
 }
 
+// Four-step variant (col_fft.cuh) for the lengths with a column
+// configuration: 8 columns of one plane per CTA, loaded straight from HBM.
+template <int N>
+__global__ void __launch_bounds__(kThreads) k_fft_cols_4s(float2* data, int ncol, const float2* __restrict__ tw)
+{
+  constexpr int R1 = colfft_r1(N), W = 8;
+  extern __shared__ float2 sm[];  // ColFft<N, R1, W>::kSmemElems
+  const int c0 = blockIdx.x * W;
+  float2* base = data + (size_t)blockIdx.y * N * ncol + c0;
+  const int nc = min(W, ncol - c0);
+  colfft_stage1<N, R1, W, -1>(sm, tw, [&](int row, int c) {
+    return c < nc ? base[(size_t)row * ncol + c] : make_float2(0.f, 0.f);
+  });
+  colfft_stage2<N, R1, W, -1>(sm, [&](int row, int c, float2 v) {
+    if (c < nc) base[(size_t)row * ncol + c] = v;
+  });
+}
+
 // Bleach correction (rescale, gpuFunctionsImpl.cu:110-157): per (d, z) the
 // nphases plane sums, ref = dir-0 phase-0 sum at z (or at z = 0 with
 // equalizez; from time 0 with equalizet), ratio = ref / sum.
@@ -274,10 +293,22 @@ int launch_ingest(const IngestArgs& a, cudaStream_t s, long long* launches)
   size_t smy = fft_smem(a.ny, W, a.ny * (W + 1));
   dim3 gy((nxh + W - 1) / W, nplanes);
   if (kt) kt->begin(s);
-  dispatch_fft_len(kSiteIngestY, a.ny, [&]<int NF>() {
-    cudaFuncSetAttribute(k_fft_cols<-1, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
-    k_fft_cols<-1, NF><<<gy, kThreads, smy, s>>>(a.spec, a.ny, nxh, py, W);
-  });
+  if (colfft_r1(a.ny)) {
+    dim3 g4((nxh + 7) / 8, nplanes);
+    auto go = [&]<int N>() {
+      const size_t bytes = ColFft<N, colfft_r1(N), 8>::kSmemElems * sizeof(float2);
+      cudaFuncSetAttribute(k_fft_cols_4s<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+      k_fft_cols_4s<N><<<g4, kThreads, bytes, s>>>(a.spec, nxh, py.tw);
+    };
+    if (a.ny == 512) go.template operator()<512>();
+    else if (a.ny == 1024) go.template operator()<1024>();
+    else go.template operator()<256>();
+  } else {
+    dispatch_fft_len(kSiteIngestY, a.ny, [&]<int NF>() {
+      cudaFuncSetAttribute(k_fft_cols<-1, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
+      k_fft_cols<-1, NF><<<gy, kThreads, smy, s>>>(a.spec, a.ny, nxh, py, W);
+    });
+  }
   if (kt) kt->end("k_fft_y", s, 2 * specb);
   if (launches) *launches += 2;
   return (int)cudaGetLastError();
