@@ -22,6 +22,7 @@
 //   k_modamp_*      sum_xy P e^{i phi_c} for a batch of candidates
 #include <algorithm>
 
+#include "col_fft.cuh"
 #include "kernels.h"
 #include "reg_fft.cuh"
 
@@ -233,6 +234,95 @@ __global__ void __launch_bounds__(kThreads) k_ovl_y_accum(OverlapArgs a, FFTPlan
   for (int t = threadIdx.x; t < ny * W; t += blockDim.x) {
     int y = t / W, w = t - y * W;
     if (c0 + w < nx) dst[(size_t)y * nx + c0 + w] = acc[t];
+  }
+  double tx = block_sum_d(sx, red);
+  double ty = block_sum_d(sy, red);
+  if (threadIdx.x == 0) {
+    int cta = blockIdx.y * gridDim.x + blockIdx.x;
+    a.sums[2 * cta] = tx;
+    a.sums[2 * cta + 1] = ty;
+  }
+}
+
+// Four-step variant (col_fft.cuh layout) of k_ovl_y_accum for ny in
+// {256, 512}: per kz plane of the group, stage 1 transforms the 8 columns of
+// both overlaps (half of the threads each, rows loaded straight from HBM),
+// stage 2 gives each thread one (column, k1) of both, and conj(X)Y, |X|^2,
+// |Y|^2 accumulate in registers over the planes.
+template <int N, int R1>
+__global__ void __launch_bounds__(kThreads) k_ovl_y4(OverlapArgs a, const float2* __restrict__ tw,
+                                                    int planes_per_group)
+{
+  using CF = ColFft<N, R1, 8>;
+  constexpr int W = 8, R2 = CF::R2, LD1 = CF::LD1;
+  static_assert(R2 * W * 2 == kThreads, "stage 1 gives half of the CTA to each overlap");
+  static_assert(R1 * W <= kThreads, "one stage-2 item per thread");
+  extern __shared__ float2 sm[];  // 2 * CF::kSmemElems
+  __shared__ double red[32];
+  const int nx = a.nx, ny = N;
+  const int nzb = 2 * a.zdc + 1;
+  const int c0 = blockIdx.x * W;
+  const int nc = min(W, nx - c0);
+  const int zb0 = blockIdx.y * planes_per_group;
+  const int zb1 = min(nzb, zb0 + planes_per_group);
+  const size_t vol = (size_t)nzb * ny * nx;
+  // stage-1 item of this thread
+  const int ov1 = threadIdx.x / (R2 * W), it1 = threadIdx.x - ov1 * (R2 * W);
+  const int c1 = it1 % W, j1 = it1 / W;
+  float2* buf1 = sm + ov1 * CF::kSmemElems;
+  // stage-2 item
+  const bool has2 = threadIdx.x < R1 * W;
+  const int c2 = threadIdx.x % W, k1 = threadIdx.x / W;
+  float2 acc[R2];
+#pragma unroll
+  for (int k2 = 0; k2 < R2; ++k2) acc[k2] = make_float2(0.f, 0.f);
+  double sx = 0.0, sy = 0.0;
+  for (int zb = zb0; zb < zb1; ++zb) {
+    {
+      const float2* src = a.ovl + (size_t)ov1 * vol + (size_t)zb * ny * nx + c0 + c1;
+      float2 v[R1];
+#pragma unroll
+      for (int e = 0; e < R1; ++e) v[e] = c1 < nc ? src[(size_t)(j1 + R2 * e) * nx] : make_float2(0.f, 0.f);
+      reg_dft<R1, +1>(v);
+#pragma unroll
+      for (int kk = 1; kk < R1; ++kk) {
+        float2 w = __ldg(tw + j1 * kk);
+        w.y = -w.y;
+        v[kk] = cmul(v[kk], w);
+      }
+#pragma unroll
+      for (int kk = 0; kk < R1; ++kk) buf1[kk * LD1 + j1 * W + c1] = v[kk];
+    }
+    __syncthreads();
+    if (has2) {
+      float2 X[R2], Y[R2];
+#pragma unroll
+      for (int j = 0; j < R2; ++j) {
+        X[j] = sm[k1 * LD1 + j * W + c2];
+        Y[j] = sm[CF::kSmemElems + k1 * LD1 + j * W + c2];
+      }
+      reg_dft<R2, +1>(X);
+      reg_dft<R2, +1>(Y);
+      float px = 0.f, py = 0.f;
+#pragma unroll
+      for (int k2 = 0; k2 < R2; ++k2) {
+        // conj(X) * Y, as reductionKernel's xsy (gpuFunctionsImpl.cu:1177-1178)
+        acc[k2].x += X[k2].x * Y[k2].x + X[k2].y * Y[k2].y;
+        acc[k2].y += X[k2].x * Y[k2].y - X[k2].y * Y[k2].x;
+        px += cmag2(X[k2]);
+        py += cmag2(Y[k2]);
+      }
+      if (c2 < nc) {  // columns past nx are zero padding, not data
+        sx += (double)px;
+        sy += (double)py;
+      }
+    }
+    __syncthreads();
+  }
+  if (has2 && c2 < nc) {
+    float2* dst = a.ppart + (size_t)blockIdx.y * ny * nx + c0 + c2;
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2) dst[(size_t)(k1 + R1 * k2) * nx] = acc[k2];
   }
   double tx = block_sum_d(sx, red);
   double ty = block_sum_d(sy, red);
@@ -515,11 +605,26 @@ int launch_overlaps(OverlapArgs& a, cudaStream_t s, long long* launches)
   const size_t fsm = fft_stage_smem(a.ny, 2 * W, tile, threads);
   const int xoff = (int)(fsm / sizeof(float2));
   size_t sm2 = fsm + (size_t)a.ny * W * sizeof(float2);
+  if (a.ny == 512 || a.ny == 256) {
+    // 8 columns per CTA; plane groups so that the grid covers the GPU
+    tiles = (a.nx + 7) / 8;
+    groups = std::max(1, std::min(nzb, (4 * 152 + tiles - 1) / tiles));
+    ppg = (nzb + groups - 1) / groups;
+    groups = (nzb + ppg - 1) / ppg;
+  }
   if (kt) kt->begin(s);
-  dispatch_fft_len(kSiteOvlY, a.ny, [&]<int NF>() {
-    cudaFuncSetAttribute(k_ovl_y_accum<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
-    k_ovl_y_accum<NF><<<dim3(tiles, groups), threads, sm2, s>>>(a, py, W, ppg, xoff);
-  });
+  auto go4 = [&]<int N, int R1>() {
+    const size_t bytes = 2 * ColFft<N, R1, 8>::kSmemElems * sizeof(float2);
+    cudaFuncSetAttribute(k_ovl_y4<N, R1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    k_ovl_y4<N, R1><<<dim3(tiles, groups), kThreads, bytes, s>>>(a, py.tw, ppg);
+  };
+  if (a.ny == 512) go4.template operator()<512, 32>();
+  else if (a.ny == 256) go4.template operator()<256, 16>();
+  else
+    dispatch_fft_len(kSiteOvlY, a.ny, [&]<int NF>() {
+      cudaFuncSetAttribute(k_ovl_y_accum<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+      k_ovl_y_accum<NF><<<dim3(tiles, groups), threads, sm2, s>>>(a, py, W, ppg, xoff);
+    });
   if (kt) kt->end("k_ovl_y_accum", s, ovlb + (double)groups * a.ny * a.nx * sizeof(float2));
   // 3) reduce plane groups
   k_p_reduce<<<std::min(1024, (a.nx * a.ny + 255) / 256), 256, 0, s>>>(a, groups, tiles * groups);
