@@ -532,6 +532,56 @@ __global__ void __launch_bounds__(kThreads) k_asm_z(AssembleArgs a, const unsign
   }
 }
 
+// Four-step variant of k_asm_z for Z = 16 * R1: 64 columns of one output row
+// per CTA.  Stage 1: the thread for (column c, j < 16) loads the R1 planes
+// z = j + 16 e of S (only the in-band ones; the rest are zero) and runs the
+// inverse R1-point DFT times conj(W_Z^(j k1)); stage 2: the thread for
+// (c, k1) runs the inverse 16-point DFT and stores the real part of planes
+// k1 + R1 k2.
+template <int R1>
+__global__ void __launch_bounds__(kThreads) k_asm_z4(AssembleArgs a, const unsigned char* __restrict__ zactive,
+                                                    const float2* __restrict__ tw)
+{
+  constexpr int R2 = 16, W = 64;
+  constexpr int LD = R2 * W + 8;
+  extern __shared__ float2 sm[];  // [R1][LD]
+  const int X = a.X, Y = a.Y;
+  const int yr = blockIdx.y, c0 = blockIdx.x * W;
+  const int nc = min(W, X - c0);
+  const size_t zstride = (size_t)Y * X;
+  const float2* src = a.S + (size_t)yr * X + c0;
+  for (int it = threadIdx.x; it < R2 * W; it += blockDim.x) {
+    const int c = it % W, j = it / W;
+    float2 v[R1];
+#pragma unroll
+    for (int e = 0; e < R1; ++e) {
+      const int z = j + R2 * e;
+      v[e] = (c < nc && zactive[z]) ? src[z * zstride + c] : make_float2(0.f, 0.f);
+    }
+    reg_dft<R1, +1>(v);
+#pragma unroll
+    for (int k1 = 1; k1 < R1; ++k1) {
+      float2 w = __ldg(tw + j * k1);
+      w.y = -w.y;
+      v[k1] = cmul(v[k1], w);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < R1; ++k1) sm[k1 * LD + j * W + c] = v[k1];
+  }
+  __syncthreads();
+  float* dst = a.out + (size_t)yr * X + c0;
+  for (int it = threadIdx.x; it < R1 * W; it += blockDim.x) {
+    const int c = it % W, k1 = it / W;
+    float2 u[R2];
+#pragma unroll
+    for (int jj = 0; jj < R2; ++jj) u[jj] = sm[k1 * LD + jj * W + c];
+    reg_dft<R2, +1>(u);
+    if (c < nc)
+#pragma unroll
+      for (int k2 = 0; k2 < R2; ++k2) dst[(size_t)(k1 + R1 * k2) * zstride + c] = u[k2].x;
+  }
+}
+
 __global__ void k_ramp(const float2* k0, int ndirs, int norders, int X, int Y, float dxyz, float fact, float2* ex,
                        float2* ey)
 {
@@ -749,10 +799,27 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
   size_t smz = fft_stage_smem(a.Z, Wz, a.Z * (Wz + 1), kThreads);
   KernelTimer* kt = kernel_timer();
   if (kt) kt->begin(s);
-  dispatch_fft_len(kSiteAsmZ, a.Z, [&]<int NF>() {
-    cudaFuncSetAttribute(k_asm_z<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
-    k_asm_z<NF><<<dim3((a.X + Wz - 1) / Wz, a.Y), kThreads, smz, s>>>(a, d_zact, pz, Wz);
-  });
+  const int zr1 = a.Z % 16 == 0 ? a.Z / 16 : 0;
+  if (zr1 == 2 || zr1 == 3 || zr1 == 4 || zr1 == 5 || zr1 == 6 || zr1 == 8) {
+    auto go = [&]<int R1>() {
+      const size_t bytes = (size_t)R1 * (16 * 64 + 8) * sizeof(float2);
+      cudaFuncSetAttribute(k_asm_z4<R1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+      k_asm_z4<R1><<<dim3((a.X + 63) / 64, a.Y), kThreads, bytes, s>>>(a, d_zact, pz.tw);
+    };
+    switch (zr1) {
+      case 2: go.template operator()<2>(); break;
+      case 3: go.template operator()<3>(); break;
+      case 4: go.template operator()<4>(); break;
+      case 5: go.template operator()<5>(); break;
+      case 6: go.template operator()<6>(); break;
+      default: go.template operator()<8>(); break;
+    }
+  } else {
+    dispatch_fft_len(kSiteAsmZ, a.Z, [&]<int NF>() {
+      cudaFuncSetAttribute(k_asm_z<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
+      k_asm_z<NF><<<dim3((a.X + Wz - 1) / Wz, a.Y), kThreads, smz, s>>>(a, d_zact, pz, Wz);
+    });
+  }
   if (kt) kt->end("k_asm_z", s, (double)np * a.X * a.Y * 8 + (double)a.X * a.Y * a.Z * 4);
   nl += 1;
   if (launches) *launches += nl;

@@ -314,6 +314,77 @@ int launch_ingest(const IngestArgs& a, cudaStream_t s, long long* launches)
   return (int)cudaGetLastError();
 }
 
+// Four-step variant of k_separate for nz = 16 * R1 (R1 <= 8): 16 columns of
+// one (direction, ky) row per CTA.  Stage 1: the thread for (column c,
+// j < 16) loads the R1 planes z = j + 16 e of every phase straight from HBM,
+// applies the bleach ratios and the separation matrix, and runs the R1-point
+// DFT of each band times W_nz^(j k1); stage 2: the thread for (c, band, k1)
+// runs the 16-point DFT over j and stores planes k1 + R1 k2 in place.
+template <int R1, int NPH>
+__global__ void __launch_bounds__(kThreads) k_separate4(float2* spec, const float* __restrict__ scale,
+                                                       const float* __restrict__ sepmat, int ny, int nxh,
+                                                       const float2* __restrict__ tw)
+{
+  constexpr int nph = NPH;
+  constexpr int R2 = 16, W = 16, NZ = R1 * R2;
+  constexpr int LD = R2 * W + 8;  // 2*LD = 16 mod 32 words
+  extern __shared__ float2 sm[];   // [nph * R1][LD]
+  __shared__ float M[kMaxPhases * kMaxPhases];
+  const int ky = blockIdx.y, c0 = blockIdx.x * W, d = blockIdx.z;
+  for (int i = threadIdx.x; i < nph * nph; i += blockDim.x) M[i] = sepmat[i];
+  __syncthreads();
+  const size_t plane = (size_t)ny * nxh;
+  float2* dbase = spec + (size_t)d * nph * NZ * plane + (size_t)ky * nxh + c0;
+  const float* dscale = scale + d * nph * NZ;
+  const int nc = min(W, nxh - c0);
+  {
+    const int c = threadIdx.x % W, j = threadIdx.x / W;  // R2 * W == blockDim
+    float2 in[NPH][R1];
+#pragma unroll
+    for (int e = 0; e < R1; ++e) {
+      const int z = j + R2 * e;
+#pragma unroll
+      for (int p = 0; p < nph; ++p) {
+        float sc = dscale[p * NZ + z];
+        float2 v = c < nc ? dbase[((size_t)p * NZ + z) * plane + c] : make_float2(0.f, 0.f);
+        in[p][e] = make_float2(v.x * sc, v.y * sc);
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < nph; ++b) {
+      float2 v[R1];
+#pragma unroll
+      for (int e = 0; e < R1; ++e) {
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int p = 0; p < nph; ++p) {
+          float m = M[b * nph + p];
+          acc.x += m * in[p][e].x;
+          acc.y += m * in[p][e].y;
+        }
+        v[e] = acc;
+      }
+      reg_dft<R1, -1>(v);
+#pragma unroll
+      for (int k1 = 1; k1 < R1; ++k1) v[k1] = cmul(v[k1], __ldg(tw + j * k1));
+#pragma unroll
+      for (int k1 = 0; k1 < R1; ++k1) sm[(b * R1 + k1) * LD + j * W + c] = v[k1];
+    }
+  }
+  __syncthreads();
+  for (int it = threadIdx.x; it < nph * R1 * W; it += blockDim.x) {
+    const int c = it % W, r = it / W;  // r = b * R1 + k1
+    const int b = r / R1, k1 = r - b * R1;
+    float2 u[R2];
+#pragma unroll
+    for (int jj = 0; jj < R2; ++jj) u[jj] = sm[r * LD + jj * W + c];
+    reg_dft<R2, -1>(u);
+    if (c < nc)
+#pragma unroll
+      for (int k2 = 0; k2 < R2; ++k2) dbase[((size_t)b * NZ + k1 + R1 * k2) * plane + c] = u[k2];
+  }
+}
+
 int launch_rescale(const float2* spec, int nx, int ny, int nz, int ndirs, int nphases, int t, int equalizez,
                    int equalizet, double* sdp0, float* scale, cudaStream_t s, long long* launches)
 {
@@ -335,10 +406,28 @@ int launch_separate(float2* spec, const float* scale, const float* sepmat, int n
   dim3 g((nxh + W - 1) / W, ny, ndirs);
   KernelTimer* kt = kernel_timer();
   if (kt) kt->begin(s);
-  dispatch_fft_len(kSiteSeparateZ, nz, [&]<int NF>() {
-    cudaFuncSetAttribute(k_separate<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_separate<NF><<<g, kThreads, sm, s>>>(spec, scale, sepmat, ny, nxh, nz, nphases, pz, W);
-  });
+  const int r1 = nz % 16 == 0 ? nz / 16 : 0;
+  if ((r1 == 2 || r1 == 3 || r1 == 4 || r1 == 5 || r1 == 6 || r1 == 8) && nphases == 5) {
+    dim3 g4((nxh + 15) / 16, ny, ndirs);
+    auto go = [&]<int R1>() {
+      const size_t bytes = (size_t)nphases * R1 * (16 * 16 + 8) * sizeof(float2);
+      cudaFuncSetAttribute(k_separate4<R1, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+      k_separate4<R1, 5><<<g4, kThreads, bytes, s>>>(spec, scale, sepmat, ny, nxh, pz.tw);
+    };
+    switch (r1) {
+      case 2: go.template operator()<2>(); break;
+      case 3: go.template operator()<3>(); break;
+      case 4: go.template operator()<4>(); break;
+      case 5: go.template operator()<5>(); break;
+      case 6: go.template operator()<6>(); break;
+      default: go.template operator()<8>(); break;
+    }
+  } else {
+    dispatch_fft_len(kSiteSeparateZ, nz, [&]<int NF>() {
+      cudaFuncSetAttribute(k_separate<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      k_separate<NF><<<g, kThreads, sm, s>>>(spec, scale, sepmat, ny, nxh, nz, nphases, pz, W);
+    });
+  }
   if (kt) kt->end("k_separate", s, 2.0 * ndirs * nphases * nz * (double)ny * nxh * sizeof(float2));
   if (launches) *launches += 1;
   return (int)cudaGetLastError();
