@@ -446,6 +446,13 @@ struct XwLanes {
 constexpr int kXwWarps = 4;
 
 template <int X>
+constexpr size_t xw_smem_bytes()
+{
+  constexpr int P = XwLanes<X>::P, E = X / P, G = 32 / P;
+  return ((size_t)kXwWarps * G * ((P + 1) * E + 1) + (size_t)kXwWarps * G * 2 * (X / 2)) * sizeof(float2);
+}
+
+template <int X>
 __global__ void __launch_bounds__(kXwWarps * 32, 3) k_asm_xw(AssembleArgs a, const int* __restrict__ plane_slot0,
                                                           const int* __restrict__ plane_nslot,
                                                           const Slot* __restrict__ slots,
@@ -454,7 +461,13 @@ __global__ void __launch_bounds__(kXwWarps * 32, 3) k_asm_xw(AssembleArgs a, con
 {
   constexpr int P = XwLanes<X>::P, E = X / P, G = 32 / P;
   constexpr int XB = (P + 1) * E + 1;
-  __shared__ float2 xs[kXwWarps * G * XB];
+  constexpr int NXB = X / 2;  // band columns (T row length)
+  // dynamic shared memory (xw_smem_bytes): the exchange buffers, then a
+  // two-entry ring per group into which the T row of the next slot is
+  // copied with cp.async while the current one is transformed
+  extern __shared__ __align__(16) float2 xw_dyn[];
+  float2* xs = xw_dyn;
+  float2(*ring)[2][NXB] = reinterpret_cast<float2(*)[2][NXB]>(xw_dyn + kXwWarps * G * XB);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane / P, p = lane - g * P;
   const int yr = (blockIdx.x * kXwWarps + warp) * G + g;
@@ -463,19 +476,36 @@ __global__ void __launch_bounds__(kXwWarps * 32, 3) k_asm_xw(AssembleArgs a, con
   const int s0 = plane_slot0[pidx], ns = plane_nslot[pidx], zout = plane_zout[pidx];
   const int nx = a.nx, Y = a.Y, xlo = nx / 2 - 1;
   float2* xb = xs + (warp * G + g) * XB;
+  float2(*rg)[NXB] = ring[warp * G + g];
+  // each lane copies 16-byte chunks (2 complex) of the nx-long row
+  auto prefetch = [&](int si) {
+    if (act && si < ns) {
+      const float2* trow = a.T + ((size_t)(s0 + si) * Y + yr) * nx;
+      for (int q = p; q < nx / 2; q += P) {
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(&rg[si & 1][2 * q]);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(trow + 2 * q) : "memory");
+      }
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  };
   float2 acc[E];
 #pragma unroll
   for (int i = 0; i < E; ++i) acc[i] = make_float2(0.f, 0.f);
+  prefetch(0);
   for (int si = 0; si < ns; ++si) {  // same trip count for every lane of the warp
     const Slot sl = slots[s0 + si];
-    const float2* trow = a.T + ((size_t)(s0 + si) * Y + (act ? yr : 0)) * nx;
+    prefetch(si + 1);
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // this lane's copies of slot si landed
+    __syncwarp();                                             // ... and every other lane's
+    const float2* trow = rg[si & 1];
     float2 v[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) {
       const int x = p + P * e;
       const bool in = act && (x <= nx / 2 || x >= X - xlo);
-      v[e] = in ? __ldg(trow + (x <= nx / 2 ? x : x - X) + xlo) : make_float2(0.f, 0.f);
+      v[e] = in ? trow[(x <= nx / 2 ? x : x - X) + xlo] : make_float2(0.f, 0.f);
     }
+    __syncwarp();  // the ring entry is read before the next prefetch overwrites it
     reg_line<X, P, +1>(v, p, xb, tw, true);
     if (sl.dir < 0) {
 #pragma unroll
@@ -779,12 +809,15 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
     auto launch_xw = [&]<int XN>() {
       constexpr int G = 32 / XwLanes<XN>::P;
       const int rows_per_cta = kXwWarps * G;
-      k_asm_xw<XN><<<dim3((a.Y + rows_per_cta - 1) / rows_per_cta, (unsigned)(pj - pi)), kXwWarps * 32, 0, s>>>(
-          ax, d_p0 + pi, d_pn + pi, d_slots, d_pz + pi, px.tw);
+      constexpr size_t bytes = xw_smem_bytes<XN>();
+      cudaFuncSetAttribute(k_asm_xw<XN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+      k_asm_xw<XN><<<dim3((a.Y + rows_per_cta - 1) / rows_per_cta, (unsigned)(pj - pi)), kXwWarps * 32, bytes,
+                     s>>>(ax, d_p0 + pi, d_pn + pi, d_slots, d_pz + pi, px.tw);
     };
-    if (a.X == 1024) launch_xw.template operator()<1024>();
-    else if (a.X == 512) launch_xw.template operator()<512>();
-    else if (a.X == 256) launch_xw.template operator()<256>();
+    // the warp kernel's prefetch ring holds X/2 = nx columns (zoom factor 2)
+    if (a.X == 1024 && a.nx == 512) launch_xw.template operator()<1024>();
+    else if (a.X == 512 && a.nx == 256) launch_xw.template operator()<512>();
+    else if (a.X == 256 && a.nx == 128) launch_xw.template operator()<256>();
     else
       dispatch_fft_len(kSiteAsmX, a.X, [&]<int NF>() {
         cudaFuncSetAttribute(k_asm_x<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);

@@ -169,6 +169,107 @@ __global__ void __launch_bounds__(kThreads) k_fft_cols(float2* data, int n, int 
   }
 }
 
+// Warp-level variant of k_ingest_x for nx in {256, 512, 1024}: each group of
+// P lanes owns one pair of rows (row 2l real, row 2l+1 imaginary), loads its
+// pixels x = p + P e straight from the raw plane, applies the flat field and
+// both edge blends in registers (row ends by warp shuffle), transforms the
+// line in registers and splits the two real spectra through its exchange
+// buffer.  No CTA barrier.
+template <int N>
+struct IngestLanes {
+  static constexpr int P = N == 1024 ? 32 : 16;
+};
+constexpr int kIngestWarps = 4;
+
+template <typename T, int N>
+__global__ void __launch_bounds__(kIngestWarps * 32, 3) k_ingest_xw(IngestArgs a, const float2* __restrict__ tw)
+{
+  constexpr int P = IngestLanes<N>::P, E = N / P, G = 32 / P;
+  constexpr int XB = (P + 1) * E + 1;  // >= N: also holds the transformed line
+  static_assert(XB >= N, "exchange buffer too small for the split");
+  __shared__ float2 xs[kIngestWarps][G][XB];
+  const int ny = a.ny, nxh = N / 2 + 1;
+  const int pl = blockIdx.y;  // plane id = (d*nph + p)*nz + z
+  const int z = pl % a.nz;
+  const int dp = pl / a.nz;
+  const int ph = dp % a.nphases, d = dp / a.nphases;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane / P, p = lane - g * P;
+  const int l = (blockIdx.x * kIngestWarps + warp) * G + g;  // row pair of this group
+  const int y = 2 * l;
+  const bool r0 = y < ny, r1 = y + 1 < ny;
+  const T* plane = (const T*)a.raw + (size_t)raw_section(d, ph, z, a.nz, a.ndirs, a.nphases, a.fastSI) * N * ny;
+  const int napo = a.napodize;
+  const bool plainbg = !a.bg && !a.slope;
+  float2 v[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const int x = p + P * e;
+    float re = 0.f, im = 0.f;
+    if (plainbg) {
+      if (r0) re = ((float)plane[(size_t)y * N + x] - a.bgconst - a.bgextra) * 1.0f * a.inscale;
+      if (r1) im = ((float)plane[(size_t)(y + 1) * N + x] - a.bgconst - a.bgextra) * 1.0f * a.inscale;
+    } else {
+      if (r0) re = flat(plane, a, y, x);
+      if (r1) im = flat(plane, a, y + 1, x);
+    }
+    v[e] = make_float2(re, im);
+  }
+  // top/bottom edge blend (apodize_x_kernel) with the unblended end rows
+  const bool e0 = r0 && (y < napo || (ny - 1 - y) < napo);
+  const bool e1 = r1 && (y + 1 < napo || (ny - 2 - y) < napo);
+  if (e0 || e1) {
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int x = p + P * e;
+      const float diff = (flat(plane, a, ny - 1, x) - flat(plane, a, 0, x)) / 2.0f;
+      if (e0) {
+        if (y < napo) v[e].x += diff * a.apofact[y];
+        if ((ny - 1 - y) < napo) v[e].x -= diff * a.apofact[ny - 1 - y];
+      }
+      if (e1) {
+        if (y + 1 < napo) v[e].y += diff * a.apofact[y + 1];
+        if ((ny - 2 - y) < napo) v[e].y -= diff * a.apofact[ny - 2 - y];
+      }
+    }
+  }
+  // left/right edge blend (apodize_y_kernel) from the blended row ends
+  if (napo > 0) {
+    const int gb = g * P;
+    const float2 first = make_float2(__shfl_sync(0xffffffffu, v[0].x, gb), __shfl_sync(0xffffffffu, v[0].y, gb));
+    const float2 last = make_float2(__shfl_sync(0xffffffffu, v[E - 1].x, gb + P - 1),
+                                    __shfl_sync(0xffffffffu, v[E - 1].y, gb + P - 1));
+    const float dx = (last.x - first.x) / 2.0f, dy = (last.y - first.y) / 2.0f;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int x = p + P * e;
+      if (x < napo) {
+        v[e].x += dx * a.apofact[x];
+        v[e].y += dy * a.apofact[x];
+      } else if (x >= N - napo) {
+        v[e].x -= dx * a.apofact[N - 1 - x];
+        v[e].y -= dy * a.apofact[N - 1 - x];
+      }
+    }
+  }
+  float2* xb = xs[warp][g];
+  reg_line<N, P, -1>(v, p, xb, tw, true);
+  // split the two real transforms: X[k] and X[N-k] live in different lanes
+#pragma unroll
+  for (int m = 0; m < E / P; ++m)
+#pragma unroll
+    for (int k2 = 0; k2 < P; ++k2) xb[p + P * m + E * k2] = v[m * P + k2];
+  __syncwarp();
+  float2* dst = a.spec + (size_t)pl * ny * nxh;
+  for (int k = p; k < nxh; k += P) {
+    const float2 zk = xb[k], zn = xb[(N - k) % N];
+    const float2 A = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+    const float2 B = make_float2(0.5f * (zk.y + zn.y), -0.5f * (zk.x - zn.x));
+    if (r0) dst[(size_t)y * nxh + k] = A;
+    if (r1) dst[(size_t)(y + 1) * nxh + k] = B;
+  }
+}
+
 // Four-step variant (col_fft.cuh) for the lengths with a column
 // configuration: 8 columns of one plane per CTA, loaded straight from HBM.
 template <int N>
@@ -269,6 +370,17 @@ int launch_ingest(const IngestArgs& a, cudaStream_t s, long long* launches)
   KernelTimer* kt = kernel_timer();
   const double specb = (double)nplanes * a.ny * nxh * sizeof(float2);
   if (kt) kt->begin(s);
+  auto go_w = [&]<int N>() {
+    constexpr int G = 32 / IngestLanes<N>::P;
+    const int pairs = (a.ny + 1) / 2;
+    dim3 gw((pairs + kIngestWarps * G - 1) / (kIngestWarps * G), nplanes);
+    if (a.raw_is_u16) k_ingest_xw<uint16_t, N><<<gw, kIngestWarps * 32, 0, s>>>(a, px.tw);
+    else k_ingest_xw<float, N><<<gw, kIngestWarps * 32, 0, s>>>(a, px.tw);
+  };
+  if (a.nx == 512) go_w.template operator()<512>();
+  else if (a.nx == 1024) go_w.template operator()<1024>();
+  else if (a.nx == 256) go_w.template operator()<256>();
+  else
   dispatch_fft_len(kSiteIngestX, a.nx, [&]<int NF>() {
     if (a.raw_is_u16) {
       if (a.nx % 8 == 0) {
