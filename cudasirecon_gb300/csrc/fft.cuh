@@ -27,7 +27,9 @@ struct FFTPlan {
   int n;
   int nstages;
   int radix[kMaxStages];
-  const float2* tw;  // device table of n twiddles exp(-2 pi i k/n)
+  const float2* tw;   // device table of n twiddles exp(-2 pi i k/n)
+  const float2* twr;  // register path (n with P lanes): twr[(k1-1)*P + p] = tw[p*k1], lane-major so a
+                      // lane group reads consecutive entries; null when n has no register path
 };
 
 #ifdef __CUDACC__

@@ -125,18 +125,25 @@ bool get_fft_plan(int n, FFTPlan* plan)
   p.n = n;
   p.nstages = (int)radix.size();
   for (int i = 0; i < p.nstages; ++i) p.radix[i] = radix[i];
-  std::vector<float2> tw(n);
+  std::vector<float2> tw(2 * (size_t)n);
   for (int k = 0; k < n; ++k) {
     double a = -2.0 * M_PI * (double)k / (double)n;
     tw[k] = make_float2((float)cos(a), (float)sin(a));
   }
+  const int P = reg_fft_lanes(n);
+  if (P) {
+    const int E = n / P;
+    for (int k1 = 1; k1 < E; ++k1)
+      for (int q = 0; q < P; ++q) tw[n + (size_t)(k1 - 1) * P + q] = tw[((size_t)q * k1) % n];
+  }
   float2* d = nullptr;
-  if (cudaMalloc(&d, sizeof(float2) * n) != cudaSuccess) return false;
-  if (cudaMemcpy(d, tw.data(), sizeof(float2) * n, cudaMemcpyHostToDevice) != cudaSuccess) {
+  if (cudaMalloc(&d, sizeof(float2) * 2 * n) != cudaSuccess) return false;
+  if (cudaMemcpy(d, tw.data(), sizeof(float2) * 2 * n, cudaMemcpyHostToDevice) != cudaSuccess) {
     cudaFree(d);
     return false;
   }
   p.tw = d;
+  p.twr = P ? d + n : nullptr;
   g_plans[{dev, n}] = p;
   *plan = p;
   return true;

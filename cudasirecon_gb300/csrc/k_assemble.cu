@@ -457,7 +457,7 @@ __global__ void __launch_bounds__(kXwWarps * 32, 3) k_asm_xw(AssembleArgs a, con
                                                           const int* __restrict__ plane_nslot,
                                                           const Slot* __restrict__ slots,
                                                           const int* __restrict__ plane_zout,
-                                                          const float2* __restrict__ tw)
+                                                          const float2* __restrict__ twr)
 {
   constexpr int P = XwLanes<X>::P, E = X / P, G = 32 / P;
   constexpr int XB = (P + 1) * E + 1;
@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(kXwWarps * 32, 3) k_asm_xw(AssembleArgs a, con
       v[e] = in ? trow[(x <= nx / 2 ? x : x - X) + xlo] : make_float2(0.f, 0.f);
     }
     __syncwarp();  // the ring entry is read before the next prefetch overwrites it
-    reg_line<X, P, +1>(v, p, xb, tw, true);
+    reg_line<X, P, +1>(v, p, xb, twr, true);
     if (sl.dir < 0) {
 #pragma unroll
       for (int i = 0; i < E; ++i) {
@@ -812,7 +812,7 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
       constexpr size_t bytes = xw_smem_bytes<XN>();
       cudaFuncSetAttribute(k_asm_xw<XN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
       k_asm_xw<XN><<<dim3((a.Y + rows_per_cta - 1) / rows_per_cta, (unsigned)(pj - pi)), kXwWarps * 32, bytes,
-                     s>>>(ax, d_p0 + pi, d_pn + pi, d_slots, d_pz + pi, px.tw);
+                     s>>>(ax, d_p0 + pi, d_pn + pi, d_slots, d_pz + pi, px.twr);
     };
     // the warp kernel's prefetch ring holds X/2 = nx columns (zoom factor 2)
     if (a.X == 1024 && a.nx == 512) launch_xw.template operator()<1024>();

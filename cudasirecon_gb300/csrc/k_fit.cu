@@ -146,7 +146,7 @@ struct OvlLanes {
 constexpr int kOvlWarps = 4;
 
 template <int N>
-__global__ void __launch_bounds__(kOvlWarps * 32, 3) k_ovl_build_xw(OverlapArgs a, const float2* __restrict__ tw)
+__global__ void __launch_bounds__(kOvlWarps * 32, 3) k_ovl_build_xw(OverlapArgs a, const float2* __restrict__ twr)
 {
   constexpr int P = OvlLanes<N>::P, E = N / P, G = 32 / P;
   constexpr int XB = (P + 1) * E + 1;
@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(kOvlWarps * 32, 3) k_ovl_build_xw(OverlapArgs 
 #pragma unroll
   for (int e = 0; e < E; ++e) v[e] = lines[warp][g][p + P * e];
   __syncwarp();  // every lane has its values before the buffer becomes the exchange
-  reg_line<N, P, +1>(v, p, lines[warp][g], tw, true);
+  reg_line<N, P, +1>(v, p, lines[warp][g], twr, true);
   const int L = l0 + g;
   if (L < nlines) {
     const int row = L >> 1, ov = L & 1;
@@ -583,7 +583,7 @@ int launch_overlaps(OverlapArgs& a, cudaStream_t s, long long* launches)
     constexpr int G = 32 / OvlLanes<N>::P;
     const int nlines = 2 * nzb * a.ny;
     const int per_cta = kOvlWarps * G;
-    k_ovl_build_xw<N><<<(nlines + per_cta - 1) / per_cta, kOvlWarps * 32, 0, s>>>(a, px.tw);
+    k_ovl_build_xw<N><<<(nlines + per_cta - 1) / per_cta, kOvlWarps * 32, 0, s>>>(a, px.twr);
   };
   if (a.nx == 512) launch_w.template operator()<512>();
   else if (a.nx == 1024) launch_w.template operator()<1024>();

@@ -182,7 +182,7 @@ struct IngestLanes {
 constexpr int kIngestWarps = 4;
 
 template <typename T, int N>
-__global__ void __launch_bounds__(kIngestWarps * 32, 3) k_ingest_xw(IngestArgs a, const float2* __restrict__ tw)
+__global__ void __launch_bounds__(kIngestWarps * 32, 3) k_ingest_xw(IngestArgs a, const float2* __restrict__ twr)
 {
   constexpr int P = IngestLanes<N>::P, E = N / P, G = 32 / P;
   constexpr int XB = (P + 1) * E + 1;  // >= N: also holds the transformed line
@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(kIngestWarps * 32, 3) k_ingest_xw(IngestArgs a
     }
   }
   float2* xb = xs[warp][g];
-  reg_line<N, P, -1>(v, p, xb, tw, true);
+  reg_line<N, P, -1>(v, p, xb, twr, true);
   // split the two real transforms: X[k] and X[N-k] live in different lanes
 #pragma unroll
   for (int m = 0; m < E / P; ++m)
@@ -374,8 +374,8 @@ int launch_ingest(const IngestArgs& a, cudaStream_t s, long long* launches)
     constexpr int G = 32 / IngestLanes<N>::P;
     const int pairs = (a.ny + 1) / 2;
     dim3 gw((pairs + kIngestWarps * G - 1) / (kIngestWarps * G), nplanes);
-    if (a.raw_is_u16) k_ingest_xw<uint16_t, N><<<gw, kIngestWarps * 32, 0, s>>>(a, px.tw);
-    else k_ingest_xw<float, N><<<gw, kIngestWarps * 32, 0, s>>>(a, px.tw);
+    if (a.raw_is_u16) k_ingest_xw<uint16_t, N><<<gw, kIngestWarps * 32, 0, s>>>(a, px.twr);
+    else k_ingest_xw<float, N><<<gw, kIngestWarps * 32, 0, s>>>(a, px.twr);
   };
   if (a.nx == 512) go_w.template operator()<512>();
   else if (a.nx == 1024) go_w.template operator()<1024>();

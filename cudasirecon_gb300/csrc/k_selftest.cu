@@ -95,8 +95,9 @@ namespace {
 constexpr size_t kNoAllocMaxElems = (size_t)1 << 21;  // complex values per call
 constexpr int kNoAllocMaxN = 8192;                    // longest line
 
-// [0, kNoAllocMaxN): twiddles; then the staging area for the lines
-static __device__ __align__(256) float2 g_noalloc_scratch[kNoAllocMaxN + kNoAllocMaxElems];
+// [0, kNoAllocMaxN): twiddles; [kNoAllocMaxN, 2 kNoAllocMaxN): the same
+// twiddles in the register path's lane-major order; then the staging area
+static __device__ __align__(256) float2 g_noalloc_scratch[2 * kNoAllocMaxN + kNoAllocMaxElems];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mu;
@@ -117,13 +118,23 @@ cudaError_t noalloc_scratch(int dev, float2** out)
   return cudaSuccess;
 }
 
-// tw[k] = exp(-2 pi i k / n), computed in double precision on the device
-__global__ void k_noalloc_twiddles(float2* tw, int n)
+// tw[k] = exp(-2 pi i k / n), computed in double precision on the device;
+// with P register-path lanes (P > 0) also twr[(k1-1)*P + q] = tw[q*k1 mod n]
+// for k1 < n/P (FFTPlan::twr), each entry from the same formula as tw
+__device__ __forceinline__ float2 noalloc_twiddle(int k, int n)
+{
+  double s, c;
+  sincospi(-2.0 * (double)k / (double)n, &s, &c);
+  return make_float2((float)c, (float)s);
+}
+__global__ void k_noalloc_twiddles(float2* tw, float2* twr, int n, int P)
 {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    double s, c;
-    sincospi(-2.0 * (double)k / (double)n, &s, &c);
-    tw[k] = make_float2((float)c, (float)s);
+    tw[k] = noalloc_twiddle(k, n);
+    if (P > 0 && k < n - P) {
+      const int k1 = k / P + 1, q = k % P;
+      twr[k] = noalloc_twiddle((int)(((long long)q * k1) % n), n);
+    }
   }
 }
 
@@ -159,10 +170,13 @@ extern "C" int SRX_fftLinesNoAlloc(const float* in, float* out, int n, int nline
   e = noalloc_scratch(dev, &base);
   if (e != cudaSuccess) return noalloc_fail("SRX_fftLinesNoAlloc: cudaGetSymbolAddress", e);
   float2* tw = base;
-  float2* data = base + kNoAllocMaxN;
+  float2* twr = base + kNoAllocMaxN;
+  float2* data = base + 2 * kNoAllocMaxN;
+  const int P = reg_fft_lanes(n);
   p.tw = tw;
+  p.twr = P ? twr : nullptr;
   const size_t bytes = (size_t)n * nlines * sizeof(float2);
-  k_noalloc_twiddles<<<(n + 255) / 256, 256>>>(tw, n);
+  k_noalloc_twiddles<<<(n + 255) / 256, 256>>>(tw, twr, n, P);
   e = cudaMemcpy(data, in, bytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return noalloc_fail("SRX_fftLinesNoAlloc: input copy", e);
   int nl = std::max(1, std::min(nlines, kFftElems / (n + 1)));
