@@ -19,6 +19,7 @@
 // k_asm_x (zero-padded x IFFT, ramp, weighted sum over all (d, o) into S)
 // and k_asm_z (one z IFFT of S, real part) write the zoomed output once.
 #include <algorithm>
+#include <cmath>
 #include <vector>
 
 #include "col_fft.cuh"
@@ -56,33 +57,14 @@ struct FilterK {
   float rdkrotf;                       // 1 / dkrotf
   float min_dkr, rmin_dkr, supp_r;     // suppression radius (1/um) and its unit
   float rrcut;                         // 1 / rdistcutoff
+  float cut2hi;                        // rdistcutoff^2 (1 + 1e-6): rejects only terms outside the support
 };
-
-// bilinear RA-OTF lookup at radius kr (otf_lookup's arithmetic with
-// krindex = kr * (1/dkrotf))
-__device__ __forceinline__ float2 otf_lookup_rr(const float2* __restrict__ otf, const OTFView& v, float krindex,
-                                               const OtfKz& z)
-{
-  int ir = (int)floorf(krindex);
-  float ar = krindex - ir;
-  int last = v.nxotf * v.nzotf - 1;
-  int i00 = min(max(ir * v.nzotf + z.iz, 0), last);
-  int i01 = min(max(ir * v.nzotf + z.izp, 0), last);
-  int i10 = min(max((ir + 1) * v.nzotf + z.iz, 0), last);
-  int i11 = min(max((ir + 1) * v.nzotf + z.izp, 0), last);
-  float2 a = __ldg(otf + i00), b = __ldg(otf + i01), c = __ldg(otf + i10), d = __ldg(otf + i11);
-  const float az = z.az;
-  float2 r;
-  r.x = (1 - ar) * (a.x * (1 - az) + b.x * az) + ar * (c.x * (1 - az) + d.x * az);
-  r.y = (1 - ar) * (a.y * (1 - az) + b.y * az) + ar * (c.y * (1 - az) + d.y * az);
-  return r;
-}
 
 // Wiener scale of pixel (x1f, y1f, z0) of band (dir, order): the body of
 // filterbands_kernel1 (gpuFunctionsImpl.cu:1504-1592) without the final
 // conjamp factor.  ND/NO: compile-time direction and order counts (0: use
 // the runtime values).
-template <int ND, int NO>
+template <int ND, int NO, bool CLAMP>
 __device__ __forceinline__ float2 filter_scale(const FilterArgs& a, const FilterK& k, int order, int z0, float rdist1, float x1f,
                                float y1f)
 {
@@ -93,7 +75,7 @@ __device__ __forceinline__ float2 filter_scale(const FilterArgs& a, const Filter
   // order-0 damping's axial part |z0 / zdc0|^3, the same for every term
   const float zf = fabsf(z0 / (float)a.zdc[0]);
   const float zf3 = zf * zf * zf;
-  float2 otf1 = otf_lookup_rr(a.otf.otf[order], a.otf, rdist1 * k.rdkrotf, kzi);
+  float2 otf1 = otf_lookup_rr<CLAMP>(a.otf.otf[order], a.otf, rdist1 * k.rdkrotf, kzi);
   float weight = otf1.x * otf1.x + otf1.y * otf1.y;
   if (order != 0) weight *= a.ampmag2[dir * no + order];
   float dampfact = k.rnv[dir * no + order];
@@ -118,9 +100,11 @@ __device__ __forceinline__ float2 filter_scale(const FilterArgs& a, const Filter
       const float sx = order2 < 0 ? -k.kxo[dir2 * no + ao2] : k.kxo[dir2 * no + ao2];
       const float sy = order2 < 0 ? -k.kyo[dir2 * no + ao2] : k.kyo[dir2 * no + ao2];
       const float x2 = xabs - sx, y2 = yabs - sy;
-      const float rdist2 = sqrtf(x2 * x2 + y2 * y2);
+      const float r2 = x2 * x2 + y2 * y2;
+      if (r2 >= k.cut2hi) continue;  // far outside: the exact test below would fail too
+      const float rdist2 = sqrtf(r2);
       if (rdist2 < a.rdistcutoff) {
-        const float2 otf2 = otf_lookup_rr(a.otf.otf[ao2], a.otf, rdist2 * k.rdkrotf, kzi);
+        const float2 otf2 = otf_lookup_rr<CLAMP>(a.otf.otf[ao2], a.otf, rdist2 * k.rdkrotf, kzi);
         float w = (otf2.x * otf2.x + otf2.y * otf2.y) * k.termw[dir2 * no + ao2];
         if (a.suppress && order2 != 0 && rdist2 <= k.supp_r)
           w *= dev_suppress(rdist2 * k.rmin_dkr);
@@ -175,7 +159,7 @@ __device__ __forceinline__ void apply_side(float2& re, float2& im, float2 scale,
   }
 }
 
-template <int ND, int NO>
+template <int ND, int NO, bool CLAMP>
 __global__ void __launch_bounds__(kThreads) k_filter(const __grid_constant__ FilterArgs a, const __grid_constant__ FilterK k)
 {
   const int nx = a.nx, ny = a.ny, nz = a.nz, nxh = nx / 2 + 1;
@@ -205,7 +189,7 @@ __global__ void __launch_bounds__(kThreads) k_filter(const __grid_constant__ Fil
     if (b2) b2[ind] = make_float2(0.f, 0.f);
     return;
   }
-  float2 s1 = filter_scale<ND, NO>(a, k, order, z0, rdist1, x1f, y1f);
+  float2 s1 = filter_scale<ND, NO, CLAMP>(a, k, order, z0, rdist1, x1f, y1f);
   if (order == 0) {
     b1[ind] = cmul(b1[ind], s1);
     return;
@@ -218,7 +202,7 @@ __global__ void __launch_bounds__(kThreads) k_filter(const __grid_constant__ Fil
     const int x2 = -jin;
     float x2f = x2 * a.dkx, y2f = y2 * a.dky;
     float rdist2 = sqrtf(x2f * x2f + y2f * y2f);
-    float2 s2 = filter_scale<ND, NO>(a, k, order, -z0, rdist2, x2f, y2f);
+    float2 s2 = filter_scale<ND, NO, CLAMP>(a, k, order, -z0, rdist2, x2f, y2f);
     apply_side(re, im, cmul(s2, a.conjamp[order]), true);
   }
   b1[ind] = re;
@@ -668,11 +652,17 @@ int launch_filter(const FilterArgs& a, cudaStream_t s, long long* launches)
   k.rmin_dkr = 1.f / k.min_dkr;
   k.supp_r = a.supp_radius * k.min_dkr;
   k.rrcut = 1.f / a.rdistcutoff;
+  k.cut2hi = (float)((double)a.rdistcutoff * a.rdistcutoff * (1.0 + 1e-6));
+  // every looked-up radius is <= rdistcutoff, so the table is never left
+  // when floor(rdistcutoff / dkrotf) + 2 <= nxotf
+  const bool clamp = !(std::floor(a.rdistcutoff * k.rdkrotf) + 2 <= a.otf.nxotf);
   KernelTimer* kt = kernel_timer();
   if (kt) kt->begin(s);
-  if (a.ndirs == 3 && a.norders == 3) k_filter<3, 3><<<g, kThreads, 0, s>>>(a, k);
-  else if (a.ndirs == 3 && a.norders == 2) k_filter<3, 2><<<g, kThreads, 0, s>>>(a, k);
-  else k_filter<0, 0><<<g, kThreads, 0, s>>>(a, k);
+  if (a.ndirs == 3 && a.norders == 3 && !clamp) k_filter<3, 3, false><<<g, kThreads, 0, s>>>(a, k);
+  else if (a.ndirs == 3 && a.norders == 3) k_filter<3, 3, true><<<g, kThreads, 0, s>>>(a, k);
+  else if (a.ndirs == 3 && a.norders == 2 && !clamp) k_filter<3, 2, false><<<g, kThreads, 0, s>>>(a, k);
+  else if (a.ndirs == 3 && a.norders == 2) k_filter<3, 2, true><<<g, kThreads, 0, s>>>(a, k);
+  else k_filter<0, 0, true><<<g, kThreads, 0, s>>>(a, k);
   // every element of the 2*norders-1 bands of this direction is read (in
   // band) or only written (cleared)
   double planeb = (double)a.ny * nxh * sizeof(float2);

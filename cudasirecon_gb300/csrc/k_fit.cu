@@ -38,7 +38,9 @@ constexpr int kMaxElems = kFftElems;
 // makeOverlaps0Kernel (ov 0, gpuFunctionsImpl.cu:677-778) / makeOverlaps1Kernel
 // (ov 1, 780-872): the order-1/order-2 band value times the partner OTF over
 // sqrt(|OTF1|^2 + |OTF2|^2) inside both supports, merged re + i im.
-__device__ __forceinline__ float2 ovl_value(const OverlapArgs& a, int ov, int zb, int i, int j)
+// kzi = otf_kz(a.otf, zb - a.zdc), rdk = 1 / a.otf.dkrotf (per row / thread)
+__device__ __forceinline__ float2 ovl_value(const OverlapArgs& a, int ov, int zb, int i, int j, const OtfKz& kzi,
+                                            float rdk)
 {
   const int nx = a.nx, ny = a.ny, nz = a.nz, nxh = nx / 2 + 1;
   const size_t bplane = (size_t)ny * nxh;
@@ -56,17 +58,16 @@ __device__ __forceinline__ float2 ovl_value(const OverlapArgs& a, int ov, int zb
   int zin = ((conj ? -z0 : z0) + nz) % nz;
   size_t indin = (size_t)zin * bplane + (size_t)iin * nxh + jin;
   if (z0 == 0 && a.nokz0) return make_float2(0.f, 0.f);
-  const OtfKz kzi = otf_kz(a.otf, z0);
   if (ov == 0 && rdist1 <= cut) {
     float x12 = x1f - a.kx, y12 = y1f - a.ky;
     float r12 = sqrtf(x12 * x12 + y12 * y12);
     if (r12 <= cut) {
-      float2 o1 = otf_lookup_rk(a.otf.otf[a.order1], a.otf, rdist1, kzi);
+      float2 o1 = otf_lookup_rr(a.otf.otf[a.order1], a.otf, rdist1 * rdk, kzi);
       if (sqrtf(cmag2(o1)) > a.otfcutoff) {
-        float2 o12 = otf_lookup_rk(a.otf.otf[a.order2], a.otf, r12, kzi);
+        float2 o12 = otf_lookup_rr(a.otf.otf[a.order2], a.otf, r12 * rdk, kzi);
         if (sqrtf(cmag2(o12)) * a.order0_2_factor > a.otfcutoff) {
-          float root = sqrtf(cmag2(o1) + cmag2(o12));
-          float2 fact = make_float2(o12.x / root, o12.y / root);
+          const float rroot = 1.f / sqrtf(cmag2(o1) + cmag2(o12));
+          float2 fact = make_float2(o12.x * rroot, o12.y * rroot);
           const float2* b1re = a.order1 == 0 ? a.bands : a.bands + (size_t)(2 * a.order1 - 1) * nz * bplane;
           float2 vre = b1re[indin];
           float2 vim = a.order1 == 0 ? make_float2(0.f, 0.f) : a.bands[(size_t)(2 * a.order1) * nz * bplane + indin];
@@ -84,12 +85,12 @@ __device__ __forceinline__ float2 ovl_value(const OverlapArgs& a, int ov, int zb
     float x21 = x1f + a.kx, y21 = y1f + a.ky;
     float r21 = sqrtf(x21 * x21 + y21 * y21);
     if (r21 <= cut) {
-      float2 o2 = otf_lookup_rk(a.otf.otf[a.order2], a.otf, rdist1, kzi);
+      float2 o2 = otf_lookup_rr(a.otf.otf[a.order2], a.otf, rdist1 * rdk, kzi);
       if (sqrtf(cmag2(o2)) * a.order0_2_factor > a.otfcutoff) {
-        float2 o21 = otf_lookup_rk(a.otf.otf[a.order1], a.otf, r21, kzi);
+        float2 o21 = otf_lookup_rr(a.otf.otf[a.order1], a.otf, r21 * rdk, kzi);
         if (sqrtf(cmag2(o21)) > a.otfcutoff) {
-          float root = sqrtf(cmag2(o2) + cmag2(o21));
-          float2 fact = make_float2(o21.x / root, o21.y / root);
+          const float rroot = 1.f / sqrtf(cmag2(o2) + cmag2(o21));
+          float2 fact = make_float2(o21.x * rroot, o21.y * rroot);
           float2 vre = a.bands[(size_t)(2 * a.order2 - 1) * nz * bplane + indin];
           float2 vim = a.bands[(size_t)(2 * a.order2) * nz * bplane + indin];
           if (conj) {
@@ -121,7 +122,7 @@ __global__ void __launch_bounds__(kThreads) k_ovl_build_x(OverlapArgs a, FFTPlan
     if (r < nrows) {
       int row = row0 + r;
       int zb = row / ny, i = row - zb * ny;
-      val = ovl_value(a, ov, zb, i, j);
+      val = ovl_value(a, ov, zb, i, j, otf_kz(a.otf, zb - a.zdc), 1.f / a.otf.dkrotf);
     }
     sm[l * ldl + j] = val;
   }
@@ -157,17 +158,20 @@ __global__ void __launch_bounds__(kOvlWarps * 32, 3) k_ovl_build_xw(OverlapArgs 
   const int ny = a.ny, nzb = 2 * a.zdc + 1;
   const int nlines = 2 * nzb * ny;
   const int l0 = (blockIdx.x * kOvlWarps + warp) * G;
-  // build the warp's G lines (all 32 lanes, consecutive j)
-  for (int t = lane; t < G * N; t += 32) {
-    const int gl = t / N, j = t - gl * N;
+  // build the warp's G lines (all 32 lanes, consecutive j); the kz part of
+  // the OTF lookups is the same along a line
+  const float rdk = 1.f / a.otf.dkrotf;
+#pragma unroll
+  for (int gl = 0; gl < G; ++gl) {
     const int L = l0 + gl;
-    float2 v = make_float2(0.f, 0.f);
-    if (L < nlines) {
-      const int row = L >> 1, ov = L & 1;
-      const int zb = row / ny, i = row - zb * ny;
-      v = ovl_value(a, ov, zb, i, j);
+    if (L >= nlines) {
+      for (int j = lane; j < N; j += 32) lines[warp][gl][j] = make_float2(0.f, 0.f);
+      continue;
     }
-    lines[warp][gl][j] = v;
+    const int row = L >> 1, ov = L & 1;
+    const int zb = row / ny, i = row - zb * ny;
+    const OtfKz kzi = otf_kz(a.otf, zb - a.zdc);
+    for (int j = lane; j < N; j += 32) lines[warp][gl][j] = ovl_value(a, ov, zb, i, j, kzi, rdk);
   }
   __syncwarp();
   float2 v[E];

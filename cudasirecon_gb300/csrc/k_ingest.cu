@@ -39,6 +39,14 @@ __device__ __forceinline__ float flat(const T* __restrict__ plane, const IngestA
   return (v - bg - a.bgextra) * sl * a.inscale;
 }
 
+// flat() for a raw value already loaded
+__device__ __forceinline__ float flat_v(float v, const IngestArgs& a, int y, int x)
+{
+  float bg = a.bg ? __ldg(a.bg + (size_t)y * a.nx + x) : a.bgconst;
+  float sl = a.slope ? __ldg(a.slope + (size_t)y * a.nx + x) : 1.0f;
+  return (v - bg - a.bgextra) * sl * a.inscale;
+}
+
 // VEC consecutive raw pixels of row y starting at x (x % VEC == 0), as floats
 template <typename T, int VEC>
 __device__ __forceinline__ void load_vec(const T* __restrict__ plane, int nx, int y, int x, float* out)
@@ -170,24 +178,35 @@ __global__ void __launch_bounds__(kThreads) k_fft_cols(float2* data, int n, int 
 }
 
 // Warp-level variant of k_ingest_x for nx in {256, 512, 1024}: each group of
-// P lanes owns one pair of rows (row 2l real, row 2l+1 imaginary), loads its
-// pixels x = p + P e straight from the raw plane, applies the flat field and
-// both edge blends in registers (row ends by warp shuffle), transforms the
-// line in registers and splits the two real spectra through its exchange
-// buffer.  No CTA barrier.
+// P lanes owns row pairs (row 2l real, row 2l+1 imaginary), K of them in
+// turn; the raw rows of the next pair are copied into a two-entry shared ring
+// with cp.async while the current pair is processed.  Per pair the lanes
+// read their pixels x = p + P e from the ring, apply the flat field and both
+// edge blends in registers (row ends by warp shuffle), transform the line in
+// registers and split the two real spectra through their exchange buffer.
+// No CTA barrier.
 template <int N>
 struct IngestLanes {
   static constexpr int P = N == 1024 ? 32 : 16;
 };
 constexpr int kIngestWarps = 4;
+constexpr int kIngestPairs = 4;  // row pairs per lane group
+
+template <typename T, int N>
+constexpr size_t ingest_xw_smem()
+{
+  constexpr int P = IngestLanes<N>::P, E = N / P, G = 32 / P;
+  return (size_t)kIngestWarps * G * (((P + 1) * E + 1) * sizeof(float2) + 2 * 2 * N * sizeof(T));
+}
 
 template <typename T, int N>
 __global__ void __launch_bounds__(kIngestWarps * 32, 3) k_ingest_xw(IngestArgs a, const float2* __restrict__ twr)
 {
   constexpr int P = IngestLanes<N>::P, E = N / P, G = 32 / P;
   constexpr int XB = (P + 1) * E + 1;  // >= N: also holds the transformed line
+  constexpr int RB = 2 * N * (int)sizeof(T);
   static_assert(XB >= N, "exchange buffer too small for the split");
-  __shared__ float2 xs[kIngestWarps][G][XB];
+  extern __shared__ __align__(16) unsigned char ig_dyn[];
   const int ny = a.ny, nxh = N / 2 + 1;
   const int pl = blockIdx.y;  // plane id = (d*nph + p)*nz + z
   const int z = pl % a.nz;
@@ -195,78 +214,106 @@ __global__ void __launch_bounds__(kIngestWarps * 32, 3) k_ingest_xw(IngestArgs a
   const int ph = dp % a.nphases, d = dp / a.nphases;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane / P, p = lane - g * P;
-  const int l = (blockIdx.x * kIngestWarps + warp) * G + g;  // row pair of this group
-  const int y = 2 * l;
-  const bool r0 = y < ny, r1 = y + 1 < ny;
+  const int gi = warp * G + g;
+  float2* xb = (float2*)ig_dyn + gi * XB;
+  unsigned char* rg = ig_dyn + (size_t)kIngestWarps * G * XB * sizeof(float2) + (size_t)gi * 2 * RB;
   const T* plane = (const T*)a.raw + (size_t)raw_section(d, ph, z, a.nz, a.ndirs, a.nphases, a.fastSI) * N * ny;
+  const int pairs = (ny + 1) / 2;
+  const int lbase = (blockIdx.x * kIngestWarps + warp) * G * kIngestPairs + g;  // pair of turn it: lbase + G*it
   const int napo = a.napodize;
   const bool plainbg = !a.bg && !a.slope;
-  float2 v[E];
-#pragma unroll
-  for (int e = 0; e < E; ++e) {
-    const int x = p + P * e;
-    float re = 0.f, im = 0.f;
-    if (plainbg) {
-      if (r0) re = ((float)plane[(size_t)y * N + x] - a.bgconst - a.bgextra) * 1.0f * a.inscale;
-      if (r1) im = ((float)plane[(size_t)(y + 1) * N + x] - a.bgconst - a.bgextra) * 1.0f * a.inscale;
-    } else {
-      if (r0) re = flat(plane, a, y, x);
-      if (r1) im = flat(plane, a, y + 1, x);
+  auto prefetch = [&](int it) {
+    const int l = lbase + G * it;
+    if (it < kIngestPairs && l < pairs) {
+      const int y = 2 * l;
+      const int chunks = (y + 1 < ny ? 2 : 1) * N * (int)sizeof(T) / 16;
+      const unsigned char* src = (const unsigned char*)(plane + (size_t)y * N);
+      unsigned char* dst = rg + (it & 1) * RB;
+      for (int q = p; q < chunks; q += P) {
+        const unsigned sa = (unsigned)__cvta_generic_to_shared(dst + 16 * q);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src + 16 * q) : "memory");
+      }
     }
-    v[e] = make_float2(re, im);
-  }
-  // top/bottom edge blend (apodize_x_kernel) with the unblended end rows
-  const bool e0 = r0 && (y < napo || (ny - 1 - y) < napo);
-  const bool e1 = r1 && (y + 1 < napo || (ny - 2 - y) < napo);
-  if (e0 || e1) {
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  };
+  prefetch(0);
+  for (int it = 0; it < kIngestPairs; ++it) {  // same trip count in every lane
+    prefetch(it + 1);
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    __syncwarp();
+    const int l = lbase + G * it;
+    const int y = 2 * l;
+    const bool r0 = y < ny, r1 = y + 1 < ny;
+    const T* rrow = (const T*)(rg + (it & 1) * RB);  // row y at [0, N), row y+1 at [N, 2N)
+    float2 v[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) {
       const int x = p + P * e;
-      const float diff = (flat(plane, a, ny - 1, x) - flat(plane, a, 0, x)) / 2.0f;
-      if (e0) {
-        if (y < napo) v[e].x += diff * a.apofact[y];
-        if ((ny - 1 - y) < napo) v[e].x -= diff * a.apofact[ny - 1 - y];
+      float re = 0.f, im = 0.f;
+      if (plainbg) {
+        if (r0) re = ((float)rrow[x] - a.bgconst - a.bgextra) * 1.0f * a.inscale;
+        if (r1) im = ((float)rrow[N + x] - a.bgconst - a.bgextra) * 1.0f * a.inscale;
+      } else {
+        if (r0) re = flat_v((float)rrow[x], a, y, x);
+        if (r1) im = flat_v((float)rrow[N + x], a, y + 1, x);
       }
-      if (e1) {
-        if (y + 1 < napo) v[e].y += diff * a.apofact[y + 1];
-        if ((ny - 2 - y) < napo) v[e].y -= diff * a.apofact[ny - 2 - y];
+      v[e] = make_float2(re, im);
+    }
+    __syncwarp();  // the ring entry is read before prefetch(it + 2) reuses it
+    // top/bottom edge blend (apodize_x_kernel) with the unblended end rows
+    const bool e0 = r0 && (y < napo || (ny - 1 - y) < napo);
+    const bool e1 = r1 && (y + 1 < napo || (ny - 2 - y) < napo);
+    if (e0 || e1) {
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int x = p + P * e;
+        const float diff = (flat(plane, a, ny - 1, x) - flat(plane, a, 0, x)) / 2.0f;
+        if (e0) {
+          if (y < napo) v[e].x += diff * a.apofact[y];
+          if ((ny - 1 - y) < napo) v[e].x -= diff * a.apofact[ny - 1 - y];
+        }
+        if (e1) {
+          if (y + 1 < napo) v[e].y += diff * a.apofact[y + 1];
+          if ((ny - 2 - y) < napo) v[e].y -= diff * a.apofact[ny - 2 - y];
+        }
       }
     }
-  }
-  // left/right edge blend (apodize_y_kernel) from the blended row ends
-  if (napo > 0) {
-    const int gb = g * P;
-    const float2 first = make_float2(__shfl_sync(0xffffffffu, v[0].x, gb), __shfl_sync(0xffffffffu, v[0].y, gb));
-    const float2 last = make_float2(__shfl_sync(0xffffffffu, v[E - 1].x, gb + P - 1),
-                                    __shfl_sync(0xffffffffu, v[E - 1].y, gb + P - 1));
-    const float dx = (last.x - first.x) / 2.0f, dy = (last.y - first.y) / 2.0f;
+    // left/right edge blend (apodize_y_kernel) from the blended row ends
+    if (napo > 0) {
+      const int gb = g * P;
+      const float2 first = make_float2(__shfl_sync(0xffffffffu, v[0].x, gb), __shfl_sync(0xffffffffu, v[0].y, gb));
+      const float2 last = make_float2(__shfl_sync(0xffffffffu, v[E - 1].x, gb + P - 1),
+                                      __shfl_sync(0xffffffffu, v[E - 1].y, gb + P - 1));
+      const float dx = (last.x - first.x) / 2.0f, dy = (last.y - first.y) / 2.0f;
 #pragma unroll
-    for (int e = 0; e < E; ++e) {
-      const int x = p + P * e;
-      if (x < napo) {
-        v[e].x += dx * a.apofact[x];
-        v[e].y += dy * a.apofact[x];
-      } else if (x >= N - napo) {
-        v[e].x -= dx * a.apofact[N - 1 - x];
-        v[e].y -= dy * a.apofact[N - 1 - x];
+      for (int e = 0; e < E; ++e) {
+        const int x = p + P * e;
+        if (x < napo) {
+          v[e].x += dx * a.apofact[x];
+          v[e].y += dy * a.apofact[x];
+        } else if (x >= N - napo) {
+          v[e].x -= dx * a.apofact[N - 1 - x];
+          v[e].y -= dy * a.apofact[N - 1 - x];
+        }
       }
     }
-  }
-  float2* xb = xs[warp][g];
-  reg_line<N, P, -1>(v, p, xb, twr, true);
-  // split the two real transforms: X[k] and X[N-k] live in different lanes
+    reg_line<N, P, -1>(v, p, xb, twr, true);
+    // split the two real transforms: X[k] and X[N-k] live in different lanes
 #pragma unroll
-  for (int m = 0; m < E / P; ++m)
+    for (int m = 0; m < E / P; ++m)
 #pragma unroll
-    for (int k2 = 0; k2 < P; ++k2) xb[p + P * m + E * k2] = v[m * P + k2];
-  __syncwarp();
-  float2* dst = a.spec + (size_t)pl * ny * nxh;
-  for (int k = p; k < nxh; k += P) {
-    const float2 zk = xb[k], zn = xb[(N - k) % N];
-    const float2 A = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
-    const float2 B = make_float2(0.5f * (zk.y + zn.y), -0.5f * (zk.x - zn.x));
-    if (r0) dst[(size_t)y * nxh + k] = A;
-    if (r1) dst[(size_t)(y + 1) * nxh + k] = B;
+      for (int k2 = 0; k2 < P; ++k2) xb[p + P * m + E * k2] = v[m * P + k2];
+    __syncwarp();
+    float2* dst = a.spec + (size_t)pl * ny * nxh;
+    for (int k = p; k < nxh; k += P) {
+      const float2 zk = xb[k], zn = xb[(N - k) % N];
+      const float2 A = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+      const float2 B = make_float2(0.5f * (zk.y + zn.y), -0.5f * (zk.x - zn.x));
+      if (r0) dst[(size_t)y * nxh + k] = A;
+      if (r1) dst[(size_t)(y + 1) * nxh + k] = B;
+    }
+    // the next turn's reg_line rewrites xb only after the wait + __syncwarp
+    // at its top, which every lane reaches after finishing these reads
   }
 }
 
@@ -373,9 +420,17 @@ int launch_ingest(const IngestArgs& a, cudaStream_t s, long long* launches)
   auto go_w = [&]<int N>() {
     constexpr int G = 32 / IngestLanes<N>::P;
     const int pairs = (a.ny + 1) / 2;
-    dim3 gw((pairs + kIngestWarps * G - 1) / (kIngestWarps * G), nplanes);
-    if (a.raw_is_u16) k_ingest_xw<uint16_t, N><<<gw, kIngestWarps * 32, 0, s>>>(a, px.twr);
-    else k_ingest_xw<float, N><<<gw, kIngestWarps * 32, 0, s>>>(a, px.twr);
+    const int per_cta = kIngestWarps * G * kIngestPairs;
+    dim3 gw((pairs + per_cta - 1) / per_cta, nplanes);
+    if (a.raw_is_u16) {
+      constexpr size_t bytes = ingest_xw_smem<uint16_t, N>();
+      cudaFuncSetAttribute(k_ingest_xw<uint16_t, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+      k_ingest_xw<uint16_t, N><<<gw, kIngestWarps * 32, bytes, s>>>(a, px.twr);
+    } else {
+      constexpr size_t bytes = ingest_xw_smem<float, N>();
+      cudaFuncSetAttribute(k_ingest_xw<float, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+      k_ingest_xw<float, N><<<gw, kIngestWarps * 32, bytes, s>>>(a, px.twr);
+    }
   };
   if (a.nx == 512) go_w.template operator()<512>();
   else if (a.nx == 1024) go_w.template operator()<1024>();

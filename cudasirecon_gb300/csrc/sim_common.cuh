@@ -86,6 +86,33 @@ __device__ __forceinline__ float2 otf_lookup_rk(const float2* __restrict__ otf, 
   return r;
 }
 
+// bilinear RA-OTF lookup at radius kr (otf_lookup's arithmetic with
+// krindex = kr * (1/dkrotf))
+// CLAMP = false only where the caller has shown that every lookup stays in
+// the table (krindex + 1 < nxotf).
+template <bool CLAMP = true>
+__device__ __forceinline__ float2 otf_lookup_rr(const float2* __restrict__ otf, const OTFView& v, float krindex,
+                                               const OtfKz& z)
+{
+  int ir = (int)floorf(krindex);
+  float ar = krindex - ir;
+  int i00 = ir * v.nzotf + z.iz, i01 = ir * v.nzotf + z.izp;
+  int i10 = i00 + v.nzotf, i11 = i01 + v.nzotf;
+  if (CLAMP) {
+    const int last = v.nxotf * v.nzotf - 1;
+    i00 = min(max(i00, 0), last);
+    i01 = min(max(i01, 0), last);
+    i10 = min(max(i10, 0), last);
+    i11 = min(max(i11, 0), last);
+  }
+  float2 a = __ldg(otf + i00), b = __ldg(otf + i01), c = __ldg(otf + i10), d = __ldg(otf + i11);
+  const float az = z.az;
+  float2 r;
+  r.x = (1 - ar) * (a.x * (1 - az) + b.x * az) + ar * (c.x * (1 - az) + d.x * az);
+  r.y = (1 - ar) * (a.y * (1 - az) + b.y * az) + ar * (c.y * (1 - az) + d.y * az);
+  return r;
+}
+
 __device__ __forceinline__ float cmag2(float2 a) { return a.x * a.x + a.y * a.y; }
 
 // Block-wide sum of a double (all threads must call).  Result valid in thread 0.
