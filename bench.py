@@ -383,13 +383,144 @@ def run_reference(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
     }
 
 
+# Serving mix: 4 acquisition configurations (two 3D, two 2D, different line
+# spacings and pattern angles) with sizes drawn from the time-series and
+# uneven-batch shapes; every request is a standalone volume (k0 fitted).
+SERVING_CONFIGS = [
+    dict(twod=False, ls=0.2035, angles=(-0.8043, -1.8555, 0.2388)),
+    dict(twod=False, ls=0.21, angles=(-0.6, -1.647, 0.447)),
+    dict(twod=True, ls=0.195, angles=(-0.7, -1.747, 0.347)),
+    dict(twod=True, ls=0.22, angles=(-0.9, -1.947, 0.147)),
+]
+SERVING_SIZES = {False: [(256, 256, 32), (512, 512, 32)], True: [(512, 512, 1), (1024, 1024, 1)]}
+
+
+def serving_requests(seed=8):
+    """One seeded raw volume per (configuration, size) type.  2D configs use
+    wiener = 2^-11 (the reference's flag-byte reading of wiener = 0.001 would
+    drop every 2D overlap)."""
+    from cudasirecon_gb300 import synthetic as syn
+    types = []
+    cache = os.environ.get("SIRECON_BENCH_CACHE")
+    for ci, c in enumerate(SERVING_CONFIGS):
+        o = syn.Optics(ls=c["ls"], angles=c["angles"], nphases=3 if c["twod"] else 5)
+        otf = syn.ra_otf(o, nx_psf=128, nz_psf=64, norders=2 if c["twod"] else 3, twod=c["twod"])
+        cfg = syn.config_text(o, twod=c["twod"], extra={"wiener": 0.00048828125} if c["twod"] else None)
+        for (nx, ny, nz) in SERVING_SIZES[c["twod"]]:
+            cp = os.path.join(cache, f"serve_{ci}_{nx}x{ny}x{nz}_{seed}.npy") if cache else None
+            if cp and os.path.exists(cp):
+                raw = np.load(cp)
+            else:
+                raw = syn.simulate(nx, ny, nz, o, seed=seed + ci, n_filaments=30).raw
+                if cp:
+                    os.makedirs(cache, exist_ok=True)
+                    np.save(cp, raw)
+            types.append(dict(config=ci, cfg=cfg, otf=otf, raw=np.ascontiguousarray(raw), nx=nx, ny=ny, nz=nz,
+                              outvox=4 * nx * ny * nz))
+    return types
+
+
+def run_serving(args):
+    """Plain one-at-a-time vs served (SRX_server*, Poisson arrivals)."""
+    import threading
+    import cudasirecon_gb300 as sr
+    sr.load_library()
+    types = serving_requests()
+    rng = np.random.default_rng(8)
+    workers = int(os.environ.get("SIRECON_SERVE_WORKERS", "4"))
+    # ---- plain: one handle per type, requests one after another
+    hs = {}
+    for i, t in enumerate(types):
+        r = sr.Reconstructor(t["nx"], t["ny"], t["raw"].shape[0], t["cfg"], t["otf"])
+        hs[i] = (r, np.empty(r.out_shape, np.float32))
+
+    def plain(i):
+        r, out = hs[i]
+        r.set_raw(types[i]["raw"])
+        r.load_and_rescale(0, 0)
+        r.set_cur_time(0)
+        r.process()
+        r.result(out)
+
+    for i in range(len(types)):
+        plain(i)
+    seq = rng.integers(0, len(types), 200)
+    t0 = time.perf_counter()
+    lat = []
+    for i in seq:
+        ts = time.perf_counter()
+        plain(int(i))
+        lat.append((time.perf_counter() - ts) * 1e3)
+    plain_s = time.perf_counter() - t0
+    plain_vox = sum(types[int(i)]["outvox"] for i in seq)
+    for r, _ in hs.values():
+        r.close()
+    plain_line = {"requests": len(seq), "req_per_s": round(len(seq) / plain_s, 1),
+                  "mvox_per_s": round(plain_vox / plain_s / 1e6, 1),
+                  "p50_ms": round(float(np.percentile(lat, 50)), 2), "p99_ms": round(float(np.percentile(lat, 99)), 2)}
+    # ---- served
+    srv = sr.Server(workers=workers, hbm_budget=150e9)
+    cid = {}
+    for t in types:
+        if t["config"] not in cid:
+            cid[t["config"]] = srv.add_config(t["cfg"], t["otf"])
+    shapes = [(t["nz"], 2 * t["ny"], 2 * t["nx"]) for t in types]
+    warm = [np.empty(shapes[i], np.float32) for _ in range(workers) for i in range(len(types))]
+    tick = [srv.submit(cid[types[i % len(types)]["config"]], types[i % len(types)]["raw"], warm[i])
+            for i in range(len(warm))]
+    for k in tick:
+        srv.wait(k)
+    served = []
+    dur = float(os.environ.get("SIRECON_SERVE_SECONDS", "3"))
+    for lam in (5, 20, 50, 100, 200):
+        n = max(10, int(lam * dur))
+        arrivals = np.cumsum(rng.exponential(1.0 / lam, n))
+        kinds = rng.integers(0, len(types), n)
+        bufs = [np.empty(shapes[int(k)], np.float32) for k in kinds]
+        tickets = [None] * n
+        start = time.perf_counter()
+
+        def submitter():
+            for j in range(n):
+                d = start + arrivals[j] - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                t = types[int(kinds[j])]
+                tickets[j] = srv.submit(cid[t["config"]], t["raw"], bufs[j])
+
+        th = threading.Thread(target=submitter)
+        th.start()
+        lats = []
+        for j in range(n):
+            while tickets[j] is None:
+                time.sleep(0.0005)
+            lats.append(srv.wait(tickets[j]))
+        th.join()
+        wall = time.perf_counter() - start
+        vox = sum(types[int(k)]["outvox"] for k in kinds)
+        served.append({"lambda_req_s": lam, "requests": n, "p50_ms": round(float(np.percentile(lats, 50)), 2),
+                       "p95_ms": round(float(np.percentile(lats, 95)), 2),
+                       "p99_ms": round(float(np.percentile(lats, 99)), 2),
+                       "req_per_s": round(n / wall, 1), "mvox_per_s": round(vox / wall / 1e6, 1)})
+    dev = srv.device_bytes()
+    srv.close()
+    return {"metric": "Served recon latency (p50/p95/p99) and throughput vs plain one-at-a-time",
+            "unit": "ms / Mvoxels/s", "impl": "gb300", "n_gpus": 1, "data": "synthetic",
+            "config": {"workload": "serving",
+                       "types": [f"{'2D' if SERVING_CONFIGS[t['config']]['twod'] else '3D'} cfg{t['config']} "
+                                 f"{t['nx']}x{t['ny']}x{t['nz']}" for t in types],
+                       "workers": workers, "hbm_budget_bytes": 150e9, "handles_bytes": dev,
+                       "request": "standalone volume, k0 searched", "arrivals": "Poisson, seeded"},
+            "plain": plain_line, "served": served}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=list(WORKLOADS), default="timeseries_512x512x48")
+    ap.add_argument("--workload", choices=list(WORKLOADS) + ["serving"], default="timeseries_512x512x48")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
@@ -398,6 +529,12 @@ def main():
         return
     if args.impl == "reference":
         world, dist = 1, None
+    if args.workload == "serving":
+        if rank == 0 and args.impl != "reference":
+            print(json.dumps(run_serving(args)), flush=True)
+        elif rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the serving workload has no reference arm"}))
+        return
     nx, ny, nz, _ = WORKLOADS[args.workload]
     vols, otf, cfg = make_workload(nx, ny, nz, 2)
     outvox = 4 * nx * ny * nz

@@ -82,6 +82,17 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.SRX_unpinHost.argtypes = [vp]
     lib.SRX_processSeries.restype = ip
     lib.SRX_processSeries.argtypes = [vp, C.POINTER(vp), ip, C.POINTER(vp), ip, ip]
+    lib.SRX_serverCreate.restype = vp
+    lib.SRX_serverCreate.argtypes = [ip, C.c_size_t]
+    lib.SRX_serverAddConfig.restype = ip
+    lib.SRX_serverAddConfig.argtypes = [vp, C.c_char_p]
+    lib.SRX_serverSubmit.restype = C.c_longlong
+    lib.SRX_serverSubmit.argtypes = [vp, ip, ip, ip, ip, vp, ip, vp]
+    lib.SRX_serverWait.restype = ip
+    lib.SRX_serverWait.argtypes = [vp, C.c_longlong, C.POINTER(C.c_double)]
+    lib.SRX_serverDeviceBytes.restype = C.c_size_t
+    lib.SRX_serverDeviceBytes.argtypes = [vp]
+    lib.SRX_serverDestroy.argtypes = [vp]
     lib.SRX_makeOTF.restype = ip
     lib.SRX_makeOTF.argtypes = [fp, ip, ip, ip, ip, C.POINTER(C.c_char_p), fp, C.c_size_t, C.POINTER(C.c_int)]
     lib.SRX_makeotfMain.restype = ip
@@ -378,3 +389,69 @@ def makeotf_main(argv: list[str]) -> None:
     arr = (C.c_char_p * len(full))(*[a.encode() for a in full])
     if lib.SRX_makeotfMain(len(full), arr) != 0:
         raise SIReconError(_err(lib))
+
+
+class Server:
+    """SRX_server*: volumes of several shapes and acquisition configurations
+    served concurrently by worker threads over pooled handles, within a
+    device-memory budget.  Each request is processed as a time-0 volume."""
+
+    def __init__(self, workers: int = 4, hbm_budget: float = 150e9):
+        self.lib = load_library()
+        self._tmp = tempfile.TemporaryDirectory(prefix="sirecon_srv_")
+        self.lib.SR_clearError()
+        self.h = self.lib.SRX_serverCreate(int(workers), int(hbm_budget))
+        if not self.h:
+            raise SIReconError(_err(self.lib))
+        self._keep = {}
+        self._n = 0
+
+    def add_config(self, config: str, otf_pages: np.ndarray) -> int:
+        """config: reference key=value text; otf_pages: the OTF TIFF's pages."""
+        self._n += 1
+        otf = os.path.join(self._tmp.name, f"otf{self._n}.tif")
+        write_tiff_float(otf, otf_pages)
+        cfg = os.path.join(self._tmp.name, f"config{self._n}.txt")
+        with open(cfg, "w") as f:
+            f.write(config.rstrip("\n") + f"\notf-file={otf}\n")
+        cid = self.lib.SRX_serverAddConfig(self.h, cfg.encode())
+        if cid < 0:
+            raise SIReconError(_err(self.lib))
+        return cid
+
+    def submit(self, config: int, raw: np.ndarray, out: np.ndarray) -> int:
+        """raw: [nimages][ny][nx] uint16 or float32 (C-contiguous); out: float32
+        array of the result size.  Both must stay alive until wait()."""
+        if not raw.flags.c_contiguous or not out.flags.c_contiguous or out.dtype != np.float32:
+            raise ValueError("raw and out must be C-contiguous, out float32")
+        nimg, ny, nx = raw.shape
+        t = self.lib.SRX_serverSubmit(self.h, config, nx, ny, nimg, raw.ctypes.data, int(raw.dtype == np.uint16),
+                                      out.ctypes.data)
+        if t < 0:
+            raise SIReconError(_err(self.lib))
+        self._keep[t] = (raw, out)
+        return int(t)
+
+    def wait(self, ticket: int) -> float:
+        """Blocks until the request is done; returns its latency in ms."""
+        lat = C.c_double(0.0)
+        rc = self.lib.SRX_serverWait(self.h, ticket, C.byref(lat))
+        self._keep.pop(ticket, None)
+        if rc != 0:
+            raise SIReconError(_err(self.lib))
+        return lat.value
+
+    def device_bytes(self) -> int:
+        return int(self.lib.SRX_serverDeviceBytes(self.h))
+
+    def close(self):
+        if self.h:
+            self.lib.SRX_serverDestroy(self.h)
+            self.h = None
+        self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

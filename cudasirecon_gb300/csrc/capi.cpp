@@ -11,6 +11,7 @@
 #include "cudasirecon.h"
 #include "makeotf.h"
 #include "reconstructor.h"
+#include "server.h"
 
 namespace simrecon {
 int makeotf_main(int argc, const char* const* argv, std::string* err);
@@ -271,6 +272,62 @@ int SRX_makeotfMain(int argc, char** argv)
     if (rc != 0) g_last_error = err;
   });
   return rc;
+}
+
+SRX_Server* SRX_serverCreate(int workers, size_t hbm_budget_bytes)
+{
+  SRX_Server* s = nullptr;
+  guarded([&] { s = (SRX_Server*)new simrecon::ReconServer(workers, hbm_budget_bytes); });
+  return s;
+}
+
+int SRX_serverAddConfig(SRX_Server* s, const char* config_path)
+{
+  int id = -1;
+  if (!s || !config_path) {
+    g_last_error = "SRX_serverAddConfig: invalid arguments";
+    return -1;
+  }
+  guarded([&] { id = ((simrecon::ReconServer*)s)->add_config(config_path); });
+  return id;
+}
+
+long long SRX_serverSubmit(SRX_Server* s, int config, int nx, int ny, int nimages, const void* raw, int raw_is_u16,
+                           float* out)
+{
+  long long t = -1;
+  if (!s) {
+    g_last_error = "SRX_serverSubmit: null server";
+    return -1;
+  }
+  guarded([&] {
+    std::string err;
+    t = ((simrecon::ReconServer*)s)->submit(config, nx, ny, nimages, raw, raw_is_u16 != 0, out, &err);
+    if (t < 0) g_last_error = err;
+  });
+  return t;
+}
+
+int SRX_serverWait(SRX_Server* s, long long ticket, double* latency_ms)
+{
+  int rc = -1;
+  if (!s) {
+    g_last_error = "SRX_serverWait: null server";
+    return -1;
+  }
+  guarded([&] {
+    std::string err;
+    rc = ((simrecon::ReconServer*)s)->wait(ticket, latency_ms, &err);
+    if (rc != 0) g_last_error = err;
+  });
+  return rc;
+}
+
+size_t SRX_serverDeviceBytes(SRX_Server* s) { return s ? ((simrecon::ReconServer*)s)->device_bytes_in_use() : 0; }
+
+void SRX_serverDestroy(SRX_Server* s)
+{
+  guarded([&] { delete (simrecon::ReconServer*)s; });
 }
 
 int SRX_pinHost(void* ptr, size_t bytes)

@@ -103,6 +103,20 @@ bool reg_fft_site_enabled(FftSite site, int n)
   }
 }
 
+void allow_dynamic_smem(const void* func, size_t bytes)
+{
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, size_t> cur;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  size_t& have = cur[{dev, func}];
+  if (bytes > have) {
+    if (cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess)
+      have = bytes;
+  }
+}
+
 bool fft_length_ok(int n)
 {
   std::vector<int> r;

@@ -774,7 +774,7 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
     if (colfft_r1(a.Y)) {
       auto go = [&]<int YN>() {
         const size_t bytes = ColFft<YN, colfft_r1(YN), 8>::kSmemElems * sizeof(float2);
-        cudaFuncSetAttribute(k_asm_y4<YN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        allow_dynamic_smem((const void*)k_asm_y4<YN>, bytes);
         k_asm_y4<YN><<<dim3((nx + 7) / 8, nsl), kThreads, bytes, s>>>(ay, d_slots + first, py.tw);
       };
       if (a.Y == 1024) go.template operator()<1024>();
@@ -782,7 +782,7 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
       else go.template operator()<256>();
     } else {
       dispatch_fft_len(kSiteAsmY, a.Y, [&]<int NF>() {
-        cudaFuncSetAttribute(k_asm_y<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
+        allow_dynamic_smem((const void*)k_asm_y<NF>, smy);
         k_asm_y<NF><<<dim3((nx + Wy - 1) / Wy, nsl), kThreads, smy, s>>>(ay, d_slots + first, py, Wy);
       });
     }
@@ -800,7 +800,7 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
       constexpr int G = 32 / XwLanes<XN>::P;
       const int rows_per_cta = kXwWarps * G;
       constexpr size_t bytes = xw_smem_bytes<XN>();
-      cudaFuncSetAttribute(k_asm_xw<XN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+      allow_dynamic_smem((const void*)k_asm_xw<XN>, bytes);
       k_asm_xw<XN><<<dim3((a.Y + rows_per_cta - 1) / rows_per_cta, (unsigned)(pj - pi)), kXwWarps * 32, bytes,
                      s>>>(ax, d_p0 + pi, d_pn + pi, d_slots, d_pz + pi, px.twr);
     };
@@ -810,7 +810,7 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
     else if (a.X == 256 && a.nx == 128) launch_xw.template operator()<256>();
     else
       dispatch_fft_len(kSiteAsmX, a.X, [&]<int NF>() {
-        cudaFuncSetAttribute(k_asm_x<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+        allow_dynamic_smem((const void*)k_asm_x<NF>, smx);
         k_asm_x<NF><<<dim3(a.Y, (unsigned)(pj - pi)), kThreads, smx, s>>>(ax, d_p0 + pi, d_pn + pi, d_slots,
                                                                          d_pz + pi, px, xlines);
       });
@@ -826,7 +826,7 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
   if (zr1 == 2 || zr1 == 3 || zr1 == 4 || zr1 == 5 || zr1 == 6 || zr1 == 8) {
     auto go = [&]<int R1>() {
       const size_t bytes = (size_t)R1 * (16 * 64 + 8) * sizeof(float2);
-      cudaFuncSetAttribute(k_asm_z4<R1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+      allow_dynamic_smem((const void*)k_asm_z4<R1>, bytes);
       k_asm_z4<R1><<<dim3((a.X + 63) / 64, a.Y), kThreads, bytes, s>>>(a, d_zact, pz.tw);
     };
     switch (zr1) {
@@ -839,7 +839,7 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
     }
   } else {
     dispatch_fft_len(kSiteAsmZ, a.Z, [&]<int NF>() {
-      cudaFuncSetAttribute(k_asm_z<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
+      allow_dynamic_smem((const void*)k_asm_z<NF>, smz);
       k_asm_z<NF><<<dim3((a.X + Wz - 1) / Wz, a.Y), kThreads, smz, s>>>(a, d_zact, pz, Wz);
     });
   }

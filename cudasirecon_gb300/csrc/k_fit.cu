@@ -594,7 +594,7 @@ int launch_overlaps(OverlapArgs& a, cudaStream_t s, long long* launches)
   else if (a.nx == 256) launch_w.template operator()<256>();
   else
     dispatch_fft_len(kSiteOvlX, a.nx, [&]<int NF>() {
-      cudaFuncSetAttribute(k_ovl_build_x<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
+      allow_dynamic_smem((const void*)k_ovl_build_x<NF>, sm1);
       k_ovl_build_x<NF><<<nb1, kThreads, sm1, s>>>(a, px, rows, ldl);
     });
   if (kt) kt->end("k_ovl_build_x", s, ovlb + (a.order1 == 0 ? 3 : 4) * bandplanes);
@@ -619,14 +619,14 @@ int launch_overlaps(OverlapArgs& a, cudaStream_t s, long long* launches)
   if (kt) kt->begin(s);
   auto go4 = [&]<int N, int R1>() {
     const size_t bytes = 2 * ColFft<N, R1, 8>::kSmemElems * sizeof(float2);
-    cudaFuncSetAttribute(k_ovl_y4<N, R1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    allow_dynamic_smem((const void*)k_ovl_y4<N, R1>, bytes);
     k_ovl_y4<N, R1><<<dim3(tiles, groups), kThreads, bytes, s>>>(a, py.tw, ppg);
   };
   if (a.ny == 512) go4.template operator()<512, 32>();
   else if (a.ny == 256) go4.template operator()<256, 16>();
   else
     dispatch_fft_len(kSiteOvlY, a.ny, [&]<int NF>() {
-      cudaFuncSetAttribute(k_ovl_y_accum<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+      allow_dynamic_smem((const void*)k_ovl_y_accum<NF>, sm2);
       k_ovl_y_accum<NF><<<dim3(tiles, groups), threads, sm2, s>>>(a, py, W, ppg, xoff);
     });
   if (kt) kt->end("k_ovl_y_accum", s, ovlb + (double)groups * a.ny * a.nx * sizeof(float2));
@@ -644,13 +644,13 @@ int launch_crosscorr_peak(const float2* pmap, float2* cc, int nx, int ny, float*
   int nl = std::max(1, std::min(ny, kMaxElems / nx));
   size_t sm1 = fft_stage_smem(nx, nl, nl * (nx + 1), kThreads);
   dispatch_fft_len(kSiteCorrRows, nx, [&]<int NF>() {
-    cudaFuncSetAttribute(k_fft_rows<-1, true, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
+    allow_dynamic_smem((const void*)k_fft_rows<-1, true, NF>, sm1);
     k_fft_rows<-1, true, NF><<<(ny + nl - 1) / nl, kThreads, sm1, s>>>(pmap, cc, nx, ny, px, nl);
   });
   int W = std::max(1, std::min(32, kMaxElems / ny));
   size_t sm2 = fft_stage_smem(ny, W, (W + 1) * ny, kThreads);
   dispatch_fft_len(kSiteCorrCols, ny, [&]<int NF>() {
-    cudaFuncSetAttribute(k_fft_cols2<-1, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+    allow_dynamic_smem((const void*)k_fft_cols2<-1, NF>, sm2);
     k_fft_cols2<-1, NF><<<(nx + W - 1) / W, kThreads, sm2, s>>>(cc, ny, nx, py, W);
   });
   int nb = 256;

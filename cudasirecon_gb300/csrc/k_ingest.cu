@@ -424,11 +424,11 @@ int launch_ingest(const IngestArgs& a, cudaStream_t s, long long* launches)
     dim3 gw((pairs + per_cta - 1) / per_cta, nplanes);
     if (a.raw_is_u16) {
       constexpr size_t bytes = ingest_xw_smem<uint16_t, N>();
-      cudaFuncSetAttribute(k_ingest_xw<uint16_t, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+      allow_dynamic_smem((const void*)k_ingest_xw<uint16_t, N>, bytes);
       k_ingest_xw<uint16_t, N><<<gw, kIngestWarps * 32, bytes, s>>>(a, px.twr);
     } else {
       constexpr size_t bytes = ingest_xw_smem<float, N>();
-      cudaFuncSetAttribute(k_ingest_xw<float, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+      allow_dynamic_smem((const void*)k_ingest_xw<float, N>, bytes);
       k_ingest_xw<float, N><<<gw, kIngestWarps * 32, bytes, s>>>(a, px.twr);
     }
   };
@@ -439,18 +439,18 @@ int launch_ingest(const IngestArgs& a, cudaStream_t s, long long* launches)
   dispatch_fft_len(kSiteIngestX, a.nx, [&]<int NF>() {
     if (a.raw_is_u16) {
       if (a.nx % 8 == 0) {
-        cudaFuncSetAttribute(k_ingest_x<uint16_t, 8, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+        allow_dynamic_smem((const void*)k_ingest_x<uint16_t, 8, NF>, smx);
         k_ingest_x<uint16_t, 8, NF><<<gx, kThreads, smx, s>>>(a, px, nl, ldl);
       } else {
-        cudaFuncSetAttribute(k_ingest_x<uint16_t, 1, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+        allow_dynamic_smem((const void*)k_ingest_x<uint16_t, 1, 0>, smx);
         k_ingest_x<uint16_t, 1, 0><<<gx, kThreads, smx, s>>>(a, px, nl, ldl);
       }
     } else {
       if (a.nx % 4 == 0) {
-        cudaFuncSetAttribute(k_ingest_x<float, 4, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+        allow_dynamic_smem((const void*)k_ingest_x<float, 4, NF>, smx);
         k_ingest_x<float, 4, NF><<<gx, kThreads, smx, s>>>(a, px, nl, ldl);
       } else {
-        cudaFuncSetAttribute(k_ingest_x<float, 1, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+        allow_dynamic_smem((const void*)k_ingest_x<float, 1, 0>, smx);
         k_ingest_x<float, 1, 0><<<gx, kThreads, smx, s>>>(a, px, nl, ldl);
       }
     }
@@ -464,7 +464,7 @@ int launch_ingest(const IngestArgs& a, cudaStream_t s, long long* launches)
     dim3 g4((nxh + 7) / 8, nplanes);
     auto go = [&]<int N>() {
       const size_t bytes = ColFft<N, colfft_r1(N), 8>::kSmemElems * sizeof(float2);
-      cudaFuncSetAttribute(k_fft_cols_4s<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+      allow_dynamic_smem((const void*)k_fft_cols_4s<N>, bytes);
       k_fft_cols_4s<N><<<g4, kThreads, bytes, s>>>(a.spec, nxh, py.tw);
     };
     if (a.ny == 512) go.template operator()<512>();
@@ -472,7 +472,7 @@ int launch_ingest(const IngestArgs& a, cudaStream_t s, long long* launches)
     else go.template operator()<256>();
   } else {
     dispatch_fft_len(kSiteIngestY, a.ny, [&]<int NF>() {
-      cudaFuncSetAttribute(k_fft_cols<-1, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smy);
+      allow_dynamic_smem((const void*)k_fft_cols<-1, NF>, smy);
       k_fft_cols<-1, NF><<<gy, kThreads, smy, s>>>(a.spec, a.ny, nxh, py, W);
     });
   }
@@ -578,7 +578,7 @@ int launch_separate(float2* spec, const float* scale, const float* sepmat, int n
     dim3 g4((nxh + 15) / 16, ny, ndirs);
     auto go = [&]<int R1>() {
       const size_t bytes = (size_t)nphases * R1 * (16 * 16 + 8) * sizeof(float2);
-      cudaFuncSetAttribute(k_separate4<R1, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+      allow_dynamic_smem((const void*)k_separate4<R1, 5>, bytes);
       k_separate4<R1, 5><<<g4, kThreads, bytes, s>>>(spec, scale, sepmat, ny, nxh, pz.tw);
     };
     switch (r1) {
@@ -591,7 +591,7 @@ int launch_separate(float2* spec, const float* scale, const float* sepmat, int n
     }
   } else {
     dispatch_fft_len(kSiteSeparateZ, nz, [&]<int NF>() {
-      cudaFuncSetAttribute(k_separate<NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      allow_dynamic_smem((const void*)k_separate<NF>, sm);
       k_separate<NF><<<g, kThreads, sm, s>>>(spec, scale, sepmat, ny, nxh, nz, nphases, pz, W);
     });
   }

@@ -46,10 +46,10 @@ int launch_fft_selftest(float2* data, int n, int nlines, int inverse, int column
   size_t sm = selftest_smem(n, nl, columns);
   dispatch_fft_len(kSiteSelfTest, n, [&]<int NF>() {
     if (inverse) {
-      cudaFuncSetAttribute(k_fft_selftest<+1, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      allow_dynamic_smem((const void*)k_fft_selftest<+1, NF>, sm);
       k_fft_selftest<+1, NF><<<nlines / nl, kFftThreads, sm, s>>>(data, n, nl, columns, p);
     } else {
-      cudaFuncSetAttribute(k_fft_selftest<-1, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      allow_dynamic_smem((const void*)k_fft_selftest<-1, NF>, sm);
       k_fft_selftest<-1, NF><<<nlines / nl, kFftThreads, sm, s>>>(data, n, nl, columns, p);
     }
   });
@@ -184,10 +184,10 @@ extern "C" int SRX_fftLinesNoAlloc(const float* in, float* out, int n, int nline
   size_t sm = selftest_smem(n, nl, columns);
   dispatch_fft_len(kSiteSelfTest, n, [&]<int NF>() {
     if (inverse) {
-      cudaFuncSetAttribute(k_fft_selftest<+1, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      allow_dynamic_smem((const void*)k_fft_selftest<+1, NF>, sm);
       k_fft_selftest<+1, NF><<<nlines / nl, kFftThreads, sm>>>(data, n, nl, columns, p);
     } else {
-      cudaFuncSetAttribute(k_fft_selftest<-1, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      allow_dynamic_smem((const void*)k_fft_selftest<-1, NF>, sm);
       k_fft_selftest<-1, NF><<<nlines / nl, kFftThreads, sm>>>(data, n, nl, columns, p);
     }
   });

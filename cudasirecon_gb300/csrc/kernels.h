@@ -44,6 +44,13 @@ struct IngestArgs {
   float2* spec;          // [ndirs*nphases*nz][ny][nx/2+1]
 };
 // flat-field + apodize + 2D R2C FFT of every raw plane into spec
+// Allow `func` to be launched with `bytes` of dynamic shared memory.  The
+// limit is per kernel and device and is only ever raised: host threads that
+// launch the same kernel with different sizes (handles of different shapes
+// used concurrently) must not lower it between another thread's set and its
+// launch.
+void allow_dynamic_smem(const void* func, size_t bytes);
+
 int launch_ingest(const IngestArgs& a, cudaStream_t s, long long* launches);
 
 // Bleach-correction ratios from the plane sums (DC terms of spec):

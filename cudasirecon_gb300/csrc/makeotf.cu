@@ -546,7 +546,7 @@ __global__ void __launch_bounds__(1024) k_mo_finish(float2* avg, FinishArgs a, f
 template <typename K>
 void set_smem(K kernel, size_t bytes)
 {
-  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  allow_dynamic_smem((const void*)kernel, bytes);
 }
 
 bool mo_fail(std::string* err, const std::string& m)

@@ -54,6 +54,7 @@ class SIM_Reconstructor {
   void reset_profile();
   long long launches() const { return launches_; }
   size_t out_elems() const { return (size_t)X_ * Y_ * Z_; }
+  size_t device_bytes() const { return arena_bytes_; }  // the handle's device arena
 
   simrecon::Options opt;  // ReconParams + ImageParams live here (references handed out)
 

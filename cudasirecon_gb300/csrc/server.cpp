@@ -1,0 +1,205 @@
+// ReconServer: a FIFO of volume requests served by worker threads, each
+// running the plain per-volume flow (setRaw -> loadAndRescaleImage(0) ->
+// processOneVolume -> getResult) on a handle it holds for the request.
+//
+// Handles are pooled per (configuration, nx, ny, nimages): a worker reuses an
+// idle handle of the request's shape, else creates one.  Device memory is
+// bounded by the budget: after a handle is created, idle handles are deleted
+// least recently used first until the handles in use fit (at most the newest
+// handle's size above the budget while every other handle is busy).  If the
+// creation itself runs out of device memory, all idle handles are deleted and
+// the creation is tried once more.
+#include "server.h"
+
+#include <chrono>
+#include <stdexcept>
+
+#include "reconstructor.h"
+
+namespace simrecon {
+
+namespace {
+double now_s()
+{
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+}  // namespace
+
+ReconServer::ReconServer(int workers, size_t hbm_budget) : budget_(hbm_budget)
+{
+  if (workers < 1) workers = 1;
+  for (int i = 0; i < workers; ++i) workers_.emplace_back([this] { worker_loop(); });
+}
+
+ReconServer::~ReconServer()
+{
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    stop_ = true;
+  }
+  cv_work_.notify_all();
+  for (auto& t : workers_) t.join();
+  for (auto& h : handles_) delete h->sr;
+}
+
+int ReconServer::add_config(const std::string& config_path)
+{
+  std::lock_guard<std::mutex> lk(mu_);
+  configs_.push_back(config_path);
+  return (int)configs_.size() - 1;
+}
+
+long long ReconServer::submit(int config, int nx, int ny, int nimages, const void* raw, bool u16, float* out,
+                              std::string* err)
+{
+  if (!raw || !out || nx < 1 || ny < 1 || nimages < 1) {
+    *err = "submit: invalid request";
+    return -1;
+  }
+  std::lock_guard<std::mutex> lk(mu_);
+  if (config < 0 || config >= (int)configs_.size()) {
+    *err = "submit: unknown configuration";
+    return -1;
+  }
+  Request r{next_ticket_++, Key{config, nx, ny, nimages}, raw, u16, out, now_s()};
+  done_[r.ticket] = Done{};
+  queue_.push_back(r);
+  cv_work_.notify_one();
+  return r.ticket;
+}
+
+int ReconServer::wait(long long ticket, double* latency_ms, std::string* err)
+{
+  std::unique_lock<std::mutex> lk(mu_);
+  if (done_.find(ticket) == done_.end()) {
+    *err = "wait: unknown ticket";
+    return -1;
+  }
+  cv_done_.wait(lk, [&] { return done_[ticket].done; });
+  Done d = done_[ticket];
+  done_.erase(ticket);
+  if (latency_ms) *latency_ms = d.latency_ms;
+  if (d.rc != 0) *err = d.err;
+  return d.rc;
+}
+
+size_t ReconServer::device_bytes_in_use()
+{
+  std::lock_guard<std::mutex> lk(mu_);
+  return in_use_;
+}
+
+ReconServer::Handle* ReconServer::acquire(const Key& k, std::string* err)
+{
+  std::string cfg;
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    for (auto& h : handles_)
+      if (!h->busy && h->key == k) {
+        h->busy = true;
+        return h.get();
+      }
+    cfg = configs_[std::get<0>(k)];
+  }
+  auto create = [&](std::string* e) {
+    return SIM_Reconstructor::from_shape(std::get<1>(k), std::get<2>(k), std::get<3>(k), cfg, e);
+  };
+  // deletes idle handles, least recently used first, until the handles fit
+  // the budget (or all idle ones)
+  auto evict_idle = [&](bool all) {
+    std::vector<SIM_Reconstructor*> doomed;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      while (all || in_use_ > budget_) {
+        Handle* lru = nullptr;
+        size_t idx = 0;
+        for (size_t i = 0; i < handles_.size(); ++i)
+          if (!handles_[i]->busy && (!lru || handles_[i]->last_used < lru->last_used)) {
+            lru = handles_[i].get();
+            idx = i;
+          }
+        if (!lru) break;
+        in_use_ -= lru->bytes;
+        doomed.push_back(lru->sr);
+        handles_.erase(handles_.begin() + idx);
+      }
+    }
+    for (auto* sr : doomed) delete sr;
+  };
+  std::string e1;
+  SIM_Reconstructor* sr = create(&e1);
+  if (!sr) {
+    evict_idle(true);
+    sr = create(&e1);
+  }
+  if (!sr) {
+    *err = e1;
+    return nullptr;
+  }
+  auto h = std::make_unique<Handle>();
+  h->key = k;
+  h->sr = sr;
+  h->busy = true;
+  h->bytes = sr->device_bytes();
+  Handle* raw = h.get();
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    in_use_ += h->bytes;
+    handles_.push_back(std::move(h));
+  }
+  evict_idle(false);
+  return raw;
+}
+
+void ReconServer::release(Handle* h)
+{
+  std::lock_guard<std::mutex> lk(mu_);
+  h->busy = false;
+  h->last_used = now_s();
+}
+
+void ReconServer::worker_loop()
+{
+  for (;;) {
+    Request r;
+    {
+      std::unique_lock<std::mutex> lk(mu_);
+      cv_work_.wait(lk, [&] { return stop_ || !queue_.empty(); });
+      if (queue_.empty()) return;  // stopping, and every queued request is done
+      r = queue_.front();
+      queue_.pop_front();
+    }
+    std::string err;
+    int rc = 0;
+    Handle* h = acquire(r.key, &err);
+    if (!h) {
+      rc = -1;
+    } else {
+      try {
+        const int nx = std::get<1>(r.key), ny = std::get<2>(r.key), ni = std::get<3>(r.key);
+        if (r.u16) h->sr->set_raw_u16((const uint16_t*)r.raw, nx, ny, ni);
+        else h->sr->set_raw_float((const float*)r.raw, nx, ny, ni);
+        h->sr->load_and_rescale(0, 0);
+        h->sr->set_cur_time(0);
+        h->sr->process_one_volume();
+        h->sr->get_result(r.out);
+      } catch (const std::exception& e) {
+        rc = -1;
+        err = e.what();
+      }
+      release(h);
+    }
+    const double t = now_s();
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      Done& d = done_[r.ticket];
+      d.done = true;
+      d.rc = rc;
+      d.err = err;
+      d.latency_ms = (t - r.t_submit) * 1e3;
+    }
+    cv_done_.notify_all();
+  }
+}
+
+}  // namespace simrecon

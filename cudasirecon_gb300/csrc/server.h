@@ -1,0 +1,77 @@
+// Request server over pooled reconstructor handles (the serving form of the
+// SR_* flow): volumes of different shapes and acquisition configurations are
+// submitted from any thread, run concurrently by worker threads that each
+// drive their own handle (own CUDA stream), and waited for by ticket.
+#pragma once
+#include <condition_variable>
+#include <cstddef>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <tuple>
+#include <vector>
+
+class SIM_Reconstructor;
+
+namespace simrecon {
+
+class ReconServer {
+ public:
+  // workers: concurrent volumes; hbm_budget: device bytes the handles may hold
+  ReconServer(int workers, size_t hbm_budget);
+  ~ReconServer();
+  // an acquisition configuration: a reference-style config file naming its OTF
+  int add_config(const std::string& config_path);
+  // one volume (the SR_setRaw layout) -> out (the SR_getResult layout); the
+  // buffers stay the caller's and must stay valid until wait() returns.
+  // Processed like a volume at time 0 (k0 fitted).  Returns a ticket, or -1.
+  long long submit(int config, int nx, int ny, int nimages, const void* raw, bool u16, float* out,
+                   std::string* err);
+  // blocks until the request is done; latency = submission to result in
+  // host memory.  Returns 0, or -1 with the request's error.
+  int wait(long long ticket, double* latency_ms, std::string* err);
+  size_t device_bytes_in_use();
+
+ private:
+  using Key = std::tuple<int, int, int, int>;  // config, nx, ny, nimages
+  struct Request {
+    long long ticket;
+    Key key;
+    const void* raw;
+    bool u16;
+    float* out;
+    double t_submit;
+  };
+  struct Done {
+    bool done = false;
+    int rc = 0;
+    std::string err;
+    double latency_ms = 0;
+  };
+  struct Handle {
+    Key key;
+    SIM_Reconstructor* sr = nullptr;
+    bool busy = false;
+    double last_used = 0;
+    size_t bytes = 0;
+  };
+  void worker_loop();
+  Handle* acquire(const Key& k, std::string* err);
+  void release(Handle* h);
+
+  std::vector<std::string> configs_;
+  std::mutex mu_;
+  std::condition_variable cv_work_, cv_done_;
+  std::deque<Request> queue_;
+  std::map<long long, Done> done_;
+  std::vector<std::unique_ptr<Handle>> handles_;
+  size_t budget_, in_use_ = 0;
+  long long next_ticket_ = 1;
+  bool stop_ = false;
+  std::vector<std::thread> workers_;
+};
+
+}  // namespace simrecon

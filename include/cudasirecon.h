@@ -243,6 +243,28 @@ int SRX_unpinHost(void* ptr);
 int SRX_processSeries(SIM_Reconstructor* sr, const void* const* raws, int raw_is_u16, float* const* outs, int n,
                       int t0);
 
+/* No counterpart in the reference.  A request server for many volumes of
+ * different shapes and acquisition configurations: worker threads run the
+ * SR_* flow on pooled handles (one per configuration, shape and worker, each
+ * with its own CUDA stream), so requests overlap on the GPU; the handles are
+ * kept within hbm_budget_bytes of device memory (idle ones evicted least
+ * recently used first).  A configuration is a reference-style config file
+ * that names its OTF (otf-file=).  Each request is one volume in the
+ * SR_setRaw layout, processed as a time-0 volume (k0 fitted), its result
+ * written in the SR_getResult layout; raw and out stay the caller's and must
+ * remain valid until SRX_serverWait returns for the ticket.  Submit returns a
+ * ticket (or -1); Wait blocks until that request is done, returns 0 or -1
+ * (SR_getLastError) and gives the latency from submission to the result in
+ * host memory.  Destroy finishes the queued requests first. */
+typedef struct SRX_Server SRX_Server;
+SRX_Server* SRX_serverCreate(int workers, size_t hbm_budget_bytes);
+int SRX_serverAddConfig(SRX_Server* s, const char* config_path);
+long long SRX_serverSubmit(SRX_Server* s, int config, int nx, int ny, int nimages, const void* raw, int raw_is_u16,
+                           float* out);
+int SRX_serverWait(SRX_Server* s, long long ticket, double* latency_ms);
+size_t SRX_serverDeviceBytes(SRX_Server* s);
+void SRX_serverDestroy(SRX_Server* s);
+
 /* makeotf.  The reference's makeotf is a program, not a library call
  * (src/otf/radialft.cpp:82-434); these replace it:
  *
