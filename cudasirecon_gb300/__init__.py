@@ -90,6 +90,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.SRX_serverSubmit.argtypes = [vp, ip, ip, ip, ip, vp, ip, vp]
     lib.SRX_serverWait.restype = ip
     lib.SRX_serverWait.argtypes = [vp, C.c_longlong, C.POINTER(C.c_double)]
+    lib.SRX_serverReserve.restype = ip
+    lib.SRX_serverReserve.argtypes = [vp, ip, ip, ip, ip, ip]
     lib.SRX_serverDeviceBytes.restype = C.c_size_t
     lib.SRX_serverDeviceBytes.argtypes = [vp]
     lib.SRX_serverDestroy.argtypes = [vp]
@@ -440,6 +442,13 @@ class Server:
         if rc != 0:
             raise SIReconError(_err(self.lib))
         return lat.value
+
+    def reserve(self, config: int, nx: int, ny: int, nimages: int, count: int) -> int:
+        """Create `count` handles of one shape ahead of its requests."""
+        n = self.lib.SRX_serverReserve(self.h, config, nx, ny, nimages, count)
+        if n < count:
+            raise SIReconError(_err(self.lib))
+        return n
 
     def device_bytes(self) -> int:
         return int(self.lib.SRX_serverDeviceBytes(self.h))

@@ -323,6 +323,21 @@ int SRX_serverWait(SRX_Server* s, long long ticket, double* latency_ms)
   return rc;
 }
 
+int SRX_serverReserve(SRX_Server* s, int config, int nx, int ny, int nimages, int count)
+{
+  int n = -1;
+  if (!s) {
+    g_last_error = "SRX_serverReserve: null server";
+    return -1;
+  }
+  guarded([&] {
+    std::string err;
+    n = ((simrecon::ReconServer*)s)->reserve(config, nx, ny, nimages, count, &err);
+    if (n < count) g_last_error = err;
+  });
+  return n;
+}
+
 size_t SRX_serverDeviceBytes(SRX_Server* s) { return s ? ((simrecon::ReconServer*)s)->device_bytes_in_use() : 0; }
 
 void SRX_serverDestroy(SRX_Server* s)

@@ -83,6 +83,27 @@ int ReconServer::wait(long long ticket, double* latency_ms, std::string* err)
   return d.rc;
 }
 
+int ReconServer::reserve(int config, int nx, int ny, int nimages, int count, std::string* err)
+{
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    if (config < 0 || config >= (int)configs_.size()) {
+      *err = "reserve: unknown configuration";
+      return -1;
+    }
+  }
+  const Key k{config, nx, ny, nimages};
+  std::vector<Handle*> got;
+  for (int i = 0; i < count; ++i) {
+    // hold the handles taken so far busy, so that each round makes a new one
+    Handle* h = acquire(k, err);
+    if (!h) break;
+    got.push_back(h);
+  }
+  for (auto* h : got) release(h);
+  return (int)got.size();
+}
+
 size_t ReconServer::device_bytes_in_use()
 {
   std::lock_guard<std::mutex> lk(mu_);

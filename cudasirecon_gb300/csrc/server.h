@@ -34,6 +34,9 @@ class ReconServer {
   // host memory.  Returns 0, or -1 with the request's error.
   int wait(long long ticket, double* latency_ms, std::string* err);
   size_t device_bytes_in_use();
+  // create handles for a shape up front so that the first requests of that
+  // shape do not pay for their creation; returns how many were created
+  int reserve(int config, int nx, int ny, int nimages, int count, std::string* err);
 
  private:
   using Key = std::tuple<int, int, int, int>;  // config, nx, ny, nimages

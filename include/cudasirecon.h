@@ -262,6 +262,10 @@ int SRX_serverAddConfig(SRX_Server* s, const char* config_path);
 long long SRX_serverSubmit(SRX_Server* s, int config, int nx, int ny, int nimages, const void* raw, int raw_is_u16,
                            float* out);
 int SRX_serverWait(SRX_Server* s, long long ticket, double* latency_ms);
+/* Create `count` handles for one shape ahead of its requests (a handle is
+ * created otherwise by the first request that finds none idle, which then
+ * pays for the device allocation).  Returns how many were created. */
+int SRX_serverReserve(SRX_Server* s, int config, int nx, int ny, int nimages, int count);
 size_t SRX_serverDeviceBytes(SRX_Server* s);
 void SRX_serverDestroy(SRX_Server* s);
 

@@ -44,6 +44,24 @@ def test_server_matches_plain(budget):
     srv.close()
 
 
+def test_server_reserve_then_serve():
+    case, _ = load("c3d_64")
+    want = plain(case)
+    srv = sr.Server(workers=2)
+    cid = srv.add_config(case["config"], case["otf"])
+    raw = np.ascontiguousarray(case["raw"][0])
+    assert srv.reserve(cid, case["nx"], case["ny"], raw.shape[0], 2) == 2
+    held = srv.device_bytes()
+    assert held > 0
+    outs = [np.zeros(want.shape, np.float32) for _ in range(4)]
+    ts = [srv.submit(cid, raw, o) for o in outs]
+    for t, o in zip(ts, outs):
+        srv.wait(t)
+        assert np.array_equal(o, want)
+    assert srv.device_bytes() == held  # the reserved handles served every request
+    srv.close()
+
+
 def test_server_rejects_unknown_config():
     case, _ = load("c3d_64")
     srv = sr.Server(workers=1)
