@@ -237,31 +237,35 @@ def run_gb300(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
     def series(n):
         r.process_series([host[i % len(host)] for i in range(n)], [outs2[i % 2] for i in range(n)], t0=t_idx)
     series(args.warmup)
-    barrier(dist)
-    t0 = time.perf_counter()
-    series(args.steps)
-    barrier(dist)
-    e2e_series_s = max_over_ranks(dist, time.perf_counter() - t0)
     # (b) plain per-volume SR_* calls (setRaw -> loadAndRescale -> process -> getResult)
+    def plain_one(i):
+        r.set_raw(host[i % len(host)])
+        r.load_and_rescale(t_idx, 0)
+        r.set_cur_time(t_idx)
+        r.process()
+        r.result(out)
+
     for i in range(args.warmup):
-        r.set_raw(host[i % len(host)])
-        r.load_and_rescale(t_idx, 0)
-        r.set_cur_time(t_idx)
-        r.process()
-        r.result(out)
-    barrier(dist)
-    t0 = time.perf_counter()
-    lat = []
-    for i in range(args.steps):
-        ts = time.perf_counter()
-        r.set_raw(host[i % len(host)])
-        r.load_and_rescale(t_idx, 0)
-        r.set_cur_time(t_idx)
-        r.process()
-        r.result(out)
-        lat.append(time.perf_counter() - ts)
-    barrier(dist)
-    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+        plain_one(i)
+    # the host link's bandwidth varies from run to run on a shared machine:
+    # three interleaved repeats of each form, medians reported
+    series_s, plain_s, lat = [], [], []
+    for rep in range(3):
+        barrier(dist)
+        t0 = time.perf_counter()
+        series(args.steps)
+        barrier(dist)
+        series_s.append(max_over_ranks(dist, time.perf_counter() - t0))
+        barrier(dist)
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            ts = time.perf_counter()
+            plain_one(i)
+            lat.append(time.perf_counter() - ts)
+        barrier(dist)
+        plain_s.append(max_over_ranks(dist, time.perf_counter() - t0))
+    e2e_series_s = statistics.median(series_s)
+    e2e_s = statistics.median(plain_s)
     # per-volume latency of the plain calls: stack submitted -> result in host memory
     lat_ms = np.sort(np.array(lat)) * 1e3
     latency = {"p50_ms": round(float(np.percentile(lat_ms, 50)), 3), "p99_ms": round(float(np.percentile(lat_ms, 99)), 3),
@@ -304,6 +308,8 @@ def run_gb300(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
                 "api": ("SRX_processSeries (uploads/downloads overlapped with computation), pinned host buffers"
                         if reuse else "plain SR_* calls per volume (k0 searched on every volume), pinned host buffers"),
                 "plain_value": round(e2e_plain, 1), "plain_latency": latency,
+                "repeats_mvox_per_s": {"series": [round(world * args.steps * outvox / v / 1e6, 1) for v in series_s],
+                                       "plain": [round(world * args.steps * outvox / v / 1e6, 1) for v in plain_s]},
                 "plain_api": "SR_setRawU16 -> SR_loadAndRescaleImage -> SR_processOneVolume -> SR_getResult"},
         "gpu_launches": int(launches),
         "clocks": clk,
@@ -479,6 +485,17 @@ def run_serving(args):
     # copy); requests of one type share the input, so a buffer written by two
     # requests in flight still ends up with their (identical) result
     pool = [[np.full(shapes[i], 0.0, np.float32) for _ in range(8)] for i in range(len(types))]
+    # saturated: the plain arm's 200 requests all submitted at once (peak
+    # served throughput; latency here is mostly queueing)
+    t0 = time.perf_counter()
+    tick = [srv.submit(cid[types[int(i)]["config"]], types[int(i)]["raw"], pool[int(i)][j % 8])
+            for j, i in enumerate(seq)]
+    sat_lat = [srv.wait(k) for k in tick]
+    sat_s = time.perf_counter() - t0
+    saturated = {"requests": len(seq), "req_per_s": round(len(seq) / sat_s, 1),
+                 "mvox_per_s": round(plain_vox / sat_s / 1e6, 1),
+                 "p50_ms": round(float(np.percentile(sat_lat, 50)), 2),
+                 "p99_ms": round(float(np.percentile(sat_lat, 99)), 2)}
     served = []
     dur = float(os.environ.get("SIRECON_SERVE_SECONDS", "3"))
     for lam in (5, 20, 50, 100, 200):
@@ -523,7 +540,137 @@ def run_serving(args):
                        "workers": workers, "hbm_budget_bytes": 150e9, "handles_bytes": dev,
                        "request": "standalone volume, k0 searched", "arrivals": "Poisson, seeded",
                        "buffers": "raw stacks page-locked, results pageable (both arms)"},
-            "plain": plain_line, "served": served}
+            "plain": plain_line, "served_saturated": saturated, "served": served}
+
+
+UNEVEN_2D = [256, 512, 1024, 2048]
+UNEVEN_3D_XY = [256, 384, 512, 640, 768]
+UNEVEN_3D_Z = [16, 24, 32, 48, 64]
+
+
+def _crop(raw, ndirs, nph, nz, n_xy, nz_new, peak):
+    """Centre crop of an Angle->Z->Phase stack to n_xy^2 x nz_new, rescaled
+    from the simulated 1000-photon peak (background 100) to `peak`."""
+    ny, nx = raw.shape[1:]
+    v = raw.reshape(ndirs, nz, nph, ny, nx)
+    y0, x0, z0 = (ny - n_xy) // 2, (nx - n_xy) // 2, (nz - nz_new) // 2
+    c = v[:, z0:z0 + nz_new, :, y0:y0 + n_xy, x0:x0 + n_xy].astype(np.float32)
+    c = (c - 100.0) * (peak / 1000.0) + 100.0
+    return np.ascontiguousarray(np.clip(np.rint(c), 0, 65535).astype(np.uint16).reshape(-1, n_xy, n_xy))
+
+
+def uneven_items(n2d=500, n3d=60):
+    """The uneven batch: n2d 2D frames (3 angles x 3 phases, nz = 1) with
+    nx = ny drawn from UNEVEN_2D (seed 6) and n3d 3D volumes (3 x 5 images per
+    z) with nx = ny drawn from UNEVEN_3D_XY and nz from UNEVEN_3D_Z (seed 7),
+    in one seeded random order.  Each shape's stack is a centre crop of one
+    simulated acquisition per dimensionality (2048^2 2D, 768^2 x 64 3D), so
+    the illumination pattern is the simulated one, rescaled to a peak drawn
+    from U[300, 3000] photons for that shape; items of one shape share it."""
+    from cudasirecon_gb300 import synthetic as syn
+    cache = os.environ.get("SIRECON_BENCH_CACHE")
+    r2, r3 = np.random.default_rng(6), np.random.default_rng(7)
+    s2 = [int(v) for v in r2.choice(UNEVEN_2D, n2d)]
+    s3 = [(int(a), int(b)) for a, b in zip(r3.choice(UNEVEN_3D_XY, n3d), r3.choice(UNEVEN_3D_Z, n3d))]
+    cfgs = {}
+    for twod in (True, False):
+        o = syn.Optics(nphases=3 if twod else 5)
+        otf = syn.ra_otf(o, nx_psf=128, nz_psf=64, norders=2 if twod else 3, twod=twod)
+        cfg = syn.config_text(o, twod=twod, extra={"wiener": 0.00048828125} if twod else None)
+        nx, nz = (2048, 1) if twod else (768, 64)
+        cp = os.path.join(cache, f"uneven_master_{'2d' if twod else '3d'}.npy") if cache else None
+        if cp and os.path.exists(cp):
+            master = np.load(cp)
+        else:
+            master = syn.simulate(nx, nx, nz, o, seed=6 if twod else 7, n_filaments=50).raw
+            if cp:
+                os.makedirs(cache, exist_ok=True)
+                np.save(cp, master)
+        cfgs[twod] = dict(cfg=cfg, otf=otf, master=master, nph=3 if twod else 5, nz=nz)
+    stacks = {}
+    for key in sorted(set((True, n, 1) for n in s2) | set((False, n, z) for n, z in s3)):
+        twod, n, z = key
+        c = cfgs[twod]
+        peak = float(np.random.default_rng(100000 * twod + 100 * n + z).uniform(300, 3000))
+        stacks[key] = _crop(c["master"], 3, c["nph"], c["nz"], n, z, peak)
+    order = [(True, n, 1) for n in s2] + [(False, n, z) for n, z in s3]
+    perm = np.random.default_rng(6).permutation(len(order))
+    return [order[k] for k in perm], stacks, cfgs
+
+
+def run_uneven(args):
+    """C4: the uneven 2D/3D batch, plain one-volume-at-a-time SR_* flow vs
+    SRX_serverRunBatch (per-shape chunks, copies overlapped, shapes
+    concurrent on the workers' streams)."""
+    import cudasirecon_gb300 as sr
+    sr.load_library()
+    order, stacks, cfgs = uneven_items()
+    for a in stacks.values():
+        sr.pin(a)
+    outvox = {k: 4 * k[1] * k[1] * k[2] for k in stacks}
+    total_vox = sum(outvox[k] for k in order)
+    # ---- plain: one handle per shape (created before the timed run)
+    hs = {}
+    for k, a in stacks.items():
+        c = cfgs[k[0]]
+        r = sr.Reconstructor(k[1], k[1], a.shape[0], c["cfg"], c["otf"])
+        hs[k] = (r, np.full(r.out_shape, 0.0, np.float32))
+
+    def plain(k):
+        r, out = hs[k]
+        r.set_raw(stacks[k])
+        r.load_and_rescale(0, 0)
+        r.set_cur_time(0)
+        r.process()
+        r.result(out)
+
+    for k in stacks:
+        plain(k)
+    plain_s = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        for k in order:
+            plain(k)
+        plain_s.append(time.perf_counter() - t0)
+    want = {k: hs[k][1].copy() for k in stacks}
+    for r, _ in hs.values():
+        r.close()
+    hs.clear()
+    # ---- batched
+    workers = int(os.environ.get("SIRECON_BATCH_WORKERS", "4"))
+    srv = sr.Server(workers=workers, hbm_budget=150e9)
+    cid = {twod: srv.add_config(c["cfg"], c["otf"]) for twod, c in cfgs.items()}
+    # result buffers: two per shape, touched up front (items of one shape
+    # share their input, so every write leaves the same volume)
+    pool = {k: [np.full((k[2], 2 * k[1], 2 * k[1]), 0.0, np.float32) for _ in range(2)] for k in stacks}
+    items = [(cid[k[0]], stacks[k], pool[k][j % 2]) for j, k in enumerate(order)]
+    srv.run_batch(items)  # warm-up: creates the handles of every shape
+    warm_counts = srv.counters()
+    batch_s = []
+    for _ in range(max(1, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        srv.run_batch(items)
+        batch_s.append(time.perf_counter() - t0)
+    written = {(k, j % 2) for j, k in enumerate(order)}
+    same = all(np.array_equal(pool[k][b], want[k]) for k, b in written)
+    dev = srv.device_bytes()
+    counts = srv.counters()
+    timed_counts = {k: counts[k] - warm_counts[k] for k in counts}
+    srv.close()
+    for a in stacks.values():
+        sr.unpin(a)
+    bs, ps = statistics.median(batch_s), statistics.median(plain_s)
+    n2 = sum(1 for k in order if k[0])
+    return {"metric": "Recon output Mvoxels/s, uneven 2D/3D batch (batched vs plain)", "impl": "gb300",
+            "value": round(total_vox / bs / 1e6, 1), "unit": "Mvoxels/s", "higher_is_better": True, "n_gpus": 1,
+            "data": "synthetic", "dtype": "f32",
+            "batched_s": [round(v, 3) for v in batch_s], "plain_s": [round(v, 3) for v in plain_s],
+            "plain_value": round(total_vox / ps / 1e6, 1), "identical_to_plain": bool(same),
+            "config": {"workload": "uneven", "items_2d": n2, "items_3d": len(order) - n2,
+                       "shapes": len(stacks), "workers": workers, "handles_bytes": dev,
+                       "handles_created_evicted_in_timed_runs": timed_counts,
+                       "request": "standalone acquisition, k0 searched",
+                       "buffers": "raw stacks page-locked, results pageable (both arms)"}}
 
 
 def main():
@@ -532,7 +679,7 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=list(WORKLOADS) + ["serving"], default="timeseries_512x512x48")
+    ap.add_argument("--workload", choices=list(WORKLOADS) + ["serving", "uneven"], default="timeseries_512x512x48")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
@@ -541,11 +688,12 @@ def main():
         return
     if args.impl == "reference":
         world, dist = 1, None
-    if args.workload == "serving":
+    if args.workload in ("serving", "uneven"):
         if rank == 0 and args.impl != "reference":
-            print(json.dumps(run_serving(args)), flush=True)
+            print(json.dumps(run_serving(args) if args.workload == "serving" else run_uneven(args)), flush=True)
         elif rank == 0:
-            print(json.dumps({"impl": "reference", "unavailable": "the serving workload has no reference arm"}))
+            print(json.dumps({"impl": "reference",
+                              "unavailable": f"the {args.workload} workload has no reference arm"}))
         return
     nx, ny, nz, _ = WORKLOADS[args.workload]
     vols, otf, cfg = make_workload(nx, ny, nz, 2)

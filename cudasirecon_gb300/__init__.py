@@ -30,6 +30,12 @@ def build(force: bool = False) -> str:
     return buildlib.build(force=force)
 
 
+class BatchItem(C.Structure):
+    """SRX_BatchItem (include/cudasirecon.h)."""
+    _fields_ = [("config", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nimages", C.c_int),
+                ("raw", C.c_void_p), ("raw_is_u16", C.c_int), ("out", C.c_void_p)]
+
+
 def load_library(path: str | None = None) -> C.CDLL:
     """Load libcudasirecon.so (raises if it has not been built)."""
     global _lib
@@ -92,7 +98,11 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.SRX_serverWait.argtypes = [vp, C.c_longlong, C.POINTER(C.c_double)]
     lib.SRX_serverReserve.restype = ip
     lib.SRX_serverReserve.argtypes = [vp, ip, ip, ip, ip, ip]
+    lib.SRX_serverRunBatch.restype = ip
+    lib.SRX_serverRunBatch.argtypes = [vp, C.POINTER(BatchItem), ip]
     lib.SRX_serverDeviceBytes.restype = C.c_size_t
+    lib.SRX_serverCounters.restype = None
+    lib.SRX_serverCounters.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
     lib.SRX_serverDeviceBytes.argtypes = [vp]
     lib.SRX_serverDestroy.argtypes = [vp]
     lib.SRX_makeOTF.restype = ip
@@ -450,8 +460,29 @@ class Server:
             raise SIReconError(_err(self.lib))
         return n
 
+    def run_batch(self, items) -> None:
+        """items: (config, raw, out) triples of any shapes (raw [nimages][ny][nx]
+        uint16 or float32, out float32 of the result size, both C-contiguous).
+        Blocks until every item's result is in its `out`."""
+        arr = (BatchItem * len(items))()
+        for i, (config, raw, out) in enumerate(items):
+            if not raw.flags.c_contiguous or not out.flags.c_contiguous or out.dtype != np.float32:
+                raise ValueError("raw and out must be C-contiguous, out float32")
+            if raw.dtype not in (np.uint16, np.float32):
+                raise ValueError("raw must be uint16 or float32")
+            nimg, ny, nx = raw.shape
+            arr[i] = BatchItem(config, nx, ny, nimg, raw.ctypes.data, int(raw.dtype == np.uint16), out.ctypes.data)
+        if self.lib.SRX_serverRunBatch(self.h, arr, len(items)) != 0:
+            raise SIReconError(_err(self.lib))
+
     def device_bytes(self) -> int:
         return int(self.lib.SRX_serverDeviceBytes(self.h))
+
+    def counters(self) -> dict:
+        """Handles created, and deleted to stay within the budget, so far."""
+        c, e = C.c_longlong(0), C.c_longlong(0)
+        self.lib.SRX_serverCounters(self.h, C.byref(c), C.byref(e))
+        return {"created": c.value, "evicted": e.value}
 
     def close(self):
         if self.h:

@@ -7,6 +7,7 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "cudasirecon.h"
 #include "makeotf.h"
@@ -336,6 +337,30 @@ int SRX_serverReserve(SRX_Server* s, int config, int nx, int ny, int nimages, in
     if (n < count) g_last_error = err;
   });
   return n;
+}
+
+int SRX_serverRunBatch(SRX_Server* s, const SRX_BatchItem* items, int n)
+{
+  if (!s || n < 0 || (n > 0 && !items)) {
+    g_last_error = "SRX_serverRunBatch: invalid arguments";
+    return -1;
+  }
+  int rc = -1;
+  guarded([&] {
+    std::vector<simrecon::ReconServer::BatchItem> v((size_t)n);
+    for (int i = 0; i < n; ++i)
+      v[i] = {items[i].config, items[i].nx, items[i].ny, items[i].nimages, items[i].raw, items[i].raw_is_u16 != 0,
+              items[i].out};
+    std::string err;
+    rc = ((simrecon::ReconServer*)s)->run_batch(v, &err);
+    if (rc != 0) g_last_error = err;
+  });
+  return rc;
+}
+
+void SRX_serverCounters(SRX_Server* s, long long* created, long long* evicted)
+{
+  if (s) ((simrecon::ReconServer*)s)->counters(created, evicted);
 }
 
 size_t SRX_serverDeviceBytes(SRX_Server* s) { return s ? ((simrecon::ReconServer*)s)->device_bytes_in_use() : 0; }

@@ -64,9 +64,27 @@ struct FilterK {
 // filterbands_kernel1 (gpuFunctionsImpl.cu:1504-1592) without the final
 // conjamp factor.  ND/NO: compile-time direction and order counts (0: use
 // the runtime values).
-template <int ND, int NO, bool CLAMP>
+// OTF value of order o at radial index krindex in the plane's kz: from the
+// plane's radial table (TAB; its entries are the kz interpolation of the
+// bilinear lookup, so the result is the same interpolation), else the
+// bilinear lookup itself
+template <bool CLAMP, bool TAB>
+__device__ __forceinline__ float2 filter_otf(const FilterArgs& a, const float2* tabz, int o, float krindex,
+                                             const OtfKz& kzi)
+{
+  if (TAB) {
+    const float2* T = tabz + o * a.otf.nxotf;
+    const int ir = (int)floorf(krindex);
+    const float ar = krindex - ir;
+    const float2 t0 = T[ir], t1 = T[ir + 1];
+    return make_float2((1 - ar) * t0.x + ar * t1.x, (1 - ar) * t0.y + ar * t1.y);
+  }
+  return otf_lookup_rr<CLAMP>(a.otf.otf[o], a.otf, krindex, kzi);
+}
+
+template <int ND, int NO, bool CLAMP, bool TAB>
 __device__ __forceinline__ float2 filter_scale(const FilterArgs& a, const FilterK& k, int order, int z0, float rdist1, float x1f,
-                               float y1f)
+                               float y1f, const float2* tabz)
 {
   const int dir = a.dir;
   const int nd = ND ? ND : a.ndirs, no = NO ? NO : a.norders;
@@ -75,7 +93,7 @@ __device__ __forceinline__ float2 filter_scale(const FilterArgs& a, const Filter
   // order-0 damping's axial part |z0 / zdc0|^3, the same for every term
   const float zf = fabsf(z0 / (float)a.zdc[0]);
   const float zf3 = zf * zf * zf;
-  float2 otf1 = otf_lookup_rr<CLAMP>(a.otf.otf[order], a.otf, rdist1 * k.rdkrotf, kzi);
+  float2 otf1 = filter_otf<CLAMP, TAB>(a, tabz, order, rdist1 * k.rdkrotf, kzi);
   float weight = otf1.x * otf1.x + otf1.y * otf1.y;
   if (order != 0) weight *= a.ampmag2[dir * no + order];
   float dampfact = k.rnv[dir * no + order];
@@ -104,7 +122,7 @@ __device__ __forceinline__ float2 filter_scale(const FilterArgs& a, const Filter
       if (r2 >= k.cut2hi) continue;  // far outside: the exact test below would fail too
       const float rdist2 = sqrtf(r2);
       if (rdist2 < a.rdistcutoff) {
-        const float2 otf2 = otf_lookup_rr<CLAMP>(a.otf.otf[ao2], a.otf, rdist2 * k.rdkrotf, kzi);
+        const float2 otf2 = filter_otf<CLAMP, TAB>(a, tabz, ao2, rdist2 * k.rdkrotf, kzi);
         float w = (otf2.x * otf2.x + otf2.y * otf2.y) * k.termw[dir2 * no + ao2];
         if (a.suppress && order2 != 0 && rdist2 <= k.supp_r)
           w *= dev_suppress(rdist2 * k.rmin_dkr);
@@ -159,20 +177,39 @@ __device__ __forceinline__ void apply_side(float2& re, float2& im, float2 scale,
   }
 }
 
-template <int ND, int NO, bool CLAMP>
+// TAB: the block (one kz plane) first builds, in shared memory, each order's
+// OTF interpolated to this plane's kz (+z0) and to the conjugate pass's kz
+// (-z0) along kr: [2][NO][nxotf]; only where no lookup can leave the table
+template <int ND, int NO, bool CLAMP, bool TAB>
 __global__ void __launch_bounds__(kThreads) k_filter(const __grid_constant__ FilterArgs a, const __grid_constant__ FilterK k)
 {
+  extern __shared__ float2 tab[];
   const int nx = a.nx, ny = a.ny, nz = a.nz, nxh = nx / 2 + 1;
   const int order = blockIdx.z, iz = blockIdx.y;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int zdc = a.zdc[order];
+  const bool inband = (iz <= zdc) || (iz >= nz - zdc);
+  if (TAB) {
+    static_assert(!TAB || NO > 0, "the table needs the order count at compile time");
+    const int nxo = a.otf.nxotf, nzo = a.otf.nzotf;
+    if (inband) {
+      const int zp = iz <= zdc ? iz : iz - nz;
+      for (int t = threadIdx.x; t < 2 * NO * nxo; t += blockDim.x) {
+        const int pass = t / (NO * nxo), r = t - pass * NO * nxo, o = r / nxo, ir = r - o * nxo;
+        const OtfKz kz = otf_kz(a.otf, pass ? -zp : zp);
+        const float2 va = __ldg(a.otf.otf[o] + ir * nzo + kz.iz), vb = __ldg(a.otf.otf[o] + ir * nzo + kz.izp);
+        const float az = kz.az;
+        tab[t] = make_float2(va.x * (1 - az) + vb.x * az, va.y * (1 - az) + vb.y * az);
+      }
+    }
+    __syncthreads();
+  }
   if (e >= ny * nxh) return;
   const int iin = e / nxh, jin = e - iin * nxh;
   const size_t plane = (size_t)ny * nxh;
   float2* b1 = a.bands + (size_t)(order == 0 ? 0 : 2 * order - 1) * nz * plane;
   float2* b2 = order == 0 ? nullptr : a.bands + (size_t)(2 * order) * nz * plane;
   const size_t ind = (size_t)iz * plane + e;
-  const int zdc = a.zdc[order];
-  const bool inband = (iz <= zdc) || (iz >= nz - zdc);
   if (!inband) {  // filterbands_kernel3
     b1[ind] = make_float2(0.f, 0.f);
     if (b2) b2[ind] = make_float2(0.f, 0.f);
@@ -189,7 +226,7 @@ __global__ void __launch_bounds__(kThreads) k_filter(const __grid_constant__ Fil
     if (b2) b2[ind] = make_float2(0.f, 0.f);
     return;
   }
-  float2 s1 = filter_scale<ND, NO, CLAMP>(a, k, order, z0, rdist1, x1f, y1f);
+  float2 s1 = filter_scale<ND, NO, CLAMP, TAB>(a, k, order, z0, rdist1, x1f, y1f, tab);
   if (order == 0) {
     b1[ind] = cmul(b1[ind], s1);
     return;
@@ -202,7 +239,7 @@ __global__ void __launch_bounds__(kThreads) k_filter(const __grid_constant__ Fil
     const int x2 = -jin;
     float x2f = x2 * a.dkx, y2f = y2 * a.dky;
     float rdist2 = sqrtf(x2f * x2f + y2f * y2f);
-    float2 s2 = filter_scale<ND, NO, CLAMP>(a, k, order, -z0, rdist2, x2f, y2f);
+    float2 s2 = filter_scale<ND, NO, CLAMP, TAB>(a, k, order, -z0, rdist2, x2f, y2f, tab + (TAB ? NO * a.otf.nxotf : 0));
     apply_side(re, im, cmul(s2, a.conjamp[order]), true);
   }
   b1[ind] = re;
@@ -546,6 +583,18 @@ __global__ void __launch_bounds__(kThreads) k_asm_z(AssembleArgs a, const unsign
   }
 }
 
+// Z = 1 (2D): the z transform is the identity, out = Re(S) (two elements per
+// thread; X = 2 nx is even)
+__global__ void __launch_bounds__(kThreads) k_asm_z1(const float4* __restrict__ S, float2* out, size_t npairs,
+                                                     const unsigned char* __restrict__ zactive)
+{
+  const bool on = zactive[0] != 0;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < npairs; i += (size_t)gridDim.x * blockDim.x) {
+    const float4 v = on ? S[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    out[i] = make_float2(v.x, v.z);
+  }
+}
+
 // Four-step variant of k_asm_z for Z = 16 * R1: 64 columns of one output row
 // per CTA.  Stage 1: the thread for (column c, j < 16) loads the R1 planes
 // z = j + 16 e of S (only the in-band ones; the rest are zero) and runs the
@@ -655,14 +704,22 @@ int launch_filter(const FilterArgs& a, cudaStream_t s, long long* launches)
   k.cut2hi = (float)((double)a.rdistcutoff * a.rdistcutoff * (1.0 + 1e-6));
   // every looked-up radius is <= rdistcutoff, so the table is never left
   // when floor(rdistcutoff / dkrotf) + 2 <= nxotf
-  const bool clamp = !(std::floor(a.rdistcutoff * k.rdkrotf) + 2 <= a.otf.nxotf);
+  // (and no kz index, |kz| <= nz/2, leaves it along kz)
+  const bool clamp = !(std::floor(a.rdistcutoff * k.rdkrotf) + 2 <= a.otf.nxotf) ||
+                     !(a.nz == 1 || (a.nz / 2) * (double)a.otf.kzscale + 1.0 < a.otf.nzotf);
   KernelTimer* kt = kernel_timer();
   if (kt) kt->begin(s);
-  if (a.ndirs == 3 && a.norders == 3 && !clamp) k_filter<3, 3, false><<<g, kThreads, 0, s>>>(a, k);
-  else if (a.ndirs == 3 && a.norders == 3) k_filter<3, 3, true><<<g, kThreads, 0, s>>>(a, k);
-  else if (a.ndirs == 3 && a.norders == 2 && !clamp) k_filter<3, 2, false><<<g, kThreads, 0, s>>>(a, k);
-  else if (a.ndirs == 3 && a.norders == 2) k_filter<3, 2, true><<<g, kThreads, 0, s>>>(a, k);
-  else k_filter<0, 0, true><<<g, kThreads, 0, s>>>(a, k);
+  // per-plane radial tables when the lookups stay inside the table and the
+  // tables fit in 48 KB of shared memory
+  const size_t tabb = 2 * (size_t)no * a.otf.nxotf * sizeof(float2);
+  const bool tab = !clamp && tabb <= 48 * 1024;
+  if (a.ndirs == 3 && a.norders == 3 && tab) k_filter<3, 3, false, true><<<g, kThreads, tabb, s>>>(a, k);
+  else if (a.ndirs == 3 && a.norders == 3 && !clamp) k_filter<3, 3, false, false><<<g, kThreads, 0, s>>>(a, k);
+  else if (a.ndirs == 3 && a.norders == 3) k_filter<3, 3, true, false><<<g, kThreads, 0, s>>>(a, k);
+  else if (a.ndirs == 3 && a.norders == 2 && tab) k_filter<3, 2, false, true><<<g, kThreads, tabb, s>>>(a, k);
+  else if (a.ndirs == 3 && a.norders == 2 && !clamp) k_filter<3, 2, false, false><<<g, kThreads, 0, s>>>(a, k);
+  else if (a.ndirs == 3 && a.norders == 2) k_filter<3, 2, true, false><<<g, kThreads, 0, s>>>(a, k);
+  else k_filter<0, 0, true, false><<<g, kThreads, 0, s>>>(a, k);
   // every element of the 2*norders-1 bands of this direction is read (in
   // band) or only written (cleared)
   double planeb = (double)a.ny * nxh * sizeof(float2);
@@ -823,7 +880,11 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
   KernelTimer* kt = kernel_timer();
   if (kt) kt->begin(s);
   const int zr1 = a.Z % 16 == 0 ? a.Z / 16 : 0;
-  if (zr1 == 2 || zr1 == 3 || zr1 == 4 || zr1 == 5 || zr1 == 6 || zr1 == 8) {
+  if (a.Z == 1 && ((size_t)a.X * a.Y) % 2 == 0) {
+    const size_t npairs = (size_t)a.X * a.Y / 2;
+    const unsigned nb = (unsigned)std::min<size_t>((npairs + kThreads - 1) / kThreads, 152 * 16);
+    k_asm_z1<<<nb, kThreads, 0, s>>>((const float4*)a.S, (float2*)a.out, npairs, d_zact);
+  } else if (zr1 == 2 || zr1 == 3 || zr1 == 4 || zr1 == 5 || zr1 == 6 || zr1 == 8) {
     auto go = [&]<int R1>() {
       const size_t bytes = (size_t)R1 * (16 * 64 + 8) * sizeof(float2);
       allow_dynamic_smem((const void*)k_asm_z4<R1>, bytes);

@@ -499,6 +499,7 @@ __global__ void k_argmax_final(const float2* cc, int nx, int ny, const float* bv
 
 // ---------------------------------------------------- modamp candidates
 constexpr int kCand = 8;  // candidates per pass (register accumulators)
+static_assert(2 * kCand == 16, "k_modamp_partial reduces 16 values per thread");
 
 // ex[c][x] = exp(i 2 pi (x - nx/2) kx_c dxy), ey[c][y] likewise
 __global__ void k_phase_tables(const float2* kc, int ncand, int nx, int ny, float dxy, float2* ex, float2* ey)
@@ -517,10 +518,14 @@ __global__ void k_phase_tables(const float2* kc, int ncand, int nx, int ny, floa
   }
 }
 
-__global__ void k_modamp_partial(const float2* __restrict__ P, int nx, int ny, const float2* __restrict__ ex,
-                                 const float2* __restrict__ ey, int c0, int nc, double* partial, int ncand)
+__global__ void __launch_bounds__(256) k_modamp_partial(const float2* __restrict__ P, int nx, int ny,
+                                                         const float2* __restrict__ ex, const float2* __restrict__ ey,
+                                                         int c0, int nc, double* partial, int ncand)
 {
-  __shared__ double red[32];
+  // per-thread float sums, then one transposed pass over shared memory: 16
+  // threads per value each add 16 threads' sums in double, then 16 of those
+  __shared__ float sacc[256][2 * kCand + 1];
+  __shared__ double sseg[16][2 * kCand];
   float2 acc[kCand];
 #pragma unroll
   for (int c = 0; c < kCand; ++c) acc[c] = make_float2(0.f, 0.f);
@@ -538,13 +543,23 @@ __global__ void k_modamp_partial(const float2* __restrict__ P, int nx, int ny, c
       }
     }
   }
-  for (int c = 0; c < nc; ++c) {
-    double re = block_sum_d((double)acc[c].x, red);
-    double im = block_sum_d((double)acc[c].y, red);
-    if (threadIdx.x == 0) {
-      partial[((size_t)blockIdx.x * ncand + c0 + c) * 2] = re;
-      partial[((size_t)blockIdx.x * ncand + c0 + c) * 2 + 1] = im;
-    }
+#pragma unroll
+  for (int c = 0; c < kCand; ++c) {
+    sacc[threadIdx.x][2 * c] = acc[c].x;
+    sacc[threadIdx.x][2 * c + 1] = acc[c].y;
+  }
+  __syncthreads();
+  const int v = threadIdx.x & 15, seg = threadIdx.x >> 4;
+  double sum = 0.0;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) sum += (double)sacc[seg * 16 + i][v];
+  sseg[seg][v] = sum;
+  __syncthreads();
+  if (threadIdx.x < 2 * nc) {
+    double tot = 0.0;
+#pragma unroll
+    for (int g = 0; g < 16; ++g) tot += sseg[g][threadIdx.x];
+    partial[((size_t)blockIdx.x * ncand + c0 + (threadIdx.x >> 1)) * 2 + (threadIdx.x & 1)] = tot;
   }
 }
 
@@ -643,6 +658,8 @@ int launch_crosscorr_peak(const float2* pmap, float2* cc, int nx, int ny, float*
   if (!get_fft_plan(nx, &px) || !get_fft_plan(ny, &py)) return -1;
   int nl = std::max(1, std::min(ny, kMaxElems / nx));
   size_t sm1 = fft_stage_smem(nx, nl, nl * (nx + 1), kThreads);
+  KernelTimer* kt = kernel_timer();
+  if (kt) kt->begin(s);
   dispatch_fft_len(kSiteCorrRows, nx, [&]<int NF>() {
     allow_dynamic_smem((const void*)k_fft_rows<-1, true, NF>, sm1);
     k_fft_rows<-1, true, NF><<<(ny + nl - 1) / nl, kThreads, sm1, s>>>(pmap, cc, nx, ny, px, nl);
@@ -656,6 +673,8 @@ int launch_crosscorr_peak(const float2* pmap, float2* cc, int nx, int ny, float*
   int nb = 256;
   k_argmax_partial<<<nb, 256, 0, s>>>(cc, nx * ny, blockval, blockidx);
   k_argmax_final<<<1, 256, 0, s>>>(cc, nx, ny, blockval, blockidx, nb, peak);
+  // pmap in, cc out; cc in and out (columns); cc in (argmax)
+  if (kt) kt->end("k_crosscorr", s, 5.0 * nx * ny * sizeof(float2));
   if (launches) *launches += 4;
   return (int)cudaGetLastError();
 }
@@ -665,14 +684,23 @@ int launch_modamp_candidates(const float2* pmap, int nx, int ny, float dxy, cons
 {
   float2* ex = tables;
   float2* ey = tables + (size_t)ncand * nx;
-  k_phase_tables<<<std::min(256, (ncand * (nx + ny) + 255) / 256), 256, 0, s>>>(kcand, ncand, nx, ny, dxy, ex, ey);
-  const int nb = 256;
+  KernelTimer* kt = kernel_timer();
+  if (kt) kt->begin(s);
+  // double sincos: spread over all SMs (FP64 throughput is per SM)
+  k_phase_tables<<<(ncand * (nx + ny) + 63) / 64, 64, 0, s>>>(kcand, ncand, nx, ny, dxy, ex, ey);
+  if (kt) kt->end("k_modamp_tables", s, (double)ncand * (nx + ny) * sizeof(float2));
+  // about four elements per thread, at most kModampBlocks blocks
+  const int nb = (int)std::min<long long>(kModampBlocks, std::max<long long>(1, ((long long)nx * ny + 1023) / 1024));
+  if (kt) kt->begin(s);
   for (int c0 = 0; c0 < ncand; c0 += kCand) {
     int nc = std::min(kCand, ncand - c0);
     k_modamp_partial<<<nb, 256, 0, s>>>(pmap, nx, ny, ex, ey, c0, nc, partial, ncand);
     if (launches) *launches += 1;
   }
+  if (kt) kt->end("k_modamp", s, (double)((ncand + kCand - 1) / kCand) * nx * ny * sizeof(float2));
+  if (kt) kt->begin(s);
   k_modamp_final<<<ncand, 256, 0, s>>>(partial, nb, ncand, xstary);
+  if (kt) kt->end("k_modamp_final", s, (double)nb * ncand * 2 * sizeof(double));
   if (launches) *launches += 2;
   return (int)cudaGetLastError();
 }

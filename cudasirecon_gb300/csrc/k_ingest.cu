@@ -399,6 +399,39 @@ __global__ void __launch_bounds__(kThreads) k_separate(float2* spec, const float
   }
 }
 
+// 2D (nz = 1): separation alone (no z transform), one thread per element of
+// one direction's plane, coalesced along kx; the same arithmetic as k_separate
+template <int NPH>
+__global__ void __launch_bounds__(kThreads) k_separate_z1(float2* spec, const float* __restrict__ scale,
+                                                          const float* __restrict__ sepmat, size_t plane)
+{
+  __shared__ float M[NPH * NPH];
+  for (int i = threadIdx.x; i < NPH * NPH; i += blockDim.x) M[i] = sepmat[i];
+  __syncthreads();
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int d = blockIdx.y;
+  if (e >= plane) return;
+  float2* base = spec + (size_t)d * NPH * plane + e;
+  float2 in[NPH];
+#pragma unroll
+  for (int p = 0; p < NPH; ++p) {
+    const float s = scale[d * NPH + p];
+    const float2 v = base[(size_t)p * plane];
+    in[p] = make_float2(v.x * s, v.y * s);
+  }
+#pragma unroll
+  for (int b = 0; b < NPH; ++b) {
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int p = 0; p < NPH; ++p) {
+      const float m = M[b * NPH + p];
+      acc.x += m * in[p].x;
+      acc.y += m * in[p].y;
+    }
+    base[(size_t)b * plane] = acc;
+  }
+}
+
 }  // namespace
 
 static size_t fft_smem(int n, int lines, int elems) { return fft_stage_smem(n, lines, elems, kThreads); }
@@ -574,7 +607,12 @@ int launch_separate(float2* spec, const float* scale, const float* sepmat, int n
   KernelTimer* kt = kernel_timer();
   if (kt) kt->begin(s);
   const int r1 = nz % 16 == 0 ? nz / 16 : 0;
-  if ((r1 == 2 || r1 == 3 || r1 == 4 || r1 == 5 || r1 == 6 || r1 == 8) && nphases == 5) {
+  if (nz == 1 && (nphases == 3 || nphases == 5)) {
+    const size_t plane = (size_t)ny * nxh;
+    dim3 g1((unsigned)((plane + kThreads - 1) / kThreads), ndirs);
+    if (nphases == 3) k_separate_z1<3><<<g1, kThreads, 0, s>>>(spec, scale, sepmat, plane);
+    else k_separate_z1<5><<<g1, kThreads, 0, s>>>(spec, scale, sepmat, plane);
+  } else if ((r1 == 2 || r1 == 3 || r1 == 4 || r1 == 5 || r1 == 6 || r1 == 8) && nphases == 5) {
     dim3 g4((nxh + 15) / 16, ny, ndirs);
     auto go = [&]<int R1>() {
       const size_t bytes = (size_t)nphases * R1 * (16 * 16 + 8) * sizeof(float2);

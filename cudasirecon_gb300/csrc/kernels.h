@@ -8,6 +8,10 @@
 
 namespace simrecon {
 
+// blocks of the modamp candidate reduction at most (four per SM); its
+// partial-sum buffer holds kModampBlocks x candidates x 2 doubles
+constexpr int kModampBlocks = 608;
+
 // ------------------------------------------------------------ kernel timing
 // When a timer is installed on the calling thread, every launcher brackets
 // its launches with begin()/end() on the launch stream and reports the

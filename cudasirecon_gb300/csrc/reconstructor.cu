@@ -441,7 +441,7 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
       {(void**)&d_peak_, 8 * sizeof(float)},
       {(void**)&d_kcand_, kMaxCand * sizeof(float2)},
       {(void**)&d_tables_, (size_t)kMaxCand * (nx_ + ny_) * sizeof(float2)},
-      {(void**)&d_partial_, (size_t)256 * kMaxCand * 2 * sizeof(double)},
+      {(void**)&d_partial_, (size_t)kModampBlocks * kMaxCand * 2 * sizeof(double)},
       {(void**)&d_xstary_, (size_t)kMaxCand * 2 * sizeof(double)},
       {(void**)&d_k0_, (size_t)kMaxDirs * sizeof(float2)},
       {(void**)&d_ex_, (size_t)ndirs_ * norders_ * X_ * sizeof(float2)},
@@ -1165,7 +1165,8 @@ void SIM_Reconstructor::get_fit(float* k0, float* amps) const
   }
 }
 
-void SIM_Reconstructor::process_series(const void* const* raws, bool u16, float* const* outs, int n, int t0)
+void SIM_Reconstructor::process_series(const void* const* raws, bool u16, float* const* outs, int n, int t0,
+                                       bool standalone)
 {
   if (n <= 0) return;
   if (!raws || !outs) throw std::runtime_error("processSeries: null buffer list");
@@ -1174,6 +1175,7 @@ void SIM_Reconstructor::process_series(const void* const* raws, bool u16, float*
   if (!d_raw_alt_) {
     check(cudaMalloc(&d_raw_alt_, (size_t)nimg_ * nx_ * ny_ * sizeof(float)), "series raw buffer");
     check(cudaMalloc((void**)&d_out_extra_, out_bytes), "series output buffer");
+    series_bytes_ = (size_t)nimg_ * nx_ * ny_ * sizeof(float) + out_bytes;
     d_out_alt_ = d_out_extra_;
     check(cudaStreamCreateWithFlags(&h2d_stream_, cudaStreamNonBlocking), "series stream");
     check(cudaStreamCreateWithFlags(&d2h_stream_, cudaStreamNonBlocking), "series stream");
@@ -1205,8 +1207,9 @@ void SIM_Reconstructor::process_series(const void* const* raws, bool u16, float*
       ingest();  // returns after the ingest kernels finished: raw buffer b is free
       check(cudaEventRecord(ev_raw_free_[b], stream_), "series event");
       if (i + 2 < n) upload(i + 2);
-      load_and_rescale(t0 + i, 0);
-      set_cur_time(t0 + i);
+      const int t = standalone ? 0 : t0 + i;
+      load_and_rescale(t, 0);
+      set_cur_time(t);
       check(cudaStreamWaitEvent(stream_, ev_out_free_[b], 0), "series wait");
       d_out_ = out_buf[b];
       process_one_volume();

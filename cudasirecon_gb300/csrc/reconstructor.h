@@ -37,8 +37,11 @@ class SIM_Reconstructor {
   // getResult(outs[i]), with the upload of volume i+1 and the download of
   // volume i-1 overlapped with the computation of volume i (double-buffered
   // device raw/output buffers, separate copy streams; page-locked host
-  // buffers make the copies asynchronous)
-  void process_series(const void* const* raws, bool u16, float* const* outs, int n, int t0);
+  // buffers make the copies asynchronous).  standalone: every volume is
+  // processed as time 0 instead (its own k0 search), the plain per-request
+  // flow, with the same overlap.
+  void process_series(const void* const* raws, bool u16, float* const* outs, int n, int t0,
+                      bool standalone = false);
   void set_file(int it, int iw);
   void write_result(int it, int iw);
   void close_files();
@@ -54,7 +57,7 @@ class SIM_Reconstructor {
   void reset_profile();
   long long launches() const { return launches_; }
   size_t out_elems() const { return (size_t)X_ * Y_ * Z_; }
-  size_t device_bytes() const { return arena_bytes_; }  // the handle's device arena
+  size_t device_bytes() const { return arena_bytes_ + series_bytes_; }  // device memory the handle holds
 
   simrecon::Options opt;  // ReconParams + ImageParams live here (references handed out)
 
@@ -93,6 +96,7 @@ class SIM_Reconstructor {
   // device arena
   char* arena_ = nullptr;
   size_t arena_bytes_ = 0;
+  size_t series_bytes_ = 0;  // process_series' second raw and output buffers
   void* d_raw_ = nullptr;
   float2* d_spec_ = nullptr;
   float* d_scale_ = nullptr;

@@ -1,6 +1,8 @@
 // ReconServer: a FIFO of volume requests served by worker threads, each
 // running the plain per-volume flow (setRaw -> loadAndRescaleImage(0) ->
-// processOneVolume -> getResult) on a handle it holds for the request.
+// processOneVolume -> getResult) on a handle it holds for the request, or, for
+// a chunk of a batch, the same flow over the chunk's volumes with copies
+// overlapped (process_series, standalone form).
 //
 // Handles are pooled per (configuration, nx, ny, nimages): a worker reuses an
 // idle handle of the request's shape, else creates one.  Device memory is
@@ -11,6 +13,7 @@
 // the creation is tried once more.
 #include "server.h"
 
+#include <algorithm>
 #include <chrono>
 #include <stdexcept>
 
@@ -56,16 +59,78 @@ long long ReconServer::submit(int config, int nx, int ny, int nimages, const voi
     *err = "submit: invalid request";
     return -1;
   }
-  std::lock_guard<std::mutex> lk(mu_);
-  if (config < 0 || config >= (int)configs_.size()) {
-    *err = "submit: unknown configuration";
-    return -1;
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    if (config < 0 || config >= (int)configs_.size()) {
+      *err = "submit: unknown configuration";
+      return -1;
+    }
   }
-  Request r{next_ticket_++, Key{config, nx, ny, nimages}, raw, u16, out, now_s()};
+  return enqueue(Request{0, Key{config, nx, ny, nimages}, {raw}, u16, {out}, now_s()});
+}
+
+long long ReconServer::enqueue(Request r)
+{
+  std::lock_guard<std::mutex> lk(mu_);
+  r.ticket = next_ticket_++;
   done_[r.ticket] = Done{};
-  queue_.push_back(r);
+  const long long t = r.ticket;
+  queue_.push_back(std::move(r));
   cv_work_.notify_one();
-  return r.ticket;
+  return t;
+}
+
+int ReconServer::run_batch(const std::vector<BatchItem>& items, std::string* err)
+{
+  // group by (config, shape, input type); a group keeps the caller's order
+  std::map<std::tuple<int, int, int, int, bool>, std::vector<size_t>> groups;
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    for (size_t i = 0; i < items.size(); ++i) {
+      const BatchItem& it = items[i];
+      if (!it.raw || !it.out || it.nx < 1 || it.ny < 1 || it.nimages < 1 || it.config < 0 ||
+          it.config >= (int)configs_.size()) {
+        *err = "runBatch: invalid item " + std::to_string(i);
+        return -1;
+      }
+      groups[{it.config, it.nx, it.ny, it.nimages, it.u16}].push_back(i);
+    }
+  }
+  // chunks: a group of g items is cut into about one chunk per worker, at
+  // most kMaxChunk items each (a chunk holds one handle for its whole run)
+  constexpr size_t kMaxChunk = 16;
+  const size_t nw = workers_.size();
+  struct Chunk {
+    Request r;
+    double cost;
+  };
+  std::vector<Chunk> chunks;
+  for (auto& [gk, idx] : groups) {
+    const size_t per = std::min(kMaxChunk, std::max<size_t>(1, (idx.size() + nw - 1) / nw));
+    for (size_t a = 0; a < idx.size(); a += per) {
+      Request r{0, Key{std::get<0>(gk), std::get<1>(gk), std::get<2>(gk), std::get<3>(gk)}, {}, std::get<4>(gk), {},
+                now_s()};
+      for (size_t j = a; j < std::min(idx.size(), a + per); ++j) {
+        r.raws.push_back(items[idx[j]].raw);
+        r.outs.push_back(items[idx[j]].out);
+      }
+      const double cost = (double)std::get<1>(gk) * std::get<2>(gk) * std::get<3>(gk) * r.raws.size();
+      chunks.push_back({std::move(r), cost});
+    }
+  }
+  // largest first, so that the last chunks to start are short ones
+  std::stable_sort(chunks.begin(), chunks.end(), [](const Chunk& a, const Chunk& b) { return a.cost > b.cost; });
+  std::vector<long long> tickets;
+  for (auto& c : chunks) tickets.push_back(enqueue(std::move(c.r)));
+  int rc = 0;
+  for (long long t : tickets) {
+    std::string e;
+    if (wait(t, nullptr, &e) != 0 && rc == 0) {
+      rc = -1;
+      *err = e;
+    }
+  }
+  return rc;
 }
 
 int ReconServer::wait(long long ticket, double* latency_ms, std::string* err)
@@ -110,6 +175,13 @@ size_t ReconServer::device_bytes_in_use()
   return in_use_;
 }
 
+void ReconServer::counters(long long* created, long long* evicted)
+{
+  std::lock_guard<std::mutex> lk(mu_);
+  if (created) *created = created_;
+  if (evicted) *evicted = evicted_;
+}
+
 ReconServer::Handle* ReconServer::acquire(const Key& k, std::string* err)
 {
   std::string cfg;
@@ -141,6 +213,7 @@ ReconServer::Handle* ReconServer::acquire(const Key& k, std::string* err)
           }
         if (!lru) break;
         in_use_ -= lru->bytes;
+        ++evicted_;
         doomed.push_back(lru->sr);
         handles_.erase(handles_.begin() + idx);
       }
@@ -166,6 +239,7 @@ ReconServer::Handle* ReconServer::acquire(const Key& k, std::string* err)
   {
     std::lock_guard<std::mutex> lk(mu_);
     in_use_ += h->bytes;
+    ++created_;
     handles_.push_back(std::move(h));
   }
   evict_idle(false);
@@ -175,6 +249,9 @@ ReconServer::Handle* ReconServer::acquire(const Key& k, std::string* err)
 void ReconServer::release(Handle* h)
 {
   std::lock_guard<std::mutex> lk(mu_);
+  const size_t nb = h->sr->device_bytes();  // grows when a chunk first used the series buffers
+  in_use_ = in_use_ - h->bytes + nb;
+  h->bytes = nb;
   h->busy = false;
   h->last_used = now_s();
 }
@@ -198,12 +275,16 @@ void ReconServer::worker_loop()
     } else {
       try {
         const int nx = std::get<1>(r.key), ny = std::get<2>(r.key), ni = std::get<3>(r.key);
-        if (r.u16) h->sr->set_raw_u16((const uint16_t*)r.raw, nx, ny, ni);
-        else h->sr->set_raw_float((const float*)r.raw, nx, ny, ni);
-        h->sr->load_and_rescale(0, 0);
-        h->sr->set_cur_time(0);
-        h->sr->process_one_volume();
-        h->sr->get_result(r.out);
+        if (r.raws.size() == 1) {  // the plain per-volume flow
+          if (r.u16) h->sr->set_raw_u16((const uint16_t*)r.raws[0], nx, ny, ni);
+          else h->sr->set_raw_float((const float*)r.raws[0], nx, ny, ni);
+          h->sr->load_and_rescale(0, 0);
+          h->sr->set_cur_time(0);
+          h->sr->process_one_volume();
+          h->sr->get_result(r.outs[0]);
+        } else {
+          h->sr->process_series(r.raws.data(), r.u16, r.outs.data(), (int)r.raws.size(), 0, true);
+        }
       } catch (const std::exception& e) {
         rc = -1;
         err = e.what();

@@ -34,18 +34,36 @@ class ReconServer {
   // host memory.  Returns 0, or -1 with the request's error.
   int wait(long long ticket, double* latency_ms, std::string* err);
   size_t device_bytes_in_use();
+  // handles created and deleted (budget evictions) since construction
+  void counters(long long* created, long long* evicted);
   // create handles for a shape up front so that the first requests of that
   // shape do not pay for their creation; returns how many were created
   int reserve(int config, int nx, int ny, int nimages, int count, std::string* err);
+
+  // A batch of standalone acquisitions of uneven shapes (every item processed
+  // like a submit()ted volume).  Items are grouped by (config, shape); each
+  // group is cut into chunks that a worker runs back to back on one handle
+  // with the upload of the next item and the download of the previous one
+  // overlapped with the computation (SIM_Reconstructor::process_series in its
+  // standalone form), and the workers run chunks of different shapes
+  // concurrently, largest first.  Blocks until every item is done; returns 0,
+  // or -1 with the first failing item's error.
+  struct BatchItem {
+    int config, nx, ny, nimages;
+    const void* raw;
+    bool u16;
+    float* out;
+  };
+  int run_batch(const std::vector<BatchItem>& items, std::string* err);
 
  private:
   using Key = std::tuple<int, int, int, int>;  // config, nx, ny, nimages
   struct Request {
     long long ticket;
     Key key;
-    const void* raw;
+    std::vector<const void*> raws;  // one volume, or a chunk of a batch
     bool u16;
-    float* out;
+    std::vector<float*> outs;
     double t_submit;
   };
   struct Done {
@@ -63,6 +81,7 @@ class ReconServer {
   };
   void worker_loop();
   Handle* acquire(const Key& k, std::string* err);
+  long long enqueue(Request r);
   void release(Handle* h);
 
   std::vector<std::string> configs_;
@@ -73,6 +92,7 @@ class ReconServer {
   std::vector<std::unique_ptr<Handle>> handles_;
   size_t budget_, in_use_ = 0;
   long long next_ticket_ = 1;
+  long long created_ = 0, evicted_ = 0;
   bool stop_ = false;
   std::vector<std::thread> workers_;
 };

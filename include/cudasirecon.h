@@ -266,7 +266,25 @@ int SRX_serverWait(SRX_Server* s, long long ticket, double* latency_ms);
  * created otherwise by the first request that finds none idle, which then
  * pays for the device allocation).  Returns how many were created. */
 int SRX_serverReserve(SRX_Server* s, int config, int nx, int ny, int nimages, int count);
+/* A batch of standalone acquisitions of uneven shapes and configurations (2D
+ * and 3D mixed), each processed exactly like a submitted request.  Items are
+ * grouped by (config, shape); each group runs in chunks on pooled handles, a
+ * chunk's volumes back to back with the upload of the next and the download
+ * of the previous overlapped with the computation, and chunks of different
+ * shapes run concurrently on the workers' streams, largest first.  Blocks
+ * until every item is done.  Returns 0, or -1 (SR_getLastError: the first
+ * failing item's error; the other items are still processed). */
+typedef struct SRX_BatchItem {
+  int config;          /* SRX_serverAddConfig id */
+  int nx, ny, nimages; /* the SR_new_from_shape shape */
+  const void* raw;     /* [nimages][ny][nx], uint16 when raw_is_u16 else float */
+  int raw_is_u16;
+  float* out;          /* the SR_getResult layout */
+} SRX_BatchItem;
+int SRX_serverRunBatch(SRX_Server* s, const SRX_BatchItem* items, int n);
 size_t SRX_serverDeviceBytes(SRX_Server* s);
+/* Handles created, and handles deleted to stay within the budget, so far. */
+void SRX_serverCounters(SRX_Server* s, long long* created, long long* evicted);
 void SRX_serverDestroy(SRX_Server* s);
 
 /* makeotf.  The reference's makeotf is a program, not a library call

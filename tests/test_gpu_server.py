@@ -69,3 +69,36 @@ def test_server_rejects_unknown_config():
     with pytest.raises(sr.SIReconError):
         srv.submit(5, raw, np.zeros(4, np.float32))
     srv.close()
+
+
+def synthetic_case(nx, nz, twod, seed):
+    from cudasirecon_gb300 import synthetic as syn
+    o = syn.Optics(nphases=3 if twod else 5)
+    raw = syn.simulate(nx, nx, nz, o, seed=seed, n_filaments=10).raw
+    otf = syn.ra_otf(o, nx_psf=128, nz_psf=64, norders=2 if twod else 3, twod=twod)
+    cfg = syn.config_text(o, twod=twod, extra={"wiener": 0.00048828125} if twod else None)
+    return {"nx": nx, "ny": nx, "raw": [raw], "config": cfg, "otf": otf}
+
+
+def test_batch_uneven_matches_plain():
+    """SRX_serverRunBatch over a 2D/3D mix of uneven shapes (radix-2, -3 and -5
+    line lengths): every item equals the plain flow's volume, whether its
+    chunk ran as a single volume or back to back with overlapped copies."""
+    cases = {n: load(n)[0] for n in CASES}
+    cases["s3d_384x16"] = synthetic_case(384, 16, False, 11)
+    cases["s2d_640"] = synthetic_case(640, 1, True, 12)
+    want = {n: plain(c) for n, c in cases.items()}
+    srv = sr.Server(workers=2)
+    cfg = {n: srv.add_config(c["config"], c["otf"]) for n, c in cases.items()}
+    items, names = [], []
+    for rep in range(3):  # groups of 3 on 2 workers: chunks of 2 and of 1
+        for n, c in cases.items():
+            items.append((cfg[n], np.ascontiguousarray(c["raw"][0]), np.zeros(want[n].shape, np.float32)))
+            names.append(n)
+    srv.run_batch(items)
+    for n, (_, _, out) in zip(names, items):
+        assert np.array_equal(out, want[n]), n
+    # an invalid item fails the call before anything runs
+    with pytest.raises(sr.SIReconError):
+        srv.run_batch([(99, items[0][1], items[0][2])])
+    srv.close()
