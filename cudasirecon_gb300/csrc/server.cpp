@@ -97,16 +97,18 @@ int ReconServer::run_batch(const std::vector<BatchItem>& items, std::string* err
     }
   }
   // chunks: a group of g items is cut into about one chunk per worker, at
-  // most kMaxChunk items each (a chunk holds one handle for its whole run)
+  // most kMaxChunk items each (a chunk holds one handle for its whole run);
+  // groups of up to four items stay one chunk (one handle, copies overlapped)
   constexpr size_t kMaxChunk = 16;
   const size_t nw = workers_.size();
-  struct Chunk {
-    Request r;
-    double cost;
+  struct Group {
+    std::vector<Request> chunks;
+    double cost = 0;
   };
-  std::vector<Chunk> chunks;
+  std::vector<Group> order;
   for (auto& [gk, idx] : groups) {
-    const size_t per = std::min(kMaxChunk, std::max<size_t>(1, (idx.size() + nw - 1) / nw));
+    const size_t per = std::min(kMaxChunk, std::max((idx.size() + nw - 1) / nw, std::min<size_t>(idx.size(), 4)));
+    Group g;
     for (size_t a = 0; a < idx.size(); a += per) {
       Request r{0, Key{std::get<0>(gk), std::get<1>(gk), std::get<2>(gk), std::get<3>(gk)}, {}, std::get<4>(gk), {},
                 now_s()};
@@ -114,14 +116,18 @@ int ReconServer::run_batch(const std::vector<BatchItem>& items, std::string* err
         r.raws.push_back(items[idx[j]].raw);
         r.outs.push_back(items[idx[j]].out);
       }
-      const double cost = (double)std::get<1>(gk) * std::get<2>(gk) * std::get<3>(gk) * r.raws.size();
-      chunks.push_back({std::move(r), cost});
+      g.cost += (double)std::get<1>(gk) * std::get<2>(gk) * std::get<3>(gk) * r.raws.size();
+      g.chunks.push_back(std::move(r));
     }
+    order.push_back(std::move(g));
   }
-  // largest first, so that the last chunks to start are short ones
-  std::stable_sort(chunks.begin(), chunks.end(), [](const Chunk& a, const Chunk& b) { return a.cost > b.cost; });
+  // groups largest first (the last to start are short), each group's chunks
+  // together: a finished group's handles become the least recently used, so
+  // under a tight budget they are the ones deleted for the next group's
+  std::stable_sort(order.begin(), order.end(), [](const Group& a, const Group& b) { return a.cost > b.cost; });
   std::vector<long long> tickets;
-  for (auto& c : chunks) tickets.push_back(enqueue(std::move(c.r)));
+  for (auto& g : order)
+    for (auto& c : g.chunks) tickets.push_back(enqueue(std::move(c)));
   int rc = 0;
   for (long long t : tickets) {
     std::string e;

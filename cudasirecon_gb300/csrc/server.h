@@ -46,8 +46,9 @@ class ReconServer {
   // with the upload of the next item and the download of the previous one
   // overlapped with the computation (SIM_Reconstructor::process_series in its
   // standalone form), and the workers run chunks of different shapes
-  // concurrently, largest first.  Blocks until every item is done; returns 0,
-  // or -1 with the first failing item's error.
+  // concurrently, groups largest first with each group's chunks together.
+  // Blocks until every item is done; returns 0, or -1 with the first failing
+  // item's error.
   struct BatchItem {
     int config, nx, ny, nimages;
     const void* raw;

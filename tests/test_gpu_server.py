@@ -91,8 +91,12 @@ def test_batch_uneven_matches_plain():
     srv = sr.Server(workers=2)
     cfg = {n: srv.add_config(c["config"], c["otf"]) for n, c in cases.items()}
     items, names = [], []
-    for rep in range(3):  # groups of 3 on 2 workers: chunks of 2 and of 1
+    # three items of most shapes (one chunk, run back to back with overlapped
+    # copies) and one of the 2D 640^2 shape (the single-volume flow)
+    for rep in range(3):
         for n, c in cases.items():
+            if n == "s2d_640" and rep > 0:
+                continue
             items.append((cfg[n], np.ascontiguousarray(c["raw"][0]), np.zeros(want[n].shape, np.float32)))
             names.append(n)
     srv.run_batch(items)
