@@ -981,7 +981,9 @@ void SIM_Reconstructor::fit_direction(int direction)
     }
   } else {
     for (int order = 1; order < norders_; ++order)
-      amp_[direction][order] = findrealspacemodamp(direction, 0, order, k0_[direction].x, k0_[direction].y, 1);
+      amp_[direction][order] = pre_amp_valid_ ? pre_amp_[direction][order]
+                                              : findrealspacemodamp(direction, 0, order, k0_[direction].x,
+                                                                    k0_[direction].y, 1);
   }
   if (ip.nz == 1)
     for (int order = 2; order < norders_; ++order)
@@ -1014,8 +1016,49 @@ void SIM_Reconstructor::fit_all()
   cudaEvent_t a;
   long long l0;
   stage_begin("fit", &a, &l0);
+  const ReconParams& p = opt.p;
+  const ImageParams& ip = opt.ip;
+  const bool reuse = ip.ntimes > 1 && ip.curTimeIdx > 0 && p.bUseTime0k0;
+  // no direction searches: every direction's modamps are findrealspacemodamp
+  // at its k0, evaluated here back to back with one synchronisation
+  if (reuse || !p.bSearchforvector) modamps_at_k0(reuse);
   for (int d = 0; d < ndirs_; ++d) fit_direction(d);
+  pre_amp_valid_ = false;
   stage_end("fit", a, l0);
+}
+
+// findrealspacemodamp(d, 0, order, k0) for every direction and order (the
+// no-search branch of fit_direction): the same launches in the same stream
+// order as the per-call path, each result copied to its own slot of the
+// pinned host buffer, one synchronisation at the end
+void SIM_Reconstructor::modamps_at_k0(bool reuse)
+{
+  pre_amp_.assign(ndirs_, std::vector<float2v>(norders_, float2v{0, 0}));
+  int slot = 0;
+  for (int d = 0; d < ndirs_; ++d) {
+    const float2v k = reuse ? k0_[d] : k0guess_[d];
+    for (int order = 1; order < norders_; ++order, ++slot) {
+      build_overlaps(d, 0, order, k.x, k.y);
+      const float2 kc = make_float2(k.x * order, k.y * order);
+      check(cudaMemcpyAsync(d_kcand_, &kc, sizeof(float2), cudaMemcpyHostToDevice, stream_), "cand");
+      check_launch(launch_modamp_candidates(d_pmap_, nx_, ny_, opt.ip.dxy, d_kcand_, 1, d_tables_, d_partial_,
+                                            d_xstary_, stream_, &launches_),
+                   "modamp");
+      check(cudaMemcpyAsync(h_pinned_ + 4 * slot, d_xstary_, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream_),
+            "d2h");
+      check(cudaMemcpyAsync(h_pinned_ + 4 * slot + 2, d_sumxy_, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream_),
+            "d2h");
+    }
+  }
+  check(cudaStreamSynchronize(stream_), "modamp");
+  slot = 0;
+  for (int d = 0; d < ndirs_; ++d)
+    for (int order = 1; order < norders_; ++order, ++slot) {
+      const float sx = (float)h_pinned_[4 * slot + 2];
+      pre_amp_[d][order] = float2v{(float)h_pinned_[4 * slot] / sx, (float)h_pinned_[4 * slot + 1] / sx};
+    }
+  cur_o1_ = cur_o2_ = -1;
+  pre_amp_valid_ = true;
 }
 
 // ------------------------------------------------------ filter + assembly

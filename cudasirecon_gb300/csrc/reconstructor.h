@@ -82,6 +82,7 @@ class SIM_Reconstructor {
   void findk0(int d);
   void fitk0andmodamps(int d);
   float2v findrealspacemodamp(int d, int o1, int o2, float k0x, float k0y, int redo);
+  void modamps_at_k0(bool reuse);
   void prefetch_line(int o1, int o2, bool angle_axis, float fixed, float start, float step, int count, int dir);
 
   // geometry
@@ -141,6 +142,9 @@ class SIM_Reconstructor {
   std::vector<float> noisevar_;
   std::vector<float2v> k0_, k0_time0_, k0guess_;
   std::vector<std::vector<float2v>> amp_;
+  // modamps of the no-search branch, evaluated for all directions at once
+  std::vector<std::vector<float2v>> pre_amp_;
+  bool pre_amp_valid_ = false;
   bool raw_u16_ = false;
   bool have_raw_ = false;
   bool rescaled_ = false;
