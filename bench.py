@@ -157,6 +157,19 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def ncu_limiter(kernel):
+    """The committed full ncu capture's issue-active and DRAM-throughput
+    percentages for `kernel` (what bounds it when DRAM is not the limit), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            e = json.load(f).get(kernel)
+    except Exception:
+        return None
+    if not e or "issue_active_pct" not in e:
+        return None
+    return {k: e[k] for k in ("issue_active_pct", "dram_throughput_pct", "sm_throughput_pct", "full_capture") if k in e}
+
+
 def ncu_traffic(kernel, workload, alg_bytes_per_launch):
     """DRAM bytes per launch of `kernel` from the committed ncu summary
     (profiles/ncu_traffic.json), or None.  A capture taken on a smaller
@@ -295,7 +308,8 @@ def run_gb300(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
                 "frac": round(ach / peak, 4), "peak_source": peak_kind,
                 "traffic": tr, "alg_bytes_per_launch": st["alg_bytes"] / max(1, st["launches"]),
                 "avg_launch_ms": st["ms"] / max(1, st["launches"]),
-                "share_of_step": round(st["ms"] / max(prof_ms, 1e-9), 4)}
+                "share_of_step": round(st["ms"] / max(prof_ms, 1e-9), 4),
+                "ncu_full_capture": ncu_limiter(name)}
     line = {
         "metric": "Recon output Mvoxels/s (SIM 3-beam, 512x512x48x15 -> 1024x1024x48)",
         "value": round(value, 1), "unit": "Mvoxels/s", "n_gpus": world, "steps": args.steps,
