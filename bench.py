@@ -62,6 +62,12 @@ def barrier(dist):
         dist.barrier()
 
 
+def weak_mvox_per_s(world, steps, outvox, seconds):
+    """Whole-job throughput of independent replicas: every rank reconstructs
+    `steps` volumes of `outvox` output voxels; `seconds` is the max over ranks."""
+    return world * steps * outvox / seconds / 1e6
+
+
 def max_over_ranks(dist, v):
     if dist is None:
         return v
@@ -240,7 +246,7 @@ def run_gb300(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
     prof_ms = r.bench_device(args.steps)
     prof = r.profile()
     r.set_profiling(False)
-    value = world * args.steps * outvox / (dev_ms / 1e3) / 1e6
+    value = weak_mvox_per_s(world, args.steps, outvox, dev_ms / 1e3)
     # ---- end to end through the C ABI from pinned host memory
     host = [np.ascontiguousarray(v) for v in vols]
     out = np.empty(r.out_shape, np.float32)
@@ -290,11 +296,11 @@ def run_gb300(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
     for h in host + outs2:
         sr.unpin(h)
     sr.unpin(out)
-    e2e_plain = world * args.steps * outvox / e2e_s / 1e6
+    e2e_plain = weak_mvox_per_s(world, args.steps, outvox, e2e_s)
     # the series numbers its volumes t0, t0+1, ...: for a time-series
     # workload (k0 reused from t = 0) that is the same work as `value`; a
     # workload that searches k0 on every volume keeps the plain path
-    e2e = world * args.steps * outvox / (e2e_series_s if reuse else e2e_s) / 1e6
+    e2e = weak_mvox_per_s(world, args.steps, outvox, e2e_series_s if reuse else e2e_s)
     # ---- roofline of the dominant kernel
     kern = prof.get("kernels", {})
     top = max(kern.items(), key=lambda kv: kv[1]["ms"]) if kern else None
@@ -325,8 +331,8 @@ def run_gb300(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
                 "api": ("SRX_processSeries (uploads/downloads overlapped with computation), pinned host buffers"
                         if reuse else "plain SR_* calls per volume (k0 searched on every volume), pinned host buffers"),
                 "plain_value": round(e2e_plain, 1), "plain_latency": latency,
-                "repeats_mvox_per_s": {"series": [round(world * args.steps * outvox / v / 1e6, 1) for v in series_s],
-                                       "plain": [round(world * args.steps * outvox / v / 1e6, 1) for v in plain_s]},
+                "repeats_mvox_per_s": {"series": [round(weak_mvox_per_s(world, args.steps, outvox, v), 1) for v in series_s],
+                                       "plain": [round(weak_mvox_per_s(world, args.steps, outvox, v), 1) for v in plain_s]},
                 "plain_api": "SR_setRawU16 -> SR_loadAndRescaleImage -> SR_processOneVolume -> SR_getResult"},
         "gpu_launches": int(launches),
         "clocks": clk,
