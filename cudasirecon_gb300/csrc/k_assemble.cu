@@ -40,13 +40,6 @@ __device__ __forceinline__ float dev_suppress(float x)
   return 1.f / (1 + 20000 / (x6 + 20));  // float division: correctly rounded, like the double one rounded
 }
 
-__device__ __forceinline__ float dev_order0damping(float radius, float zindex, float rlimit, int zlimit)
-{
-  float rfraction = radius / rlimit;
-  float zfraction = fabsf(zindex / zlimit);
-  return rfraction * rfraction + zfraction * zfraction * zfraction;
-}
-
 // Per-launch constants derived on the host from FilterArgs (reciprocals and
 // products the per-term arithmetic would otherwise recompute per element).
 struct FilterK {
@@ -82,10 +75,15 @@ __device__ __forceinline__ float2 filter_otf(const FilterArgs& a, const float2* 
   return otf_lookup_rr<CLAMP>(a.otf.otf[o], a.otf, krindex, kzi);
 }
 
-template <int ND, int NO, bool CLAMP, bool TAB>
+// FL >= 0: the suppress (bit 0), dampen-order-0 (bit 1) and filter-overlaps
+// (bit 2) switches fixed at compile time; FL < 0: read from the arguments
+template <int ND, int NO, bool CLAMP, bool TAB, int FL>
 __device__ __forceinline__ float2 filter_scale(const FilterArgs& a, const FilterK& k, int order, int z0, float rdist1, float x1f,
                                float y1f, const float2* tabz)
 {
+  const bool suppress = FL >= 0 ? (FL & 1) != 0 : a.suppress != 0;
+  const bool dampen0 = FL >= 0 ? (FL & 2) != 0 : a.dampen0 != 0;
+  const bool filteroverlaps = FL >= 0 ? (FL & 4) != 0 : a.filteroverlaps != 0;
   const int dir = a.dir;
   const int nd = ND ? ND : a.ndirs, no = NO ? NO : a.norders;
   const float xabs = x1f + k.kxo[dir * no + order], yabs = y1f + k.kyo[dir * no + order];
@@ -97,11 +95,11 @@ __device__ __forceinline__ float2 filter_scale(const FilterArgs& a, const Filter
   float weight = otf1.x * otf1.x + otf1.y * otf1.y;
   if (order != 0) weight *= a.ampmag2[dir * no + order];
   float dampfact = k.rnv[dir * no + order];
-  if (a.suppress && order != 0 && rdist1 <= k.supp_r)
+  if (suppress && order != 0 && rdist1 <= k.supp_r)
     dampfact *= dev_suppress(rdist1 * k.rmin_dkr);
-  else if (!a.dampen0 && a.suppress && order == 0 && rdist1 <= k.supp_r)
+  else if (!dampen0 && suppress && order == 0 && rdist1 <= k.supp_r)
     dampfact *= dev_suppress(rdist1 * k.rmin_dkr);
-  else if (a.dampen0 && order == 0) {
+  else if (dampen0 && order == 0) {
     const float rf = rdist1 * k.rrcut;
     dampfact *= rf * rf + zf3;
   }
@@ -113,7 +111,7 @@ __device__ __forceinline__ float2 filter_scale(const FilterArgs& a, const Filter
 #pragma unroll
     for (int order2 = -(no - 1); order2 < no; order2++) {
       if (dir2 == dir && order2 == order) continue;
-      if (!a.filteroverlaps && !(order2 == 0 && order == 0)) continue;
+      if (!filteroverlaps && !(order2 == 0 && order == 0)) continue;
       const int ao2 = order2 < 0 ? -order2 : order2;
       const float sx = order2 < 0 ? -k.kxo[dir2 * no + ao2] : k.kxo[dir2 * no + ao2];
       const float sy = order2 < 0 ? -k.kyo[dir2 * no + ao2] : k.kyo[dir2 * no + ao2];
@@ -124,11 +122,11 @@ __device__ __forceinline__ float2 filter_scale(const FilterArgs& a, const Filter
       if (rdist2 < a.rdistcutoff) {
         const float2 otf2 = filter_otf<CLAMP, TAB>(a, tabz, ao2, rdist2 * k.rdkrotf, kzi);
         float w = (otf2.x * otf2.x + otf2.y * otf2.y) * k.termw[dir2 * no + ao2];
-        if (a.suppress && order2 != 0 && rdist2 <= k.supp_r)
+        if (suppress && order2 != 0 && rdist2 <= k.supp_r)
           w *= dev_suppress(rdist2 * k.rmin_dkr);
-        else if (!a.dampen0 && a.suppress && order2 == 0 && rdist2 <= k.supp_r)
+        else if (!dampen0 && suppress && order2 == 0 && rdist2 <= k.supp_r)
           w *= dev_suppress(rdist2 * k.rmin_dkr);
-        else if (a.dampen0 && order2 == 0) {
+        else if (dampen0 && order2 == 0) {
           const float rf = rdist2 * k.rrcut;
           w *= rf * rf + zf3;
         }
@@ -180,7 +178,7 @@ __device__ __forceinline__ void apply_side(float2& re, float2& im, float2 scale,
 // TAB: the block (one kz plane) first builds, in shared memory, each order's
 // OTF interpolated to this plane's kz (+z0) and to the conjugate pass's kz
 // (-z0) along kr: [2][NO][nxotf]; only where no lookup can leave the table
-template <int ND, int NO, bool CLAMP, bool TAB>
+template <int ND, int NO, bool CLAMP, bool TAB, int FL = -1>
 __global__ void __launch_bounds__(kThreads) k_filter(const __grid_constant__ FilterArgs a, const __grid_constant__ FilterK k)
 {
   extern __shared__ float2 tab[];
@@ -226,7 +224,7 @@ __global__ void __launch_bounds__(kThreads) k_filter(const __grid_constant__ Fil
     if (b2) b2[ind] = make_float2(0.f, 0.f);
     return;
   }
-  float2 s1 = filter_scale<ND, NO, CLAMP, TAB>(a, k, order, z0, rdist1, x1f, y1f, tab);
+  float2 s1 = filter_scale<ND, NO, CLAMP, TAB, FL>(a, k, order, z0, rdist1, x1f, y1f, tab);
   if (order == 0) {
     b1[ind] = cmul(b1[ind], s1);
     return;
@@ -239,7 +237,7 @@ __global__ void __launch_bounds__(kThreads) k_filter(const __grid_constant__ Fil
     const int x2 = -jin;
     float x2f = x2 * a.dkx, y2f = y2 * a.dky;
     float rdist2 = sqrtf(x2f * x2f + y2f * y2f);
-    float2 s2 = filter_scale<ND, NO, CLAMP, TAB>(a, k, order, -z0, rdist2, x2f, y2f, tab + (TAB ? NO * a.otf.nxotf : 0));
+    float2 s2 = filter_scale<ND, NO, CLAMP, TAB, FL>(a, k, order, -z0, rdist2, x2f, y2f, tab + (TAB ? NO * a.otf.nxotf : 0));
     apply_side(re, im, cmul(s2, a.conjamp[order]), true);
   }
   b1[ind] = re;
@@ -713,10 +711,25 @@ int launch_filter(const FilterArgs& a, cudaStream_t s, long long* launches)
   // tables fit in 48 KB of shared memory
   const size_t tabb = 2 * (size_t)no * a.otf.nxotf * sizeof(float2);
   const bool tab = !clamp && tabb <= 48 * 1024;
-  if (a.ndirs == 3 && a.norders == 3 && tab) k_filter<3, 3, false, true><<<g, kThreads, tabb, s>>>(a, k);
+  // the table path with the three switches fixed at compile time
+  const int fl = (a.suppress ? 1 : 0) | (a.dampen0 ? 2 : 0) | (a.filteroverlaps ? 4 : 0);
+  auto tab_path = [&]<int NO>() {
+    auto go = [&]<int FL>() { k_filter<3, NO, false, true, FL><<<g, kThreads, tabb, s>>>(a, k); };
+    switch (fl) {
+      case 0: go.template operator()<0>(); break;
+      case 1: go.template operator()<1>(); break;
+      case 2: go.template operator()<2>(); break;
+      case 3: go.template operator()<3>(); break;
+      case 4: go.template operator()<4>(); break;
+      case 5: go.template operator()<5>(); break;
+      case 6: go.template operator()<6>(); break;
+      default: go.template operator()<7>(); break;
+    }
+  };
+  if (a.ndirs == 3 && a.norders == 3 && tab) tab_path.template operator()<3>();
   else if (a.ndirs == 3 && a.norders == 3 && !clamp) k_filter<3, 3, false, false><<<g, kThreads, 0, s>>>(a, k);
   else if (a.ndirs == 3 && a.norders == 3) k_filter<3, 3, true, false><<<g, kThreads, 0, s>>>(a, k);
-  else if (a.ndirs == 3 && a.norders == 2 && tab) k_filter<3, 2, false, true><<<g, kThreads, tabb, s>>>(a, k);
+  else if (a.ndirs == 3 && a.norders == 2 && tab) tab_path.template operator()<2>();
   else if (a.ndirs == 3 && a.norders == 2 && !clamp) k_filter<3, 2, false, false><<<g, kThreads, 0, s>>>(a, k);
   else if (a.ndirs == 3 && a.norders == 2) k_filter<3, 2, true, false><<<g, kThreads, 0, s>>>(a, k);
   else k_filter<0, 0, true, false><<<g, kThreads, 0, s>>>(a, k);
