@@ -20,7 +20,7 @@ EXE = os.path.join(ROOT, "cudasirecon_gb300", "bin", "cudasirecon")
 
 def run_cli(args):
     r = subprocess.run([EXE] + args, capture_output=True, text=True, timeout=300)
-    # like the reference, the driver reports errors and still exits with 0
+    # like the reference's cudaSireconDriver, the program reports errors and still exits with 0
     assert r.returncode == 0 and "Error" not in r.stderr, r.stderr
     return r
 

@@ -1,7 +1,7 @@
 """GPU parity: the CUDA reconstruction through the C ABI against the golden
 outputs of the reference's own kernels (tests/golden) and the FP64 oracle.
 
-Tolerances (spec bar): volume rel-L2 <= 1e-4 and max-abs <= 1e-3 of
+Tolerances (the parity bar): volume rel-L2 <= 1e-4 and max-abs <= 1e-3 of
 the peak; k0 within 1e-3 px; modamps within 1e-3.
 """
 import warnings

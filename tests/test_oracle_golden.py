@@ -3,7 +3,7 @@
 The fixtures in tests/golden were produced by tests/golden/make_golden.py on a
 GB300 with the reference's gpuFunctionsImpl.cu compiled unmodified
 (oracle/ref_harness).  Tolerances are those the oracle must meet to serve as
-the parity checker: volume rel-L2 <= 2e-5 (spec bar 1e-4), k0 within
+the parity checker: volume rel-L2 <= 2e-5 (parity bar 1e-4), k0 within
 1e-4 px, modamps within 1e-5.
 """
 import warnings
