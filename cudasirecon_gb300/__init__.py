@@ -101,6 +101,10 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.SRX_serverRunBatch.restype = ip
     lib.SRX_serverRunBatch.argtypes = [vp, C.POINTER(BatchItem), ip]
     lib.SRX_serverDeviceBytes.restype = C.c_size_t
+    lib.SRX_serverSetK0Reuse.restype = ip
+    lib.SRX_serverSetK0Reuse.argtypes = [vp, ip, ip]
+    lib.SRX_serverRecordedK0.restype = ip
+    lib.SRX_serverRecordedK0.argtypes = [vp, ip, C.POINTER(C.c_float), ip]
     lib.SRX_serverCounters.restype = None
     lib.SRX_serverCounters.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
     lib.SRX_serverDeviceBytes.argtypes = [vp]
@@ -477,6 +481,17 @@ class Server:
 
     def device_bytes(self) -> int:
         return int(self.lib.SRX_serverDeviceBytes(self.h))
+
+    def set_k0_reuse(self, config: int, on: bool = True) -> None:
+        """Keep the first request's fitted k0 for the configuration's later
+        requests (SRX_serverSetK0Reuse)."""
+        if self.lib.SRX_serverSetK0Reuse(self.h, config, int(on)) != 0:
+            raise SIReconError(_err(self.lib))
+
+    def recorded_k0(self, config: int, ndirs: int = 3):
+        k0 = np.zeros((ndirs, 2), np.float32)
+        ok = self.lib.SRX_serverRecordedK0(self.h, config, k0.ctypes.data_as(C.POINTER(C.c_float)), ndirs)
+        return k0 if ok else None
 
     def counters(self) -> dict:
         """Handles created, and deleted to stay within the budget, so far."""

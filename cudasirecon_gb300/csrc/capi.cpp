@@ -358,6 +358,30 @@ int SRX_serverRunBatch(SRX_Server* s, const SRX_BatchItem* items, int n)
   return rc;
 }
 
+int SRX_serverSetK0Reuse(SRX_Server* s, int config, int on)
+{
+  if (!s) {
+    g_last_error = "SRX_serverSetK0Reuse: null server";
+    return -1;
+  }
+  int rc = -1;
+  guarded([&] {
+    std::string err;
+    rc = ((simrecon::ReconServer*)s)->set_k0_reuse(config, on != 0, &err);
+    if (rc != 0) g_last_error = err;
+  });
+  return rc;
+}
+
+int SRX_serverRecordedK0(SRX_Server* s, int config, float* k0, int ndirs)
+{
+  if (!s || !k0) return 0;
+  std::vector<float> v;
+  if (!((simrecon::ReconServer*)s)->recorded_k0(config, &v)) return 0;
+  for (int i = 0; i < 2 * ndirs && i < (int)v.size(); ++i) k0[i] = v[i];
+  return 1;
+}
+
 void SRX_serverCounters(SRX_Server* s, long long* created, long long* evicted)
 {
   if (s) ((simrecon::ReconServer*)s)->counters(created, evicted);

@@ -393,8 +393,11 @@ __global__ void __launch_bounds__(kThreads) k_asm_x(AssembleArgs a, const int* _
 // Four-step variant of k_asm_y (col_fft.cuh) for zoomed column lengths with
 // a column configuration: 8 output columns of one slot per CTA, band values
 // loaded straight from HBM during the first stage.
+// At most 128 registers (two CTAs per SM): left to its own heuristic the
+// compiler has given this kernel 191 registers (one CTA per SM, 1.78 instead
+// of 1.00 ms per 512^2 x 48 volume) after an unrelated change to its arguments.
 template <int Y>
-__global__ void __launch_bounds__(kThreads) k_asm_y4(AssembleArgs a, const Slot* __restrict__ slots,
+__global__ void __launch_bounds__(kThreads, 2) k_asm_y4(AssembleArgs a, const Slot* __restrict__ slots,
                                                     const float2* __restrict__ tw)
 {
   constexpr int R1 = colfft_r1(Y), W = 8;
@@ -600,7 +603,7 @@ __global__ void __launch_bounds__(kThreads) k_asm_z1(const float4* __restrict__ 
 // (c, k1) runs the inverse 16-point DFT and stores the real part of planes
 // k1 + R1 k2.
 template <int R1>
-__global__ void __launch_bounds__(kThreads) k_asm_z4(AssembleArgs a, const unsigned char* __restrict__ zactive,
+__global__ void __launch_bounds__(kThreads, 2) k_asm_z4(AssembleArgs a, const unsigned char* __restrict__ zactive,
                                                     const float2* __restrict__ tw)
 {
   constexpr int R2 = 16, W = 64;
@@ -764,8 +767,10 @@ int launch_fill(float* buf, size_t n, float v, cudaStream_t s, long long* launch
 }
 
 // The slot tables live in a small per-call device buffer carved from T's
-// tail: the host fills them with cudaMemcpyAsync from pageable memory, which
-// is synchronous with respect to the host but ordered on the stream.
+// tail: the host fills them with cudaMemcpyAsync from pageable memory.  Small
+// pageable copies are ordered on the stream without waiting for the copy
+// engines, which other handles' large transfers may be occupying; copies from
+// page-locked memory would queue behind those.
 int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
 {
   FFTPlan py, px, pz;

@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(kThreads) k_ovl_y_accum(OverlapArgs a, FFTPlan
 // stage 2 gives each thread one (column, k1) of both, and conj(X)Y, |X|^2,
 // |Y|^2 accumulate in registers over the planes.
 template <int N, int R1>
-__global__ void __launch_bounds__(kThreads) k_ovl_y4(OverlapArgs a, const float2* __restrict__ tw,
+__global__ void __launch_bounds__(kThreads, 2) k_ovl_y4(OverlapArgs a, const float2* __restrict__ tw,
                                                     int planes_per_group)
 {
   using CF = ColFft<N, R1, 8>;
@@ -676,6 +676,24 @@ int launch_crosscorr_peak(const float2* pmap, float2* cc, int nx, int ny, float*
   // pmap in, cc out; cc in and out (columns); cc in (argmax)
   if (kt) kt->end("k_crosscorr", s, 5.0 * nx * ny * sizeof(float2));
   if (launches) *launches += 4;
+  return (int)cudaGetLastError();
+}
+
+namespace {
+__global__ void k_copy_out(const unsigned* __restrict__ s1, unsigned* d1, int n1, const unsigned* __restrict__ s2,
+                           unsigned* d2, int n2)
+{
+  for (int i = threadIdx.x; i < n1; i += blockDim.x) d1[i] = s1[i];
+  for (int i = threadIdx.x; i < n2; i += blockDim.x) d2[i] = s2[i];
+}
+}  // namespace
+
+int launch_copy_out(const void* src1, void* dst1, size_t n1, const void* src2, void* dst2, size_t n2, cudaStream_t s,
+                    long long* launches)
+{
+  k_copy_out<<<1, 128, 0, s>>>((const unsigned*)src1, (unsigned*)dst1, (int)n1, (const unsigned*)src2, (unsigned*)dst2,
+                               (int)n2);
+  if (launches) *launches += 1;
   return (int)cudaGetLastError();
 }
 

@@ -93,6 +93,11 @@ int launch_crosscorr_peak(const float2* pmap, float2* cc, int nx, int ny, float*
                           float* peak, cudaStream_t s, long long* launches);
 
 // XStarY[c] = sum_xy pmap(x,y) exp(i 2pi ((x - nx/2) kx_c + (y - ny/2) ky_c) dxy), c < ncand
+// Copies n1 and n2 4-byte words from device memory to (mapped, page-locked)
+// host memory with one small kernel: results of a few bytes reach the host
+// without queueing on the copy engines behind other streams' large transfers.
+int launch_copy_out(const void* src1, void* dst1, size_t n1, const void* src2, void* dst2, size_t n2, cudaStream_t s,
+                    long long* launches);
 int launch_modamp_candidates(const float2* pmap, int nx, int ny, float dxy, const float2* kcand /* device */,
                              int ncand, float2* tables, double* partial, double* xstary, cudaStream_t s,
                              long long* launches);

@@ -464,7 +464,8 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
     *r.ptr = arena_ + off;
     off += align_up(r.bytes, 256);
   }
-  check(cudaMallocHost((void**)&h_pinned_, 4096), "cudaMallocHost");
+  check(cudaHostAlloc((void**)&h_pinned_, 4096, cudaHostAllocMapped), "cudaHostAlloc");
+  check(cudaHostGetDevicePointer((void**)&dh_pinned_, h_pinned_, 0), "cudaHostGetDevicePointer");
   std::vector<float> fact(kMaxApo, 0.f);
   for (int l = 0; l < p.napodize; ++l) fact[l] = 1.0 - sinf((l + 0.5) / (float)p.napodize * M_PI * 0.5);
   check(cudaMemcpy(d_apofact_, fact.data(), kMaxApo * sizeof(float), cudaMemcpyHostToDevice), "upload");
@@ -740,9 +741,9 @@ void SIM_Reconstructor::eval_candidates(int o1, int o2, const std::vector<std::p
     check_launch(launch_modamp_candidates(d_pmap_, nx_, ny_, opt.ip.dxy, d_kcand_, (int)nc, d_tables_, d_partial_,
                                           d_xstary_, stream_, &launches_),
                  "modamp");
-    check(cudaMemcpyAsync(h_pinned_, d_xstary_, nc * 2 * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
-    check(cudaMemcpyAsync(h_pinned_ + 2 * kMaxCand, d_sumxy_, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream_),
-          "d2h");
+    check_launch(launch_copy_out(d_xstary_, dh_pinned_, nc * 4, d_sumxy_, dh_pinned_ + 2 * kMaxCand, 4, stream_,
+                                 &launches_),
+                 "d2h");
     check(cudaStreamSynchronize(stream_), "modamp");
     sumx_ = h_pinned_[2 * kMaxCand];
     sumy_ = h_pinned_[2 * kMaxCand + 1];
@@ -793,8 +794,7 @@ float2v SIM_Reconstructor::findrealspacemodamp(int d, int o1, int o2, float k0x,
   check_launch(launch_modamp_candidates(d_pmap_, nx_, ny_, opt.ip.dxy, d_kcand_, 1, d_tables_, d_partial_,
                                         d_xstary_, stream_, &launches_),
                "modamp");
-  check(cudaMemcpyAsync(h_pinned_, d_xstary_, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
-  check(cudaMemcpyAsync(h_pinned_ + 2, d_sumxy_, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream_), "d2h");
+  check_launch(launch_copy_out(d_xstary_, dh_pinned_, 4, d_sumxy_, dh_pinned_ + 2, 4, stream_, &launches_), "d2h");
   check(cudaStreamSynchronize(stream_), "modamp");
   float sx = (float)h_pinned_[2];
   return float2v{(float)h_pinned_[0] / sx, (float)h_pinned_[1] / sx};
@@ -809,7 +809,7 @@ void SIM_Reconstructor::findk0(int d)
   check_launch(launch_crosscorr_peak(d_pmap_, d_cc_, nx_, ny_, d_bval_, d_bidx_, d_peak_, stream_, &launches_),
                "crosscorr");
   float* pk = (float*)(h_pinned_ + 256);
-  check(cudaMemcpyAsync(pk, d_peak_, 7 * sizeof(float), cudaMemcpyDeviceToHost, stream_), "d2h");
+  check_launch(launch_copy_out(d_peak_, dh_pinned_ + 256, 7, nullptr, nullptr, 0, stream_, &launches_), "d2h");
   check(cudaStreamSynchronize(stream_), "findk0");
   int xcent = (int)pk[0], ycent = (int)pk[1];
   float peakx = fitparabola(pk[2], pk[3], pk[4]) + xcent;
@@ -1044,10 +1044,9 @@ void SIM_Reconstructor::modamps_at_k0(bool reuse)
       check_launch(launch_modamp_candidates(d_pmap_, nx_, ny_, opt.ip.dxy, d_kcand_, 1, d_tables_, d_partial_,
                                             d_xstary_, stream_, &launches_),
                    "modamp");
-      check(cudaMemcpyAsync(h_pinned_ + 4 * slot, d_xstary_, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream_),
-            "d2h");
-      check(cudaMemcpyAsync(h_pinned_ + 4 * slot + 2, d_sumxy_, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream_),
-            "d2h");
+      check_launch(launch_copy_out(d_xstary_, dh_pinned_ + 4 * slot, 4, d_sumxy_, dh_pinned_ + 4 * slot + 2, 4, stream_,
+                                   &launches_),
+                   "d2h");
     }
   }
   check(cudaStreamSynchronize(stream_), "modamp");
@@ -1191,6 +1190,14 @@ int SIM_Reconstructor::get_band(int dir, int b, float* out)
         "getBand");
   check(cudaStreamSynchronize(stream_), "getBand");
   return 0;
+}
+
+void SIM_Reconstructor::set_fitted_k0(const float* k0)
+{
+  for (int d = 0; d < ndirs_; ++d) {
+    k0_[d] = float2v{k0[2 * d], k0[2 * d + 1]};
+    k0_time0_[d] = k0_[d];
+  }
 }
 
 void SIM_Reconstructor::get_fit(float* k0, float* amps) const

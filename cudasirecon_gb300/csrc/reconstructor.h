@@ -46,6 +46,9 @@ class SIM_Reconstructor {
   void write_result(int it, int iw);
   void close_files();
   int ntimes() const { return opt.ip.ntimes; }
+  void set_ntimes(int n) { opt.ip.ntimes = (short)n; }
+  // the k0 of every direction as if time point 0 had fitted it (k0[2 d], k0[2 d + 1])
+  void set_fitted_k0(const float* k0);
 
   // introspection / performance
   void get_fit(float* k0, float* amps) const;
@@ -135,7 +138,10 @@ class SIM_Reconstructor {
   cudaStream_t h2d_stream_ = nullptr, d2h_stream_ = nullptr;
   cudaEvent_t ev_raw_ready_[2] = {nullptr, nullptr}, ev_raw_free_[2] = {nullptr, nullptr};
   cudaEvent_t ev_out_ready_[2] = {nullptr, nullptr}, ev_out_free_[2] = {nullptr, nullptr};
-  double* h_pinned_ = nullptr;  // small pinned host buffer for results of the fit
+  // small page-locked host buffer for results of the fit, mapped into the
+  // device's address space (dh_pinned_) so that kernels write the results
+  double* h_pinned_ = nullptr;
+  double* dh_pinned_ = nullptr;
 
   // host-side state (ReconData equivalents)
   std::vector<float> sepmat_;

@@ -49,6 +49,7 @@ int ReconServer::add_config(const std::string& config_path)
 {
   std::lock_guard<std::mutex> lk(mu_);
   configs_.push_back(config_path);
+  cstate_.emplace_back();
   return (int)configs_.size() - 1;
 }
 
@@ -175,6 +176,26 @@ int ReconServer::reserve(int config, int nx, int ny, int nimages, int count, std
   return (int)got.size();
 }
 
+int ReconServer::set_k0_reuse(int config, bool on, std::string* err)
+{
+  std::lock_guard<std::mutex> lk(mu_);
+  if (config < 0 || config >= (int)configs_.size()) {
+    *err = "setK0Reuse: unknown configuration";
+    return -1;
+  }
+  cstate_[config].reuse_k0 = on;
+  cstate_[config].k0.clear();
+  return 0;
+}
+
+bool ReconServer::recorded_k0(int config, std::vector<float>* k0)
+{
+  std::lock_guard<std::mutex> lk(mu_);
+  if (config < 0 || config >= (int)configs_.size() || cstate_[config].k0.empty()) return false;
+  *k0 = cstate_[config].k0;
+  return true;
+}
+
 size_t ReconServer::device_bytes_in_use()
 {
   std::lock_guard<std::mutex> lk(mu_);
@@ -281,13 +302,34 @@ void ReconServer::worker_loop()
     } else {
       try {
         const int nx = std::get<1>(r.key), ny = std::get<2>(r.key), ni = std::get<3>(r.key);
+        const int cfg = std::get<0>(r.key);
+        bool reuse = false, record = false;
+        std::vector<float> k0;
+        {
+          std::lock_guard<std::mutex> lk(mu_);
+          reuse = cstate_[cfg].reuse_k0 && !cstate_[cfg].k0.empty();
+          record = cstate_[cfg].reuse_k0 && cstate_[cfg].k0.empty();
+          if (reuse) k0 = cstate_[cfg].k0;
+        }
         if (r.raws.size() == 1) {  // the plain per-volume flow
           if (r.u16) h->sr->set_raw_u16((const uint16_t*)r.raws[0], nx, ny, ni);
           else h->sr->set_raw_float((const float*)r.raws[0], nx, ny, ni);
           h->sr->load_and_rescale(0, 0);
-          h->sr->set_cur_time(0);
+          if (reuse) {  // a later time point: the recorded k0, modamps fitted
+            h->sr->set_fitted_k0(k0.data());
+            if (h->sr->ntimes() < 2) h->sr->set_ntimes(2);
+            h->sr->set_cur_time(1);
+          } else {
+            h->sr->set_cur_time(0);
+          }
           h->sr->process_one_volume();
           h->sr->get_result(r.outs[0]);
+          if (record) {
+            std::vector<float> fk(2 * kMaxDirs);
+            h->sr->get_fit(fk.data(), nullptr);
+            std::lock_guard<std::mutex> lk(mu_);
+            if (cstate_[cfg].reuse_k0 && cstate_[cfg].k0.empty()) cstate_[cfg].k0 = fk;
+          }
         } else {
           h->sr->process_series(r.raws.data(), r.u16, r.outs.data(), (int)r.raws.size(), 0, true);
         }

@@ -33,6 +33,14 @@ class ReconServer {
   // blocks until the request is done; latency = submission to result in
   // host memory.  Returns 0, or -1 with the request's error.
   int wait(long long ticket, double* latency_ms, std::string* err);
+  // k0 reuse per configuration (off by default): the first request of the
+  // configuration to finish searches k0 as usual and records it; every later
+  // request of that configuration is processed like a later time point of a
+  // series (the recorded k0 reused, modamps fitted, bleach correction against
+  // its own planes), whatever its shape.  Turning it on clears the record.
+  int set_k0_reuse(int config, bool on, std::string* err);
+  // the recorded k0 of a configuration (2 floats per direction); false if none
+  bool recorded_k0(int config, std::vector<float>* k0);
   size_t device_bytes_in_use();
   // handles created and deleted (budget evictions) since construction
   void counters(long long* created, long long* evicted);
@@ -86,6 +94,11 @@ class ReconServer {
   void release(Handle* h);
 
   std::vector<std::string> configs_;
+  struct ConfigState {
+    bool reuse_k0 = false;
+    std::vector<float> k0;  // empty until recorded
+  };
+  std::vector<ConfigState> cstate_;
   std::mutex mu_;
   std::condition_variable cv_work_, cv_done_;
   std::deque<Request> queue_;

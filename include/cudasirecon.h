@@ -283,6 +283,18 @@ typedef struct SRX_BatchItem {
 } SRX_BatchItem;
 int SRX_serverRunBatch(SRX_Server* s, const SRX_BatchItem* items, int n);
 size_t SRX_serverDeviceBytes(SRX_Server* s);
+/* k0 kept per acquisition configuration (off by default).  With it on, the
+ * first submitted request of the configuration to finish searches k0 as
+ * usual and the server records it; every later submitted request of that
+ * configuration, of any shape, is processed like a later time point of a
+ * series with time-0 k0 reuse (cudaSirecon.cpp:296-301: k0 kept, modamps
+ * fitted) -- the same as SR_setRaw -> SR_loadAndRescaleImage(0) ->
+ * SR_setCurTimeIdx(1) -> SR_processOneVolume on a handle whose time point 0
+ * fitted that k0.  Turning it on clears the record.  Batches
+ * (SRX_serverRunBatch) always search.  RecordedK0 copies 2 floats per
+ * direction (k0x, k0y in 1/um) and returns 1, or returns 0 if none yet. */
+int SRX_serverSetK0Reuse(SRX_Server* s, int config, int on);
+int SRX_serverRecordedK0(SRX_Server* s, int config, float* k0, int ndirs);
 /* Handles created, and handles deleted to stay within the budget, so far. */
 void SRX_serverCounters(SRX_Server* s, long long* created, long long* evicted);
 void SRX_serverDestroy(SRX_Server* s);

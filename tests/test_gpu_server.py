@@ -106,3 +106,41 @@ def test_batch_uneven_matches_plain():
     with pytest.raises(sr.SIReconError):
         srv.run_batch([(99, items[0][1], items[0][2])])
     srv.close()
+
+
+def test_server_k0_reuse_is_a_later_time_point():
+    """k0 kept per configuration: the first request searches k0 and the server
+    records it; the next request of the configuration is processed like time
+    point 1 of a series whose time point 0 fitted that k0 (k0 kept, modamps
+    fitted, its own bleach correction)."""
+    case, _ = load("c3d_64_ts")
+    raw0, raw1 = (np.ascontiguousarray(case["raw"][t]) for t in (0, 1))
+    r = sr.Reconstructor(case["nx"], case["ny"], raw0.shape[0], case["config"], case["otf"])
+    r.set_ntimes(2)
+    want = []
+    for t, raw in enumerate((raw0, raw1)):
+        r.set_raw(raw)
+        r.load_and_rescale(0, 0)
+        r.set_cur_time(t)
+        r.process()
+        want.append(r.result().copy())
+        if t == 0:
+            k0_t0 = r.fit()[0]
+    r.close()
+    srv = sr.Server(workers=2)
+    cid = srv.add_config(case["config"], case["otf"])
+    srv.set_k0_reuse(cid, True)
+    assert srv.recorded_k0(cid) is None
+    outs = [np.zeros(w.shape, np.float32) for w in want]
+    srv.wait(srv.submit(cid, raw0, outs[0]))
+    assert np.array_equal(srv.recorded_k0(cid), k0_t0)
+    srv.wait(srv.submit(cid, raw1, outs[1]))
+    assert np.array_equal(outs[0], want[0])
+    assert np.array_equal(outs[1], want[1])
+    # reuse off again: the request searches k0 like a standalone volume
+    srv.set_k0_reuse(cid, False)
+    out = np.zeros(want[1].shape, np.float32)
+    srv.wait(srv.submit(cid, raw1, out))
+    assert np.array_equal(out, plain({"raw": [raw1], "nx": case["nx"], "ny": case["ny"], "config": case["config"],
+                                      "otf": case["otf"]}))
+    srv.close()
