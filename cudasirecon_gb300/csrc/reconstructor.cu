@@ -473,6 +473,7 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
   check(cudaMemcpy(d_otf_, hotf.data(), hotf.size() * sizeof(float2), cudaMemcpyHostToDevice), "upload");
   check(cudaMemset(d_sdp0_, 0, (size_t)nz_ * sizeof(double)), "memset");
   check(cudaMemset(d_spec_, 0, nspec * sizeof(float2)), "memset");
+  if (p.bUsecorr && !load_corr(err)) return false;
   return true;
 }
 
@@ -494,6 +495,7 @@ SIM_Reconstructor::~SIM_Reconstructor()
   if (d_out_extra_) cudaFree(d_out_extra_);
   if (arena_) cudaFree(arena_);
   if (d_flush_) cudaFree(d_flush_);
+  if (d_bgslope_) cudaFree(d_bgslope_);
   if (h_pinned_) cudaFreeHost(h_pinned_);
   if (stream_) cudaStreamDestroy(stream_);
 }
@@ -612,8 +614,8 @@ void SIM_Reconstructor::ingest()
   ia.ndirs = ndirs_;
   ia.nphases = nph_;
   ia.fastSI = opt.p.bFastSIM;
-  ia.bg = nullptr;
-  ia.slope = nullptr;
+  ia.bg = d_bgslope_;
+  ia.slope = d_bgslope_ ? d_bgslope_ + (size_t)nx_ * ny_ : nullptr;
   ia.bgconst = opt.p.constbkgd;
   ia.bgextra = 0.f;
   ia.inscale = opt.ip.inscale;
@@ -1190,6 +1192,36 @@ int SIM_Reconstructor::get_band(int dir, int b, float* out)
         "getBand");
   check(cudaStreamSynchronize(stream_), "getBand");
   return 0;
+}
+
+// bgAndSlope / getbg_and_slope (cudaSirecon.cpp:139-192): with usecorr the
+// per-pixel background and slope come from the two first sections of an MRC
+// calibration file of the data's nx x ny; ingest applies
+// (raw - background) * slope * inscale instead of the constant background
+bool SIM_Reconstructor::load_corr(std::string* err)
+{
+  const std::string& path = opt.p.corrfiles;
+  MrcFile f;
+  std::string e;
+  if (!mrc_open(path, &f, &e)) {
+    *err = "File " + path + " does not exist";
+    return false;
+  }
+  if (f.hdr.nx != nx_ || f.hdr.ny != ny_ || f.hdr.nz < 2) {
+    *err = "calibration file " + path + " has different dimension than data file";
+    return false;
+  }
+  std::vector<float> bg, sl;
+  if (!mrc_read_section(f, 0, &bg, err) || !mrc_read_section(f, 1, &sl, err)) return false;
+  const size_t n = (size_t)nx_ * ny_;
+  if (bg.size() != n || sl.size() != n) {
+    *err = "calibration file " + path + ": sections are not real nx x ny images";
+    return false;
+  }
+  if (!d_bgslope_) check(cudaMalloc((void**)&d_bgslope_, 2 * n * sizeof(float)), "calibration buffer");
+  check(cudaMemcpy(d_bgslope_, bg.data(), n * sizeof(float), cudaMemcpyHostToDevice), "calibration upload");
+  check(cudaMemcpy(d_bgslope_ + n, sl.data(), n * sizeof(float), cudaMemcpyHostToDevice), "calibration upload");
+  return true;
 }
 
 void SIM_Reconstructor::set_fitted_k0(const float* k0)

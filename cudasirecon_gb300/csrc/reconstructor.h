@@ -60,7 +60,10 @@ class SIM_Reconstructor {
   void reset_profile();
   long long launches() const { return launches_; }
   size_t out_elems() const { return (size_t)X_ * Y_ * Z_; }
-  size_t device_bytes() const { return arena_bytes_ + series_bytes_; }  // device memory the handle holds
+  size_t device_bytes() const  // device memory the handle holds
+  {
+    return arena_bytes_ + series_bytes_ + (d_bgslope_ ? 2 * (size_t)nx_ * ny_ * sizeof(float) : 0);
+  }
 
   simrecon::Options opt;  // ReconParams + ImageParams live here (references handed out)
 
@@ -68,6 +71,7 @@ class SIM_Reconstructor {
   SIM_Reconstructor() = default;
   bool setup(int nx, int ny, int nimages, int nwaves, const simrecon::Stack* otf, std::string* err);
   bool load_otf_tiff(const std::string& path, simrecon::Stack* out, std::string* err);
+  bool load_corr(std::string* err);
   void stage_raw(const void* raw, bool u16);
   void ingest();
   void separate();
@@ -105,6 +109,7 @@ class SIM_Reconstructor {
   float2* d_spec_ = nullptr;
   float* d_scale_ = nullptr;
   double* d_sdp0_ = nullptr;
+  float* d_bgslope_ = nullptr;  // usecorr: per-pixel background then slope, [2][ny][nx]
   float* d_sepmat_ = nullptr;
   float* d_apofact_ = nullptr;
   float2* d_otf_ = nullptr;
