@@ -62,3 +62,46 @@ def test_cli_reports_missing_otf(tmp_path):
     r = subprocess.run([EXE, str(data), "cell", str(tmp_path / "missing_otf.tif")], capture_output=True, text=True,
                        timeout=120)
     assert r.returncode == 0 and "Error" in r.stderr
+
+
+def write_mrc(path, stack, dxy, dz, wave):
+    """float32 [nz][ny][nx] as a DV/MRC file with the pixel sizes and the wavelength in the header"""
+    import struct
+    nz, ny, nx = stack.shape
+    h = bytearray(1024)
+    struct.pack_into("<4i", h, 0, nx, ny, nz, 2)
+    struct.pack_into("<3f", h, 40, dxy, dxy, dz)
+    struct.pack_into("<3i", h, 64, 1, 2, 3)
+    struct.pack_into("<h", h, 96, -16224)
+    struct.pack_into("<hh", h, 196, 1, wave)
+    with open(path, "wb") as f:
+        f.write(bytes(h))
+        f.write(np.ascontiguousarray(stack, np.float32).tobytes())
+
+
+def read_mrc(path):
+    import struct
+    with open(path, "rb") as f:
+        h = f.read(1024)
+        nx, ny, nz, mode = struct.unpack_from("<4i", h, 0)
+        nxt = struct.unpack_from("<i", h, 92)[0]
+        f.read(max(nxt, 0))
+        assert mode == 2
+        return np.frombuffer(f.read(4 * nx * ny * nz), np.float32).reshape(nz, ny, nx), h
+
+
+def test_cli_mrc_input_and_output_match_reference(tmp_path):
+    case, ref = load("c3d_64")
+    inp, out = tmp_path / "cell.dv", tmp_path / "cell_proc.dv"
+    write_mrc(inp, case["raw"][0].astype(np.float32), 0.08, 0.125, 528)
+    otf = tmp_path / "otf.tif"
+    sr.load_library()
+    sr.write_tiff_float(str(otf), case["otf"])
+    cfg = tmp_path / "config"
+    cfg.write_text(case["config"])
+    run_cli([str(inp), str(out), str(otf), "-c", str(cfg)])
+    got, hdr = read_mrc(out)
+    want = ref["result"][0]
+    assert got.shape == want.shape
+    assert rel_l2(got, want) < 1e-4
+    assert np.abs(got - want).max() / np.abs(want).max() < 1e-3
