@@ -99,6 +99,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.SRX_serverReserve.restype = ip
     lib.SRX_serverReserve.argtypes = [vp, ip, ip, ip, ip, ip]
     lib.SRX_serverRunBatch.restype = ip
+    lib.SRX_batchPlan.restype = ip
+    lib.SRX_batchPlan.argtypes = [C.POINTER(BatchItem), ip, ip, C.POINTER(C.c_int)]
     lib.SRX_serverRunBatch.argtypes = [vp, C.POINTER(BatchItem), ip]
     lib.SRX_serverDeviceBytes.restype = C.c_size_t
     lib.SRX_serverSetK0Reuse.restype = ip

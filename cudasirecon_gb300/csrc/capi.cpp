@@ -387,6 +387,26 @@ void SRX_serverCounters(SRX_Server* s, long long* created, long long* evicted)
   if (s) ((simrecon::ReconServer*)s)->counters(created, evicted);
 }
 
+int SRX_batchPlan(const SRX_BatchItem* items, int n, int workers, int* chunk_of_item)
+{
+  if (n < 0 || (n > 0 && (!items || !chunk_of_item))) {
+    g_last_error = "SRX_batchPlan: invalid arguments";
+    return -1;
+  }
+  int nchunks = -1;
+  guarded([&] {
+    std::vector<simrecon::ReconServer::BatchItem> v((size_t)n);
+    for (int i = 0; i < n; ++i)
+      v[i] = {items[i].config, items[i].nx, items[i].ny, items[i].nimages, items[i].raw, items[i].raw_is_u16 != 0,
+              items[i].out};
+    const auto plan = simrecon::plan_batch(v, workers < 1 ? 1 : (size_t)workers);
+    for (size_t c = 0; c < plan.size(); ++c)
+      for (size_t i : plan[c]) chunk_of_item[i] = (int)c;
+    nchunks = (int)plan.size();
+  });
+  return nchunks;
+}
+
 size_t SRX_serverDeviceBytes(SRX_Server* s) { return s ? ((simrecon::ReconServer*)s)->device_bytes_in_use() : 0; }
 
 void SRX_serverDestroy(SRX_Server* s)

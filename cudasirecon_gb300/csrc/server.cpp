@@ -81,10 +81,45 @@ long long ReconServer::enqueue(Request r)
   return t;
 }
 
-int ReconServer::run_batch(const std::vector<BatchItem>& items, std::string* err)
+std::vector<std::vector<size_t>> plan_batch(const std::vector<ReconServer::BatchItem>& items, size_t workers)
 {
   // group by (config, shape, input type); a group keeps the caller's order
   std::map<std::tuple<int, int, int, int, bool>, std::vector<size_t>> groups;
+  for (size_t i = 0; i < items.size(); ++i) {
+    const ReconServer::BatchItem& it = items[i];
+    groups[{it.config, it.nx, it.ny, it.nimages, it.u16}].push_back(i);
+  }
+  // chunks: a group of g items is cut into about one chunk per worker, at
+  // most kMaxChunk items each (a chunk holds one handle for its whole run);
+  // groups of up to four items stay one chunk (one handle, copies overlapped)
+  constexpr size_t kMaxChunk = 16;
+  const size_t nw = std::max<size_t>(1, workers);
+  struct Group {
+    std::vector<std::vector<size_t>> chunks;
+    double cost = 0;
+  };
+  std::vector<Group> order;
+  for (auto& [gk, idx] : groups) {
+    const size_t per = std::min(kMaxChunk, std::max((idx.size() + nw - 1) / nw, std::min<size_t>(idx.size(), 4)));
+    Group g;
+    for (size_t a = 0; a < idx.size(); a += per) {
+      g.chunks.emplace_back(idx.begin() + a, idx.begin() + std::min(idx.size(), a + per));
+      g.cost += (double)std::get<1>(gk) * std::get<2>(gk) * std::get<3>(gk) * g.chunks.back().size();
+    }
+    order.push_back(std::move(g));
+  }
+  // groups largest first (the last to start are short), each group's chunks
+  // together: a finished group's handles become the least recently used, so
+  // under a tight budget they are the ones deleted for the next group's
+  std::stable_sort(order.begin(), order.end(), [](const Group& a, const Group& b) { return a.cost > b.cost; });
+  std::vector<std::vector<size_t>> chunks;
+  for (auto& g : order)
+    for (auto& c : g.chunks) chunks.push_back(std::move(c));
+  return chunks;
+}
+
+int ReconServer::run_batch(const std::vector<BatchItem>& items, std::string* err)
+{
   {
     std::lock_guard<std::mutex> lk(mu_);
     for (size_t i = 0; i < items.size(); ++i) {
@@ -94,41 +129,18 @@ int ReconServer::run_batch(const std::vector<BatchItem>& items, std::string* err
         *err = "runBatch: invalid item " + std::to_string(i);
         return -1;
       }
-      groups[{it.config, it.nx, it.ny, it.nimages, it.u16}].push_back(i);
     }
   }
-  // chunks: a group of g items is cut into about one chunk per worker, at
-  // most kMaxChunk items each (a chunk holds one handle for its whole run);
-  // groups of up to four items stay one chunk (one handle, copies overlapped)
-  constexpr size_t kMaxChunk = 16;
-  const size_t nw = workers_.size();
-  struct Group {
-    std::vector<Request> chunks;
-    double cost = 0;
-  };
-  std::vector<Group> order;
-  for (auto& [gk, idx] : groups) {
-    const size_t per = std::min(kMaxChunk, std::max((idx.size() + nw - 1) / nw, std::min<size_t>(idx.size(), 4)));
-    Group g;
-    for (size_t a = 0; a < idx.size(); a += per) {
-      Request r{0, Key{std::get<0>(gk), std::get<1>(gk), std::get<2>(gk), std::get<3>(gk)}, {}, std::get<4>(gk), {},
-                now_s()};
-      for (size_t j = a; j < std::min(idx.size(), a + per); ++j) {
-        r.raws.push_back(items[idx[j]].raw);
-        r.outs.push_back(items[idx[j]].out);
-      }
-      g.cost += (double)std::get<1>(gk) * std::get<2>(gk) * std::get<3>(gk) * r.raws.size();
-      g.chunks.push_back(std::move(r));
-    }
-    order.push_back(std::move(g));
-  }
-  // groups largest first (the last to start are short), each group's chunks
-  // together: a finished group's handles become the least recently used, so
-  // under a tight budget they are the ones deleted for the next group's
-  std::stable_sort(order.begin(), order.end(), [](const Group& a, const Group& b) { return a.cost > b.cost; });
   std::vector<long long> tickets;
-  for (auto& g : order)
-    for (auto& c : g.chunks) tickets.push_back(enqueue(std::move(c)));
+  for (const auto& c : plan_batch(items, workers_.size())) {
+    const BatchItem& f = items[c[0]];
+    Request r{0, Key{f.config, f.nx, f.ny, f.nimages}, {}, f.u16, {}, now_s()};
+    for (size_t i : c) {
+      r.raws.push_back(items[i].raw);
+      r.outs.push_back(items[i].out);
+    }
+    tickets.push_back(enqueue(std::move(r)));
+  }
   int rc = 0;
   for (long long t : tickets) {
     std::string e;

@@ -111,4 +111,12 @@ class ReconServer {
   std::vector<std::thread> workers_;
 };
 
+// The batch schedule run_batch uses: the items grouped by (config, nx, ny,
+// nimages, input type), each group cut into chunks (about one per worker, at
+// most 16 items, groups of up to four items whole), groups ordered by
+// nx * ny * nimages * items, largest first, each group's chunks together.
+// Returns the chunks in execution order, each a list of item indices in the
+// caller's order.
+std::vector<std::vector<size_t>> plan_batch(const std::vector<ReconServer::BatchItem>& items, size_t workers);
+
 }  // namespace simrecon

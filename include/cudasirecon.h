@@ -282,6 +282,10 @@ typedef struct SRX_BatchItem {
   float* out;          /* the SR_getResult layout */
 } SRX_BatchItem;
 int SRX_serverRunBatch(SRX_Server* s, const SRX_BatchItem* items, int n);
+/* The schedule SRX_serverRunBatch would use for these items with `workers`
+ * workers, without running it (no GPU needed): chunk_of_item[i] = the chunk
+ * (in execution order) of item i; returns the number of chunks, or -1. */
+int SRX_batchPlan(const SRX_BatchItem* items, int n, int workers, int* chunk_of_item);
 size_t SRX_serverDeviceBytes(SRX_Server* s);
 /* k0 kept per acquisition configuration (off by default).  With it on, the
  * first submitted request of the configuration to finish searches k0 as
