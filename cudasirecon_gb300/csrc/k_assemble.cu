@@ -603,7 +603,7 @@ __global__ void __launch_bounds__(kThreads) k_asm_z1(const float4* __restrict__ 
 // (c, k1) runs the inverse 16-point DFT and stores the real part of planes
 // k1 + R1 k2.
 template <int R1>
-__global__ void __launch_bounds__(kThreads, 2) k_asm_z4(AssembleArgs a, const unsigned char* __restrict__ zactive,
+__global__ void __launch_bounds__(kThreads) k_asm_z4(AssembleArgs a, const unsigned char* __restrict__ zactive,
                                                     const float2* __restrict__ tw)
 {
   constexpr int R2 = 16, W = 64;

@@ -521,7 +521,7 @@ int launch_ingest(const IngestArgs& a, cudaStream_t s, long long* launches)
 // DFT of each band times W_nz^(j k1); stage 2: the thread for (c, band, k1)
 // runs the 16-point DFT over j and stores planes k1 + R1 k2 in place.
 template <int R1, int NPH>
-__global__ void __launch_bounds__(kThreads, 2) k_separate4(float2* spec, const float* __restrict__ scale,
+__global__ void __launch_bounds__(kThreads) k_separate4(float2* spec, const float* __restrict__ scale,
                                                        const float* __restrict__ sepmat, int ny, int nxh,
                                                        const float2* __restrict__ tw)
 {
