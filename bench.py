@@ -11,14 +11,21 @@ Mvoxels/s.
 
   value : steps x output voxels / device time with the raw stack already
           resident in HBM (CUDA events on the library's stream, L2 flushed
-          between steps by writing 256 MiB).
-  e2e   : the same through the C ABI from pinned host memory:
-          SR_setRawU16 (H2D) -> SR_loadAndRescaleImage -> SR_setCurTimeIdx ->
-          SR_processOneVolume -> SR_getResult (D2H), host wall clock.
+          between steps by writing 256 MiB); per-kernel times come from a
+          separate profiled pass of the same steps.
+  e2e   : the same through the C ABI from pinned host memory with every
+          step's upload (377 MB) and download (201 MB) in the timed region:
+          SRX_processSeries (copies overlapped with the computation), median
+          of three repeats; plain_value is the plain SR_* sequence per volume.
 
 --impl reference runs the reference's own CUDA build (gpuFunctionsImpl.cu +
 cuFFT, compiled from the reference sources by oracle/build_ref.py) through
 its SR_* flow on the same workload.
+
+--workload uneven: a 2D/3D batch of 560 acquisitions of 28 shapes through
+SRX_serverRunBatch vs the plain one-at-a-time flow.  --workload serving:
+Poisson arrivals of requests of four configurations through SRX_server*,
+p50/p95/p99 latency and throughput vs the plain flow.
 
 Prints one JSON line (rank 0).  N>1 runs independent replicas (one process
 per GPU, weak scaling: each rank reconstructs its own time points).
