@@ -442,6 +442,8 @@ class Server:
         array of the result size.  Both must stay alive until wait()."""
         if not raw.flags.c_contiguous or not out.flags.c_contiguous or out.dtype != np.float32:
             raise ValueError("raw and out must be C-contiguous, out float32")
+        if raw.dtype not in (np.uint16, np.float32) or raw.ndim != 3:
+            raise ValueError("raw must be a [nimages][ny][nx] uint16 or float32 array")
         nimg, ny, nx = raw.shape
         t = self.lib.SRX_serverSubmit(self.h, config, nx, ny, nimg, raw.ctypes.data, int(raw.dtype == np.uint16),
                                       out.ctypes.data)

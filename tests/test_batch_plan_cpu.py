@@ -61,3 +61,15 @@ def test_plan_single_worker_and_empty_fields():
     assert nch == 2 and chunk == [0] * 16 + [1] * 4     # at most 16 items per chunk
     nch, chunk = plan([(0, 64, 64, 180, True)], 8)
     assert nch == 1 and chunk == [0]
+
+
+def test_server_wrapper_rejects_unsupported_inputs_before_the_library():
+    """Input checks of the Python server wrapper, made before any library call."""
+    srv = sr.Server.__new__(sr.Server)  # no device needed: the checks come first
+    srv._keep = {}
+    with pytest.raises(ValueError):
+        srv.submit(0, np.zeros((15, 8, 8), np.float64), np.zeros(4, np.float32))
+    with pytest.raises(ValueError):
+        srv.submit(0, np.zeros((15, 8, 8), np.uint16), np.zeros(4, np.float64))
+    with pytest.raises(ValueError):
+        srv.submit(0, np.zeros((15, 8, 8), np.uint16)[:, ::2], np.zeros(4, np.float32))
