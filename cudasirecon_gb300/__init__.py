@@ -414,7 +414,7 @@ class Server:
     served concurrently by worker threads over pooled handles, within a
     device-memory budget.  Each request is processed as a time-0 volume."""
 
-    def __init__(self, workers: int = 4, hbm_budget: float = 150e9):
+    def __init__(self, workers: int = 6, hbm_budget: float = 150e9):
         self.lib = load_library()
         self._tmp = tempfile.TemporaryDirectory(prefix="sirecon_srv_")
         self.lib.SR_clearError()
