@@ -73,3 +73,22 @@ def test_server_wrapper_rejects_unsupported_inputs_before_the_library():
         srv.submit(0, np.zeros((15, 8, 8), np.uint16), np.zeros(4, np.float64))
     with pytest.raises(ValueError):
         srv.submit(0, np.zeros((15, 8, 8), np.uint16)[:, ::2], np.zeros(4, np.float32))
+
+
+def test_uneven_workload_crop_keeps_the_section_order():
+    """The uneven benchmark crops one simulated stack to every shape: sections
+    stay in Angle -> Z -> Phase order, the crop is centred, and the photon
+    level is rescaled about the background."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    ndirs, nph, nz, n = 3, 5, 8, 32
+    d, z, p, y, x = np.meshgrid(*[np.arange(k) for k in (ndirs, nz, nph, n, n)], indexing="ij")
+    raw = (100 + d * 10000 + z * 1000 + p * 100 + (y * n + x) % 50).astype(np.uint16).reshape(-1, n, n)
+    c = bench._crop(raw, ndirs, nph, nz, 16, 4, 1000.0)        # peak 1000: values unchanged
+    assert c.shape == (ndirs * 4 * nph, 16, 16) and c.dtype == np.uint16
+    want = raw.reshape(ndirs, nz, nph, n, n)[:, 2:6, :, 8:24, 8:24].reshape(-1, 16, 16)
+    assert np.array_equal(c, want)
+    half = bench._crop(raw, ndirs, nph, nz, 16, 4, 500.0)     # half the photons above the background
+    assert np.array_equal(half, np.rint((want.astype(np.float32) - 100) * 0.5 + 100).astype(np.uint16))
