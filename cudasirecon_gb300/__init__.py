@@ -110,6 +110,12 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.SRX_serverCounters.restype = None
     lib.SRX_serverCounters.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
     lib.SRX_serverDeviceBytes.argtypes = [vp]
+    lib.SRX_serverDeviceBytesHeld.restype = C.c_size_t
+    lib.SRX_serverDeviceBytesHeld.argtypes = [vp]
+    lib.SRX_serverPlannedBytes.restype = C.c_size_t
+    lib.SRX_serverPlannedBytes.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
+    lib.SRX_serverAdmissionWaits.restype = C.c_longlong
+    lib.SRX_serverAdmissionWaits.argtypes = [vp]
     lib.SRX_serverDestroy.argtypes = [vp]
     lib.SRX_makeOTF.restype = ip
     lib.SRX_makeOTF.argtypes = [fp, ip, ip, ip, ip, C.POINTER(C.c_char_p), fp, C.c_size_t, C.POINTER(C.c_int)]
@@ -484,7 +490,19 @@ class Server:
             raise SIReconError(_err(self.lib))
 
     def device_bytes(self) -> int:
+        """Device bytes reserved against the budget (never above it)."""
         return int(self.lib.SRX_serverDeviceBytes(self.h))
+
+    def planned_bytes(self, config: int, nx: int, ny: int, nimages: int) -> int:
+        """Bytes admission reserves for a handle of this configuration and shape."""
+        b = int(self.lib.SRX_serverPlannedBytes(self.h, config, nx, ny, nimages))
+        if b == 0:
+            raise SIReconError(_err(self.lib))
+        return b
+
+    def device_bytes_held(self) -> int:
+        """Device bytes the pooled handles actually hold now."""
+        return int(self.lib.SRX_serverDeviceBytesHeld(self.h))
 
     def set_k0_reuse(self, config: int, on: bool = True) -> None:
         """Keep the first request's fitted k0 for the configuration's later
@@ -501,7 +519,8 @@ class Server:
         """Handles created, and deleted to stay within the budget, so far."""
         c, e = C.c_longlong(0), C.c_longlong(0)
         self.lib.SRX_serverCounters(self.h, C.byref(c), C.byref(e))
-        return {"created": c.value, "evicted": e.value}
+        return {"created": c.value, "evicted": e.value,
+                "admission_waits": int(self.lib.SRX_serverAdmissionWaits(self.h))}
 
     def close(self):
         if self.h:

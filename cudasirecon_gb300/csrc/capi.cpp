@@ -409,6 +409,30 @@ int SRX_batchPlan(const SRX_BatchItem* items, int n, int workers, int* chunk_of_
 
 size_t SRX_serverDeviceBytes(SRX_Server* s) { return s ? ((simrecon::ReconServer*)s)->device_bytes_in_use() : 0; }
 
+size_t SRX_serverDeviceBytesHeld(SRX_Server* s) { return s ? ((simrecon::ReconServer*)s)->device_bytes_held() : 0; }
+
+size_t SRX_serverPlannedBytes(SRX_Server* s, int config, int nx, int ny, int nimages)
+{
+  if (!s) {
+    g_last_error = "SRX_serverPlannedBytes: null server";
+    return 0;
+  }
+  size_t b = 0;
+  std::string e;
+  if (!((simrecon::ReconServer*)s)->planned_bytes(config, nx, ny, nimages, &b, &e)) {
+    g_last_error = e;
+    return 0;
+  }
+  return b;
+}
+
+long long SRX_serverAdmissionWaits(SRX_Server* s)
+{
+  long long w = 0;
+  if (s) ((simrecon::ReconServer*)s)->counters(nullptr, nullptr, &w);
+  return w;
+}
+
 void SRX_serverDestroy(SRX_Server* s)
 {
   guarded([&] { delete (simrecon::ReconServer*)s; });
@@ -420,6 +444,20 @@ int SRX_pinHost(void* ptr, size_t bytes)
   if (e != cudaSuccess) {
     g_last_error = std::string("cudaHostRegister: ") + cudaGetErrorString(e);
     return (int)e;
+  }
+  return 0;
+}
+
+int SRX_deviceMemInfo(size_t* free_bytes, size_t* total_bytes)
+{
+  if (!free_bytes || !total_bytes) {
+    g_last_error = "SRX_deviceMemInfo: null argument";
+    return -1;
+  }
+  cudaError_t e = cudaMemGetInfo(free_bytes, total_bytes);
+  if (e != cudaSuccess) {
+    g_last_error = std::string("SRX_deviceMemInfo: ") + cudaGetErrorString(e);
+    return -1;
   }
   return 0;
 }

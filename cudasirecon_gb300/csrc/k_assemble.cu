@@ -43,7 +43,6 @@ __device__ __forceinline__ float dev_suppress(float x)
 // Per-launch constants derived on the host from FilterArgs (reciprocals and
 // products the per-term arithmetic would otherwise recompute per element).
 struct FilterK {
-  float termw[kMaxDirs * kMaxOrders];  // |amp|^2 / noisevar (order 0: 1 / noisevar)
   float rnv[kMaxDirs * kMaxOrders];    // 1 / noisevar
   float kxo[kMaxDirs * kMaxOrders];    // order * k0x of each direction
   float kyo[kMaxDirs * kMaxOrders];
@@ -76,10 +75,13 @@ __device__ __forceinline__ float2 filter_otf(const FilterArgs& a, const float2* 
 }
 
 // FL >= 0: the suppress (bit 0), dampen-order-0 (bit 1) and filter-overlaps
-// (bit 2) switches fixed at compile time; FL < 0: read from the arguments
+// (bit 2) switches fixed at compile time; FL < 0: read from the arguments.
+// termw: |amp|^2 / noisevar of every (direction, order) (FitDev::termw, in
+// registers on the compile-time paths); ampmag2: |amp|^2 of this band.
 template <int ND, int NO, bool CLAMP, bool TAB, int FL>
-__device__ __forceinline__ float2 filter_scale(const FilterArgs& a, const FilterK& k, int order, int z0, float rdist1, float x1f,
-                               float y1f, const float2* tabz)
+__device__ __forceinline__ float2 filter_scale(const FilterArgs& a, const FilterK& k, const float* termw,
+                                               float ampmag2, int order, int z0, float rdist1, float x1f, float y1f,
+                                               const float2* tabz)
 {
   const bool suppress = FL >= 0 ? (FL & 1) != 0 : a.suppress != 0;
   const bool dampen0 = FL >= 0 ? (FL & 2) != 0 : a.dampen0 != 0;
@@ -93,7 +95,7 @@ __device__ __forceinline__ float2 filter_scale(const FilterArgs& a, const Filter
   const float zf3 = zf * zf * zf;
   float2 otf1 = filter_otf<CLAMP, TAB>(a, tabz, order, rdist1 * k.rdkrotf, kzi);
   float weight = otf1.x * otf1.x + otf1.y * otf1.y;
-  if (order != 0) weight *= a.ampmag2[dir * no + order];
+  if (order != 0) weight *= ampmag2;
   float dampfact = k.rnv[dir * no + order];
   if (suppress && order != 0 && rdist1 <= k.supp_r)
     dampfact *= dev_suppress(rdist1 * k.rmin_dkr);
@@ -121,7 +123,7 @@ __device__ __forceinline__ float2 filter_scale(const FilterArgs& a, const Filter
       const float rdist2 = sqrtf(r2);
       if (rdist2 < a.rdistcutoff) {
         const float2 otf2 = filter_otf<CLAMP, TAB>(a, tabz, ao2, rdist2 * k.rdkrotf, kzi);
-        float w = (otf2.x * otf2.x + otf2.y * otf2.y) * k.termw[dir2 * no + ao2];
+        float w = (otf2.x * otf2.x + otf2.y * otf2.y) * termw[dir2 * no + ao2];
         if (suppress && order2 != 0 && rdist2 <= k.supp_r)
           w *= dev_suppress(rdist2 * k.rmin_dkr);
         else if (!dampen0 && suppress && order2 == 0 && rdist2 <= k.supp_r)
@@ -224,21 +226,34 @@ __global__ void __launch_bounds__(kThreads) k_filter(const __grid_constant__ Fil
     if (b2) b2[ind] = make_float2(0.f, 0.f);
     return;
   }
-  float2 s1 = filter_scale<ND, NO, CLAMP, TAB, FL>(a, k, order, z0, rdist1, x1f, y1f, tab);
+  // the fitted amplitudes' weights, read once per thread
+  constexpr int kTw = ND > 0 && NO > 0 ? ND * NO : 1;
+  float twr[kTw];
+  const float* termw = a.fit->termw;
+  if (ND > 0 && NO > 0) {
+#pragma unroll
+    for (int i = 0; i < kTw; ++i) twr[i] = __ldg(a.fit->termw + i);
+    termw = twr;
+  }
+  const float ampmag2 = __ldg(a.fit->ampmag2 + a.dir * a.norders + order);
+  const float2 amp = __ldg(a.fit->amp + a.dir * a.norders + order);
+  const float2 conjamp = make_float2(amp.x, -amp.y);
+  float2 s1 = filter_scale<ND, NO, CLAMP, TAB, FL>(a, k, termw, ampmag2, order, z0, rdist1, x1f, y1f, tab);
   if (order == 0) {
     b1[ind] = cmul(b1[ind], s1);
     return;
   }
   float2 re = b1[ind], im = b2[ind];
-  apply_side(re, im, cmul(s1, a.conjamp[order]), false);
+  apply_side(re, im, cmul(s1, conjamp), false);
   if (jin >= 1 && jin <= nx / 2 - 1) {
     // second pass: the conjugate pixel (-jin, -y, -z0)
     const int y2 = (iin <= ny / 2) ? -iin : ny - iin;
     const int x2 = -jin;
     float x2f = x2 * a.dkx, y2f = y2 * a.dky;
     float rdist2 = sqrtf(x2f * x2f + y2f * y2f);
-    float2 s2 = filter_scale<ND, NO, CLAMP, TAB, FL>(a, k, order, -z0, rdist2, x2f, y2f, tab + (TAB ? NO * a.otf.nxotf : 0));
-    apply_side(re, im, cmul(s2, a.conjamp[order]), true);
+    float2 s2 = filter_scale<ND, NO, CLAMP, TAB, FL>(a, k, termw, ampmag2, order, -z0, rdist2, x2f, y2f,
+                                                     tab + (TAB ? NO * a.otf.nxotf : 0));
+    apply_side(re, im, cmul(s2, conjamp), true);
   }
   b1[ind] = re;
   b2[ind] = im;
@@ -646,14 +661,14 @@ __global__ void __launch_bounds__(kThreads) k_asm_z4(AssembleArgs a, const unsig
   }
 }
 
-__global__ void k_ramp(const float2* k0, int ndirs, int norders, int X, int Y, float dxyz, float fact, float2* ex,
-                       float2* ey)
+__global__ void k_ramp(const __grid_constant__ K0List k0, int ndirs, int norders, int X, int Y, float dxyz, float fact,
+                       float2* ex, float2* ey)
 {
   int n = ndirs * norders * (X + Y);
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     int ro = t / (X + Y), r = t - ro * (X + Y);
     int d = ro / norders, o = ro - d * norders;
-    float kx = k0[d].x * (float)o, ky = k0[d].y * (float)o;
+    float kx = k0.k[d].x * (float)o, ky = k0.k[d].y * (float)o;
     double ang;
     if (r < X) ang = (double)fact * M_PI * (double)(r - X / 2) * (double)kx * (double)dxyz;
     else ang = (double)fact * M_PI * (double)((r - X) - Y / 2) * (double)ky * (double)dxyz;
@@ -671,15 +686,65 @@ __global__ void k_fill(float* buf, size_t n, float v)
     buf[i] = v;
 }
 
-// per-process device scratch for the small slot tables (re-uploaded per call)
-struct SlotTables {
-  Slot* slots = nullptr;
-  int* p0 = nullptr;
-  int* pn = nullptr;
-  int* pz = nullptr;
-  unsigned char* zact = nullptr;
-  int cap_slots = 0, cap_planes = 0;
+// Host form of an assembly's slot tables: the in-band planes of every
+// (direction, order) band grouped by output plane (move_kernel ranges,
+// gpuFunctionsImpl.cu:1853-1913), the order-0 bands of a plane in one summed
+// slot.  The device copy is laid out as [slots][plane_slot0][plane_nslot]
+// [plane_zout][zactive].
+struct HostTables {
+  std::vector<Slot> slots;
+  std::vector<int> p0, pn, pzo;
+  std::vector<unsigned char> zact;
+  size_t bytes() const
+  {
+    return slots.size() * sizeof(Slot) + 3 * p0.size() * sizeof(int) + zact.size();
+  }
 };
+
+HostTables build_tables(const AssembleArgs& a)
+{
+  HostTables t;
+  const int nz = a.nz;
+  std::vector<int> kzs;  // signed kz planes of the band grid (z in [-nz/2+1, nz/2])
+  if (nz > 1)
+    for (int z = -(nz / 2 - 1); z <= nz / 2; ++z) kzs.push_back(z);
+  else
+    kzs.push_back(0);
+  t.zact.assign(a.Z, 0);
+  for (int kz : kzs) {
+    const int start = (int)t.slots.size();
+    const int az = kz < 0 ? -kz : kz;
+    const int zo = kz < 0 ? kz + a.Z : kz;
+    if (az <= a.zdc[0]) t.slots.push_back(Slot{-1, 0, kz, zo});  // order 0 of all directions, summed
+    for (int d = 0; d < a.ndirs; ++d)
+      for (int o = 1; o < a.norders; ++o)
+        if (az <= a.zdc[o]) t.slots.push_back(Slot{d, o, kz, zo});
+    const int cnt = (int)t.slots.size() - start;
+    if (cnt > 0) {
+      t.p0.push_back(start);
+      t.pn.push_back(cnt);
+      t.pzo.push_back(zo);
+      t.zact[zo] = 1;
+    }
+  }
+  return t;
+}
+
+struct DevTables {
+  Slot* slots;
+  int *p0, *pn, *pz;
+  unsigned char* zact;
+};
+DevTables dev_tables(const AssembleArgs& a, const HostTables& t)
+{
+  DevTables d;
+  d.slots = (Slot*)a.tables;
+  d.p0 = (int*)(d.slots + t.slots.size());
+  d.pn = d.p0 + t.p0.size();
+  d.pz = d.pn + t.p0.size();
+  d.zact = (unsigned char*)(d.pz + t.p0.size());
+  return d;
+}
 
 }  // namespace
 
@@ -693,7 +758,6 @@ int launch_filter(const FilterArgs& a, cudaStream_t s, long long* launches)
     for (int o = 0; o < no; ++o) {
       const int i = d * no + o;
       k.rnv[i] = 1.f / a.noisevar[i];
-      k.termw[i] = o == 0 ? k.rnv[i] : a.ampmag2[i] / a.noisevar[i];
       k.kxo[i] = o * a.k0[d].x;
       k.kyo[i] = o * a.k0[d].y;
     }
@@ -750,9 +814,10 @@ int launch_filter(const FilterArgs& a, cudaStream_t s, long long* launches)
   return (int)cudaGetLastError();
 }
 
-int launch_ramp_tables(const float2* k0, int ndirs, int norders, int X, int Y, float dxyz, float fact, float2* ex,
+int launch_ramp_tables(const K0List& k0, int ndirs, int norders, int X, int Y, float dxyz, float fact, float2* ex,
                        float2* ey, cudaStream_t s, long long* launches)
 {
+  if (ndirs < 1 || ndirs > kMaxDirs) return -1;
   int n = ndirs * norders * (X + Y);
   k_ramp<<<std::min(1024, (n + 255) / 256), 256, 0, s>>>(k0, ndirs, norders, X, Y, dxyz, fact, ex, ey);
   if (launches) *launches += 1;
@@ -766,62 +831,57 @@ int launch_fill(float* buf, size_t n, float v, cudaStream_t s, long long* launch
   return (int)cudaGetLastError();
 }
 
-// The slot tables live in a small per-call device buffer carved from T's
-// tail: the host fills them with cudaMemcpyAsync from pageable memory.  Small
-// pageable copies are ordered on the stream without waiting for the copy
-// engines, which other handles' large transfers may be occupying; copies from
-// page-locked memory would queue behind those.
+// The slot tables live in their own small device buffer, written once per
+// geometry: a launch makes no host-to-device copy, so it never waits behind
+// another stream's large transfer on a copy engine and can be captured in a
+// CUDA graph.
+size_t assemble_tables_bytes(const AssembleArgs& a)
+{
+  // the largest table set of the geometry: every order in band on every plane
+  AssembleArgs full = a;
+  for (int o = 0; o < kMaxOrders; ++o) full.zdc[o] = a.nz;
+  return (build_tables(full).bytes() + 255) / 256 * 256;
+}
+
+int assemble_tables_upload(const AssembleArgs& a)
+{
+  if (!a.tables) return -2;
+  const HostTables t = build_tables(a);
+  if (t.bytes() > assemble_tables_bytes(a)) return -2;
+  const DevTables d = dev_tables(a, t);
+  cudaError_t e = cudaSuccess;
+  auto put = [&](void* dst, const void* src, size_t n) {
+    if (n && e == cudaSuccess) e = cudaMemcpy(dst, src, n, cudaMemcpyHostToDevice);
+  };
+  put(d.slots, t.slots.data(), t.slots.size() * sizeof(Slot));
+  put(d.p0, t.p0.data(), t.p0.size() * sizeof(int));
+  put(d.pn, t.pn.data(), t.pn.size() * sizeof(int));
+  put(d.pz, t.pzo.data(), t.pzo.size() * sizeof(int));
+  put(d.zact, t.zact.data(), t.zact.size());
+  return (int)e;
+}
+
 int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
 {
   FFTPlan py, px, pz;
   if (!get_fft_plan(a.Y, &py) || !get_fft_plan(a.X, &px) || !get_fft_plan(a.Z, &pz)) return -1;
-  const int nx = a.nx, nz = a.nz;
-  // signed kz planes of the band grid (move_kernel: z in [-nz/2+1, nz/2])
-  std::vector<int> kzs;
-  if (nz > 1)
-    for (int z = -(nz / 2 - 1); z <= nz / 2; ++z) kzs.push_back(z);
-  else
-    kzs.push_back(0);
-  // slots per plane
-  std::vector<Slot> slots;
-  std::vector<int> p0, pn, pzo;
-  std::vector<unsigned char> zact(a.Z, 0);
-  for (int kz : kzs) {
-    int start = (int)slots.size();
-    const int az = kz < 0 ? -kz : kz;
-    int zo = kz;
-    if (zo < 0) zo += a.Z;
-    if (az <= a.zdc[0]) slots.push_back(Slot{-1, 0, kz, zo});  // order 0 of all directions, summed
-    for (int d = 0; d < a.ndirs; ++d)
-      for (int o = 1; o < a.norders; ++o)
-        if (az <= a.zdc[o]) slots.push_back(Slot{d, o, kz, zo});
-    int cnt = (int)slots.size() - start;
-    if (cnt > 0) {
-      int zo = kz < 0 ? kz + a.Z : kz;
-      p0.push_back(start);
-      pn.push_back(cnt);
-      pzo.push_back(zo);
-      zact[zo] = 1;
-    }
-  }
-  // device copies of the tables: placed after the T scratch region
+  const int nx = a.nx;
+  // slot tables: built on the host (a few hundred entries), their device copy
+  // uploaded once per geometry by assemble_tables_upload
+  if (!a.tables) return -2;
+  const HostTables tabs = build_tables(a);
+  const std::vector<Slot>& slots = tabs.slots;
+  const std::vector<int>& p0 = tabs.p0;
+  const std::vector<int>& pn = tabs.pn;
+  const DevTables dt = dev_tables(a, tabs);
+  Slot* d_slots = dt.slots;
+  int* d_p0 = dt.p0;
+  int* d_pn = dt.pn;
+  int* d_pz = dt.pz;
+  unsigned char* d_zact = dt.zact;
   const size_t per_slot = (size_t)a.Y * nx;  // complex elements of T per slot
-  size_t table_bytes = slots.size() * sizeof(Slot) + 3 * p0.size() * sizeof(int) + a.Z + 64;
-  size_t table_elems = (table_bytes + sizeof(float2) - 1) / sizeof(float2) + 8;
-  if (a.tcap < per_slot + table_elems) return -2;
-  const size_t tslots = (a.tcap - table_elems) / per_slot;  // slots that fit in T at once
-  char* tail = (char*)(a.T + tslots * per_slot);
-  tail = (char*)(((uintptr_t)tail + 15) & ~(uintptr_t)15);
-  Slot* d_slots = (Slot*)tail;
-  int* d_p0 = (int*)(d_slots + slots.size());
-  int* d_pn = d_p0 + p0.size();
-  int* d_pz = d_pn + p0.size();
-  unsigned char* d_zact = (unsigned char*)(d_pz + p0.size());
-  cudaMemcpyAsync(d_slots, slots.data(), slots.size() * sizeof(Slot), cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(d_p0, p0.data(), p0.size() * sizeof(int), cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(d_pn, pn.data(), pn.size() * sizeof(int), cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(d_pz, pzo.data(), pzo.size() * sizeof(int), cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(d_zact, zact.data(), a.Z, cudaMemcpyHostToDevice, s);
+  if (a.tcap < per_slot) return -2;
+  const size_t tslots = a.tcap / per_slot;  // slots that fit in T at once
   // tile sizes
   int Wy = std::max(1, std::min(32, kMaxElems / a.Y));
   size_t smy = fft_stage_smem(a.Y, Wy, a.Y * (Wy + 1), kThreads);

@@ -502,14 +502,15 @@ constexpr int kCand = 8;  // candidates per pass (register accumulators)
 static_assert(2 * kCand == 16, "k_modamp_partial reduces 16 values per thread");
 
 // ex[c][x] = exp(i 2 pi (x - nx/2) kx_c dxy), ey[c][y] likewise
-__global__ void k_phase_tables(const float2* kc, int ncand, int nx, int ny, float dxy, float2* ex, float2* ey)
+__global__ void k_phase_tables(const __grid_constant__ CandList kc, int ncand, int nx, int ny, float dxy, float2* ex,
+                               float2* ey)
 {
   int n = ncand * (nx + ny);
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     int c = t / (nx + ny), r = t - c * (nx + ny);
     double ang;
-    if (r < nx) ang = 2.0 * M_PI * ((double)r - 0.5 * nx) * (double)kc[c].x * (double)dxy;
-    else ang = 2.0 * M_PI * ((double)(r - nx) - 0.5 * ny) * (double)kc[c].y * (double)dxy;
+    if (r < nx) ang = 2.0 * M_PI * ((double)r - 0.5 * nx) * (double)kc.k[c].x * (double)dxy;
+    else ang = 2.0 * M_PI * ((double)(r - nx) - 0.5 * ny) * (double)kc.k[c].y * (double)dxy;
     double s, co;
     sincos(ang, &s, &co);
     float2 v = make_float2((float)co, (float)s);
@@ -688,6 +689,90 @@ __global__ void k_copy_out(const unsigned* __restrict__ s1, unsigned* d1, int n1
 }
 }  // namespace
 
+namespace {
+// Float arithmetic as the host code does it (compiled without contraction
+// into FMA): products and sums rounded separately, so device-finished
+// amplitudes equal the host-computed ones bit for bit.
+__device__ __forceinline__ float2 cmul_rn(float2 a, float2 b)
+{
+  return make_float2(__fsub_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)),
+                     __fadd_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
+}
+__device__ __forceinline__ float mag2_rn(float2 a) { return __fadd_rn(__fmul_rn(a.x, a.x), __fmul_rn(a.y, a.y)); }
+
+// |amp|^2 and the filter's per-term weights (filterbands, gpuFunctionsImpl.cu:1341-1360)
+__device__ void fit_derived(const FitFinishArgs& a, FitDev* out)
+{
+  for (int i = 0; i < a.ndirs * a.norders; ++i) {
+    const int o = i % a.norders;
+    const float m2 = mag2_rn(out->amp[i]);
+    out->ampmag2[i] = m2;
+    out->termw[i] = o == 0 ? a.rnv[i] : __fdiv_rn(m2, a.noisevar[i]);
+  }
+}
+
+// findModulationVectorsAndPhasesForAllDirections without a k0 search
+// (cudaSirecon.cpp:409-492): amp[o] = XStarY / sum|X|^2 of findrealspacemodamp
+// (gpuFunctionsImpl.cu:1128-1130), then the 2D chaining, forcemodamp and the
+// fitallphases = 0 phase rule, in that order.  One thread: at most 64 values.
+__global__ void k_fit_finish(const double* __restrict__ slots, const __grid_constant__ FitFinishArgs a, FitDev* out)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int no = a.norders;
+  for (int d = 0; d < a.ndirs; ++d) {
+    float2* amp = out->amp + d * no;
+    amp[0] = make_float2(1.f, 0.f);
+    for (int o = 1; o < no; ++o) {
+      const double* sl = slots + (size_t)(d * no + o) * 4;
+      const float sx = __double2float_rn(sl[2]);
+      amp[o] = make_float2(__fdiv_rn(__double2float_rn(sl[0]), sx), __fdiv_rn(__double2float_rn(sl[1]), sx));
+    }
+    if (a.chain2d)
+      for (int o = 2; o < no; ++o) amp[o] = cmul_rn(amp[o], amp[o - 1]);
+    if (a.nforce > 0 && a.forceamp[0] > 0.f)
+      for (int o = 1; o < no; ++o) {
+        const float m = __fsqrt_rn(mag2_rn(amp[o]));
+        const float want = o - 1 < a.nforce ? a.forceamp[o - 1] : 0.f;
+        if (m < want) {
+          const float f = __fdiv_rn(want, m);
+          amp[o] = make_float2(__fmul_rn(amp[o].x, f), __fmul_rn(amp[o].y, f));
+        }
+      }
+    if (!a.fitallphases && no > 1) {
+      const float base = atan2f(amp[1].y, amp[1].x);
+      for (int o = 2; o < no; ++o) {
+        const float phi = __fmul_rn((float)o, base);
+        amp[o] = cmul_rn(make_float2(__fsqrt_rn(mag2_rn(amp[o])), 0.f), make_float2(cosf(phi), sinf(phi)));
+      }
+    }
+  }
+  fit_derived(a, out);
+}
+
+__global__ void k_set_fit(const __grid_constant__ AmpList amps, const __grid_constant__ FitFinishArgs a, FitDev* out)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int i = 0; i < a.ndirs * a.norders; ++i) out->amp[i] = amps.amp[i];
+  fit_derived(a, out);
+}
+}  // namespace
+
+int launch_fit_finish(const double* slots, const FitFinishArgs& a, FitDev* out, cudaStream_t s, long long* launches)
+{
+  if (a.ndirs < 1 || a.ndirs > kMaxDirs || a.norders < 1 || a.norders > kMaxOrders) return -1;
+  k_fit_finish<<<1, 32, 0, s>>>(slots, a, out);
+  if (launches) *launches += 1;
+  return (int)cudaGetLastError();
+}
+
+int launch_set_fit(const AmpList& amps, const FitFinishArgs& a, FitDev* out, cudaStream_t s, long long* launches)
+{
+  if (a.ndirs < 1 || a.ndirs > kMaxDirs || a.norders < 1 || a.norders > kMaxOrders) return -1;
+  k_set_fit<<<1, 32, 0, s>>>(amps, a, out);
+  if (launches) *launches += 1;
+  return (int)cudaGetLastError();
+}
+
 int launch_copy_out(const void* src1, void* dst1, size_t n1, const void* src2, void* dst2, size_t n2, cudaStream_t s,
                     long long* launches)
 {
@@ -697,9 +782,10 @@ int launch_copy_out(const void* src1, void* dst1, size_t n1, const void* src2, v
   return (int)cudaGetLastError();
 }
 
-int launch_modamp_candidates(const float2* pmap, int nx, int ny, float dxy, const float2* kcand, int ncand,
+int launch_modamp_candidates(const float2* pmap, int nx, int ny, float dxy, const CandList& kcand, int ncand,
                              float2* tables, double* partial, double* xstary, cudaStream_t s, long long* launches)
 {
+  if (ncand < 1 || ncand > kMaxCand) return -1;
   float2* ex = tables;
   float2* ey = tables + (size_t)ncand * nx;
   KernelTimer* kt = kernel_timer();

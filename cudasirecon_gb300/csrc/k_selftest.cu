@@ -61,20 +61,25 @@ int launch_fft_selftest(float2* data, int n, int nlines, int inverse, int column
 // ---------------------------------------------------------------------------
 // Allocation-free FFT entry point (SRX_fftLinesNoAlloc).
 //
-// Some callers cannot call cudaMalloc: code that runs while a CUDA stream is
-// being captured into a graph, real-time acquisition loops in microscope
-// control software where an allocation's implicit device synchronisation
-// would stall the camera pipeline, and plug-in hosts (for example a JVM
-// image-analysis application driving this library over JNI) that own the
-// device and forbid allocations outside their own memory pool.  For them
-// this entry point transforms lines with the same kernel as SRX_fftSelfTest
-// but keeps its device staging buffer and its twiddle table in the
-// file-scope array below instead of allocating them.
+// Some callers of this library cannot call cudaMalloc: real-time acquisition
+// loops in microscope control software, where an allocation's implicit device
+// synchronisation would stall the camera pipeline, and plug-in hosts (for
+// example a JVM image-analysis application driving this library over JNI)
+// that own the device and forbid allocations outside their own memory pool.
+// For them this entry point transforms lines with the same kernel as
+// SRX_fftSelfTest but keeps its device staging buffer and its twiddle table in
+// the file-scope array below instead of allocating them.
 //
 // Limits and contract:
+//  * a synchronous host-to-host call: the input is copied from host memory,
+//    transformed and copied back with blocking copies and launches on the
+//    calling thread's default stream; the call returns when the result is in
+//    `out`;
 //  * at most kNoAllocMaxElems complex values (4 Mi floats, 16 MiB of
-//    staging) per call and line lengths up to kNoAllocMaxN; larger requests
-//    are rejected with an error, nothing is transformed;
+//    staging) per call and line lengths up to kNoAllocMaxN; in the column
+//    layout a line must also fit the per-CTA shared-memory limit (lengths up
+//    to 7264 with GB300's 227 KB).  Larger requests are rejected with an
+//    error; nothing is transformed and `out` is not written;
 //  * the array lives in every GPU that loads this library, for the life of
 //    the process, whether or not the entry point is used;
 //  * all calls share the array: calls whose work overlaps on the GPU (from
@@ -176,12 +181,18 @@ extern "C" int SRX_fftLinesNoAlloc(const float* in, float* out, int n, int nline
   p.tw = tw;
   p.twr = P ? twr : nullptr;
   const size_t bytes = (size_t)n * nlines * sizeof(float2);
-  k_noalloc_twiddles<<<(n + 255) / 256, 256>>>(tw, twr, n, P);
-  e = cudaMemcpy(data, in, bytes, cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) return noalloc_fail("SRX_fftLinesNoAlloc: input copy", e);
   int nl = std::max(1, std::min(nlines, kFftElems / (n + 1)));
   while (nlines % nl) --nl;
   size_t sm = selftest_smem(n, nl, columns);
+  int smem_max = 0;
+  e = cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return noalloc_fail("SRX_fftLinesNoAlloc: cudaDeviceGetAttribute", e);
+  if (sm > (size_t)smem_max)
+    return noalloc_fail("SRX_fftLinesNoAlloc: line too long for the column layout (the per-CTA shared-memory "
+                        "limit is exceeded); use the row layout");
+  k_noalloc_twiddles<<<(n + 255) / 256, 256>>>(tw, twr, n, P);
+  e = cudaMemcpy(data, in, bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return noalloc_fail("SRX_fftLinesNoAlloc: input copy", e);
   dispatch_fft_len(kSiteSelfTest, n, [&]<int NF>() {
     if (inverse) {
       allow_dynamic_smem((const void*)k_fft_selftest<+1, NF>, sm);

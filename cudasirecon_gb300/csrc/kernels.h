@@ -92,15 +92,52 @@ int launch_overlaps(OverlapArgs& a, cudaStream_t s, long long* launches);
 int launch_crosscorr_peak(const float2* pmap, float2* cc, int nx, int ny, float* blockval, int* blockidx,
                           float* peak, cudaStream_t s, long long* launches);
 
-// XStarY[c] = sum_xy pmap(x,y) exp(i 2pi ((x - nx/2) kx_c + (y - ny/2) ky_c) dxy), c < ncand
-// Copies n1 and n2 4-byte words from device memory to (mapped, page-locked)
-// host memory with one small kernel: results of a few bytes reach the host
-// without queueing on the copy engines behind other streams' large transfers.
+// Copies n1 and n2 4-byte words with one small kernel: from device memory to
+// (mapped, page-locked) host memory, so that results of a few bytes reach the
+// host without queueing on the copy engines behind other streams' large
+// transfers, or from device to device memory.
 int launch_copy_out(const void* src1, void* dst1, size_t n1, const void* src2, void* dst2, size_t n2, cudaStream_t s,
                     long long* launches);
-int launch_modamp_candidates(const float2* pmap, int nx, int ny, float dxy, const float2* kcand /* device */,
-                             int ncand, float2* tables, double* partial, double* xstary, cudaStream_t s,
-                             long long* launches);
+
+// Candidate pattern vectors of one modamp pass, passed by value as a kernel
+// argument (no host-to-device copy): k[c] = k0_c * (order2 - order1), 1/um.
+constexpr int kMaxCand = 64;
+struct CandList {
+  float2 k[kMaxCand];
+};
+// XStarY[c] = sum_xy pmap(x,y) exp(i 2pi ((x - nx/2) kx_c + (y - ny/2) ky_c) dxy), c < ncand
+int launch_modamp_candidates(const float2* pmap, int nx, int ny, float dxy, const CandList& kcand, int ncand,
+                             float2* tables, double* partial, double* xstary, cudaStream_t s, long long* launches);
+
+// Modulation amplitudes of the last fit and the Wiener-filter weights derived
+// from them, in device memory: the filter reads them there, so a volume whose
+// fit needs no host decision runs without a host round trip.  Index d *
+// norders + o.
+struct FitDev {
+  float2 amp[kMaxDirs * kMaxOrders];
+  float ampmag2[kMaxDirs * kMaxOrders];  // |amp|^2
+  float termw[kMaxDirs * kMaxOrders];    // |amp|^2 / noisevar; order 0: 1 / noisevar
+};
+struct FitFinishArgs {
+  int ndirs, norders;
+  int chain2d;       // nz == 1: amp[o] *= amp[o - 1] for o >= 2 (cudaSirecon.cpp:450-452)
+  int nforce;        // forcemodamp values (cudaSirecon.cpp:453-464); 0: none
+  float forceamp[kMaxOrders];
+  int fitallphases;  // 0: orders >= 2 take order * phase of order 1 (cudaSirecon.cpp:465-482)
+  float noisevar[kMaxDirs * kMaxOrders];
+  float rnv[kMaxDirs * kMaxOrders];  // 1 / noisevar
+};
+// The no-search branch of the modamp fit (findrealspacemodamp at the known k0
+// for every direction and order, cudaSirecon.cpp:409-492) finished on the
+// device: slots[(d * norders + o) * 4 + {0, 1, 2}] = XStarY re, im and
+// sum |X|^2 of order o (o >= 1) -> FitDev.
+int launch_fit_finish(const double* slots, const FitFinishArgs& a, FitDev* out, cudaStream_t s, long long* launches);
+// Host-fitted amplitudes (after a k0 search) -> FitDev, through the kernel's
+// arguments.
+struct AmpList {
+  float2 amp[kMaxDirs * kMaxOrders];
+};
+int launch_set_fit(const AmpList& amps, const FitFinishArgs& a, FitDev* out, cudaStream_t s, long long* launches);
 
 // ---------------------------------------------------------------- assembly
 struct FilterArgs {
@@ -109,13 +146,17 @@ struct FilterArgs {
   float dkx, dky, rdistcutoff, apocutoff, zapocutoff, wiener2;
   int zdc[kMaxOrders];
   float2 k0[kMaxDirs];
-  float ampmag2[kMaxDirs * kMaxOrders];
   float noisevar[kMaxDirs * kMaxOrders];
-  float2 conjamp[kMaxOrders];
+  const FitDev* fit;     // modulation amplitudes and term weights (device)
   int suppress, supp_radius, dampen0, nokz0, filteroverlaps, apodizeoutput, bessel;
   OTFView otf;
 };
 int launch_filter(const FilterArgs& a, cudaStream_t s, long long* launches);
+
+// Pattern vectors of every direction, by value (1/um)
+struct K0List {
+  float2 k[kMaxDirs];
+};
 
 struct AssembleArgs {
   const float2* bands;  // all directions [ndirs][nph][nz][ny][nxh]
@@ -128,13 +169,21 @@ struct AssembleArgs {
   size_t tcap;          // capacity of T in complex elements
   float2* S;            // [Z][Y][X]
   float* out;           // [Z][Y][X]
+  void* tables;         // device slot tables (assemble_tables_bytes), uploaded by assemble_tables_upload
 };
+// The slot tables of an assembly (which band planes are summed into which
+// output plane) depend only on the shape and the in-band plane counts; they
+// are uploaded once and reused by every launch_assemble of that geometry.
+size_t assemble_tables_bytes(const AssembleArgs& a);
+// Writes the tables of `a` into a.tables (synchronous copy; call outside the
+// timed/captured work, again whenever zdc changes).
+int assemble_tables_upload(const AssembleArgs& a);
 int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches);
 
 // Phase-ramp tables for assembly: ex[d*no+o][j] = exp(i fact pi (j - X/2) o k0x_d dxyz),
 // ey likewise along y (computed in double precision).
-int launch_ramp_tables(const float2* k0 /* device [ndirs] */, int ndirs, int norders, int X, int Y, float dxyz,
-                       float fact, float2* ex, float2* ey, cudaStream_t s, long long* launches);
+int launch_ramp_tables(const K0List& k0, int ndirs, int norders, int X, int Y, float dxyz, float fact, float2* ex,
+                       float2* ey, cudaStream_t s, long long* launches);
 
 // FFT-engine self test on `nlines` lines of length n (in place, device memory)
 int launch_fft_selftest(float2* data, int n, int nlines, int inverse, int columns, cudaStream_t s);

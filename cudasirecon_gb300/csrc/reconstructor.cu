@@ -21,7 +21,6 @@ using namespace simrecon;
 namespace {
 
 constexpr float kK0WarningThresh = 0.05f;  // cudaSireconImpl.h:55
-constexpr int kMaxCand = 64;
 
 uint32_t fbits(float f)
 {
@@ -31,6 +30,9 @@ uint32_t fbits(float f)
 }
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+float2v cmulh(float2v a, float2v b) { return float2v{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+float cmagh(float2v a) { return sqrt(a.x * a.x + a.y * a.y); }
 
 // fitparabola, gpuFunctionsImpl.cu:479-495
 float fitparabola(float a1, float a2, float a3)
@@ -124,32 +126,40 @@ bool SIM_Reconstructor::load_otf_tiff(const std::string& path, Stack* out, std::
   return tiff_read(path, out, err);
 }
 
+bool SIM_Reconstructor::init_shape(int nx, int ny, int nimages, const std::string& config, std::string* err)
+{
+  set_defaults(&opt);
+  // the config file is parsed if it can be opened (cudaSirecon.cpp:884-890)
+  if (!apply_config_file(&opt, config, false, err)) return false;
+  if (opt.p.otffiles.empty()) {
+    *err = "the option '--otf-file' is required but missing";
+    return false;
+  }
+  Stack otf;
+  if (!load_otf_tiff(opt.p.otffiles, &otf, err)) return false;
+  opt.p.bTIFF = true;  // cudaSirecon.cpp:901
+  return setup(nx, ny, nimages, 1, &otf, err);
+}
+
 SIM_Reconstructor* SIM_Reconstructor::from_shape(int nx, int ny, int nimages, const std::string& config,
                                                  std::string* err)
 {
   SIM_Reconstructor* r = new SIM_Reconstructor();
-  set_defaults(&r->opt);
-  // the config file is parsed if it can be opened (cudaSirecon.cpp:884-890)
-  if (!apply_config_file(&r->opt, config, false, err)) {
-    delete r;
-    return nullptr;
-  }
-  if (r->opt.p.otffiles.empty()) {
-    *err = "the option '--otf-file' is required but missing";
-    delete r;
-    return nullptr;
-  }
-  Stack otf;
-  if (!r->load_otf_tiff(r->opt.p.otffiles, &otf, err)) {
-    delete r;
-    return nullptr;
-  }
-  r->opt.p.bTIFF = true;  // cudaSirecon.cpp:901
-  if (!r->setup(nx, ny, nimages, 1, &otf, err)) {
+  if (!r->init_shape(nx, ny, nimages, config, err)) {
     delete r;
     return nullptr;
   }
   return r;
+}
+
+bool SIM_Reconstructor::plan_bytes(int nx, int ny, int nimages, const std::string& config, size_t* bytes,
+                                   std::string* err)
+{
+  SIM_Reconstructor r;
+  r.dry_run_ = true;
+  if (!r.init_shape(nx, ny, nimages, config, err)) return false;
+  *bytes = r.planned_bytes_;
+  return true;
 }
 
 SIM_Reconstructor* SIM_Reconstructor::from_argv(int argc, char** argv, std::string* err)
@@ -405,8 +415,6 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
   }
 
   // device arena
-  check(cudaGetDevice(&device_), "cudaGetDevice");
-  check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
   const size_t nspec = (size_t)ndirs_ * nph_ * nz_ * ny_ * nxh_;
   const int nzb = 2 * zdc_ovl_ + 1;
   const size_t nxy = (size_t)nx_ * ny_;
@@ -439,11 +447,12 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
       {(void**)&d_bval_, 256 * sizeof(float)},
       {(void**)&d_bidx_, 256 * sizeof(int)},
       {(void**)&d_peak_, 8 * sizeof(float)},
-      {(void**)&d_kcand_, kMaxCand * sizeof(float2)},
       {(void**)&d_tables_, (size_t)kMaxCand * (nx_ + ny_) * sizeof(float2)},
       {(void**)&d_partial_, (size_t)kModampBlocks * kMaxCand * 2 * sizeof(double)},
       {(void**)&d_xstary_, (size_t)kMaxCand * 2 * sizeof(double)},
-      {(void**)&d_k0_, (size_t)kMaxDirs * sizeof(float2)},
+      {(void**)&d_fit_, sizeof(FitDev)},
+      {(void**)&d_fitslots_, (size_t)kMaxDirs * kMaxOrders * 4 * sizeof(double)},
+      {(void**)&d_asmtab_, asm_table_bytes()},
       {(void**)&d_ex_, (size_t)ndirs_ * norders_ * X_ * sizeof(float2)},
       {(void**)&d_ey_, (size_t)ndirs_ * norders_ * Y_ * sizeof(float2)},
       {(void**)&d_T_, tcap_ * sizeof(float2)},
@@ -452,6 +461,15 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
   };
   size_t total = 0;
   for (auto& r : reqs) total += align_up(r.bytes, 256);
+  if (dry_run_) {
+    // every buffer the handle can hold: the arena, process_series' second raw
+    // and output buffers, the flat-field calibration
+    planned_bytes_ = total + (size_t)nimg_ * nxy * sizeof(float) + (size_t)X_ * Y_ * Z_ * sizeof(float) +
+                     (p.bUsecorr ? 2 * nxy * sizeof(float) : 0);
+    return true;
+  }
+  check(cudaGetDevice(&device_), "cudaGetDevice");
+  check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
   cudaError_t e = cudaMalloc((void**)&arena_, total);
   if (e != cudaSuccess) {
     *err = std::string("device allocation of ") + std::to_string(total >> 20) + " MiB failed: " +
@@ -473,12 +491,16 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
   check(cudaMemcpy(d_otf_, hotf.data(), hotf.size() * sizeof(float2), cudaMemcpyHostToDevice), "upload");
   check(cudaMemset(d_sdp0_, 0, (size_t)nz_ * sizeof(double)), "memset");
   check(cudaMemset(d_spec_, 0, nspec * sizeof(float2)), "memset");
+  check(cudaMemset(d_fitslots_, 0, (size_t)kMaxDirs * kMaxOrders * 4 * sizeof(double)), "memset");
+  check_launch(upload_amps(), "fit init");
+  check(cudaStreamSynchronize(stream_), "fit init");
   if (p.bUsecorr && !load_corr(err)) return false;
   return true;
 }
 
 SIM_Reconstructor::~SIM_Reconstructor()
 {
+  drop_graphs();
   for (auto& pd : pending_) {
     cudaEventDestroy(pd.a);
     cudaEventDestroy(pd.b);
@@ -597,6 +619,9 @@ void SIM_Reconstructor::stage_raw(const void* raw, bool u16)
   check(cudaMemcpyAsync(d_raw_, raw, n * (u16 ? 2 : 4), cudaMemcpyHostToDevice, stream_), "raw upload");
   have_raw_ = true;
   ingest();
+  // setRaw copies the caller's stack (interface.cpp:19-25): return once the
+  // upload and the ingest kernels are done with it
+  check(cudaStreamSynchronize(stream_), "ingest");
 }
 
 void SIM_Reconstructor::ingest()
@@ -623,12 +648,9 @@ void SIM_Reconstructor::ingest()
   ia.apofact = d_apofact_;
   ia.spec = d_spec_;
   check_launch(launch_ingest(ia, stream_, &launches_), "ingest");
-  stage_end("ingest", a, l0);
   // processOneVolume without loadAndRescaleImage uses unit ratios
-  std::vector<float> ones((size_t)ndirs_ * nph_ * nz_, 1.0f);
-  check(cudaMemcpyAsync(d_scale_, ones.data(), ones.size() * sizeof(float), cudaMemcpyHostToDevice, stream_),
-        "scale init");
-  check(cudaStreamSynchronize(stream_), "ingest");
+  check_launch(launch_fill(d_scale_, (size_t)ndirs_ * nph_ * nz_, 1.0f, stream_, &launches_), "scale init");
+  stage_end("ingest", a, l0);
   rescaled_ = false;
 }
 
@@ -732,15 +754,14 @@ void SIM_Reconstructor::eval_candidates(int o1, int o2, const std::vector<std::p
     if (!cache_.count({fbits(c.first), fbits(c.second)})) todo.push_back(c);
   for (size_t b0 = 0; b0 < todo.size(); b0 += kMaxCand) {
     size_t nc = std::min<size_t>(kMaxCand, todo.size() - b0);
-    std::vector<float2> kc(nc);
+    CandList kc{};
     for (size_t i = 0; i < nc; ++i) {
       float angle = todo[b0 + i].first, mag = todo[b0 + i].second;
       // getmodamp: k1 = klength*(cosf, sinf)(kangle); findrealspacemodamp: k1*(order2-order1)
       float k1x = mag * cosf(angle), k1y = mag * sinf(angle);
-      kc[i] = make_float2(k1x * (o2 - o1), k1y * (o2 - o1));
+      kc.k[i] = make_float2(k1x * (o2 - o1), k1y * (o2 - o1));
     }
-    check(cudaMemcpyAsync(d_kcand_, kc.data(), nc * sizeof(float2), cudaMemcpyHostToDevice, stream_), "cand");
-    check_launch(launch_modamp_candidates(d_pmap_, nx_, ny_, opt.ip.dxy, d_kcand_, (int)nc, d_tables_, d_partial_,
+    check_launch(launch_modamp_candidates(d_pmap_, nx_, ny_, opt.ip.dxy, kc, (int)nc, d_tables_, d_partial_,
                                           d_xstary_, stream_, &launches_),
                  "modamp");
     check_launch(launch_copy_out(d_xstary_, dh_pinned_, nc * 4, d_sumxy_, dh_pinned_ + 2 * kMaxCand, 4, stream_,
@@ -791,10 +812,10 @@ float2v SIM_Reconstructor::findrealspacemodamp(int d, int o1, int o2, float k0x,
   if (redo || o1 != cur_o1_ || o2 != cur_o2_) build_overlaps(d, o1, o2, k0x, k0y);
   // the candidate kernel takes (angle, mag) pairs; pass k0 through an exact
   // (angle, mag) key by evaluating directly
-  std::vector<float2> kc = {make_float2(k0x * (o2 - o1), k0y * (o2 - o1))};
-  check(cudaMemcpyAsync(d_kcand_, kc.data(), sizeof(float2), cudaMemcpyHostToDevice, stream_), "cand");
-  check_launch(launch_modamp_candidates(d_pmap_, nx_, ny_, opt.ip.dxy, d_kcand_, 1, d_tables_, d_partial_,
-                                        d_xstary_, stream_, &launches_),
+  CandList kc{};
+  kc.k[0] = make_float2(k0x * (o2 - o1), k0y * (o2 - o1));
+  check_launch(launch_modamp_candidates(d_pmap_, nx_, ny_, opt.ip.dxy, kc, 1, d_tables_, d_partial_, d_xstary_,
+                                        stream_, &launches_),
                "modamp");
   check_launch(launch_copy_out(d_xstary_, dh_pinned_, 4, d_sumxy_, dh_pinned_ + 2, 4, stream_, &launches_), "d2h");
   check(cudaStreamSynchronize(stream_), "modamp");
@@ -955,37 +976,26 @@ void SIM_Reconstructor::fitk0andmodamps(int d)
   }
 }
 
-static float2v cmulh(float2v a, float2v b) { return float2v{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
-static float cmagh(float2v a) { return sqrt(a.x * a.x + a.y * a.y); }
-
-// findModulationVectorsAndPhasesForAllDirections, k0 / modamp part
-// (cudaSirecon.cpp:296-493)
+// findModulationVectorsAndPhasesForAllDirections, k0 / modamp part with a
+// k0 search (cudaSirecon.cpp:296-408, 450-492)
 void SIM_Reconstructor::fit_direction(int direction)
 {
   ReconParams& p = opt.p;
   const ImageParams& ip = opt.ip;
-  const bool reuse = ip.ntimes > 1 && ip.curTimeIdx > 0 && p.bUseTime0k0;
-  if (!reuse) k0_[direction] = k0guess_[direction];
+  k0_[direction] = k0guess_[direction];
   cur_o1_ = cur_o2_ = -1;  // overlaps belong to another direction
-  if (p.bSearchforvector && !reuse) {
-    findk0(direction);
-    p.recalcarrays = 1;
-    fitk0andmodamps(direction);
-    if (ip.curTimeIdx == 0) k0_time0_[direction] = k0_[direction];
-    float dx = k0_[direction].x - k0guess_[direction].x, dy = k0_[direction].y - k0guess_[direction].y;
-    float dist = sqrt(dx * dx + dy * dy);
-    if (ip.ntimes > 1 && ip.curTimeIdx > 0 && dist > 2 * kK0WarningThresh) {
-      k0_[direction] = k0_time0_[direction];
-      for (int order = 1; order < norders_; ++order) {
-        int o1 = nz_ > 1 ? 0 : order - 1;
-        amp_[direction][order] = findrealspacemodamp(direction, o1, order, k0_[direction].x, k0_[direction].y, 1);
-      }
+  findk0(direction);
+  p.recalcarrays = 1;
+  fitk0andmodamps(direction);
+  if (ip.curTimeIdx == 0) k0_time0_[direction] = k0_[direction];
+  float dx = k0_[direction].x - k0guess_[direction].x, dy = k0_[direction].y - k0guess_[direction].y;
+  float dist = sqrt(dx * dx + dy * dy);
+  if (ip.ntimes > 1 && ip.curTimeIdx > 0 && dist > 2 * kK0WarningThresh) {
+    k0_[direction] = k0_time0_[direction];
+    for (int order = 1; order < norders_; ++order) {
+      int o1 = nz_ > 1 ? 0 : order - 1;
+      amp_[direction][order] = findrealspacemodamp(direction, o1, order, k0_[direction].x, k0_[direction].y, 1);
     }
-  } else {
-    for (int order = 1; order < norders_; ++order)
-      amp_[direction][order] = pre_amp_valid_ ? pre_amp_[direction][order]
-                                              : findrealspacemodamp(direction, 0, order, k0_[direction].x,
-                                                                    k0_[direction].y, 1);
   }
   if (ip.nz == 1)
     for (int order = 2; order < norders_; ++order)
@@ -1012,57 +1022,157 @@ void SIM_Reconstructor::fit_direction(int direction)
   }
 }
 
+// Whether this volume's fit makes no host decision: k0 known (reused from
+// time 0 or no search), only the modamps are evaluated
+bool SIM_Reconstructor::fit_without_search() const
+{
+  const ReconParams& p = opt.p;
+  const ImageParams& ip = opt.ip;
+  const bool reuse = ip.ntimes > 1 && ip.curTimeIdx > 0 && p.bUseTime0k0;
+  return reuse || !p.bSearchforvector;
+}
+
 void SIM_Reconstructor::fit_all()
 {
   TimerScope ts(this);
   cudaEvent_t a;
   long long l0;
   stage_begin("fit", &a, &l0);
-  const ReconParams& p = opt.p;
-  const ImageParams& ip = opt.ip;
-  const bool reuse = ip.ntimes > 1 && ip.curTimeIdx > 0 && p.bUseTime0k0;
-  // no direction searches: every direction's modamps are findrealspacemodamp
-  // at its k0, evaluated here back to back with one synchronisation
-  if (reuse || !p.bSearchforvector) modamps_at_k0(reuse);
-  for (int d = 0; d < ndirs_; ++d) fit_direction(d);
-  pre_amp_valid_ = false;
+  if (fit_without_search()) {
+    fit_on_device();
+  } else {
+    for (int d = 0; d < ndirs_; ++d) fit_direction(d);
+    check_launch(upload_amps(), "fit results");
+  }
   stage_end("fit", a, l0);
 }
 
-// findrealspacemodamp(d, 0, order, k0) for every direction and order (the
-// no-search branch of fit_direction): the same launches in the same stream
-// order as the per-call path, each result copied to its own slot of the
-// pinned host buffer, one synchronisation at the end
-void SIM_Reconstructor::modamps_at_k0(bool reuse)
+FitFinishArgs SIM_Reconstructor::fit_finish_args() const
 {
-  pre_amp_.assign(ndirs_, std::vector<float2v>(norders_, float2v{0, 0}));
-  int slot = 0;
+  const ReconParams& p = opt.p;
+  FitFinishArgs fa{};
+  fa.ndirs = ndirs_;
+  fa.norders = norders_;
+  fa.chain2d = opt.ip.nz == 1;
+  fa.nforce = (int)std::min<size_t>(p.forceamp.size(), kMaxOrders);
+  for (int i = 0; i < fa.nforce; ++i) fa.forceamp[i] = p.forceamp[i];
+  fa.fitallphases = p.bFitallphases;
+  for (int i = 0; i < ndirs_ * norders_; ++i) {
+    fa.noisevar[i] = noisevar_[i];
+    fa.rnv[i] = 1.f / noisevar_[i];
+  }
+  return fa;
+}
+
+// the host's amplitudes (after a k0 search) into the device fit results
+int SIM_Reconstructor::upload_amps()
+{
+  AmpList al{};
+  for (int d = 0; d < ndirs_; ++d)
+    for (int o = 0; o < norders_; ++o) al.amp[d * norders_ + o] = make_float2(amp_[d][o].x, amp_[d][o].y);
+  amps_on_device_only_ = false;
+  return launch_set_fit(al, fit_finish_args(), d_fit_, stream_, &launches_);
+}
+
+// The no-search branch (cudaSirecon.cpp:409-449 and the amplitude rules
+// after it): findrealspacemodamp(d, 0, order, k0) for every direction and
+// order, each XStarY / sum|X|^2 kept in device memory, the amplitudes
+// finished on the device.  No copy and no synchronisation: the host learns
+// the amplitudes only when asked (get_fit).
+void SIM_Reconstructor::fit_on_device()
+{
+  const ReconParams& p = opt.p;
+  const ImageParams& ip = opt.ip;
+  const bool reuse = ip.ntimes > 1 && ip.curTimeIdx > 0 && p.bUseTime0k0;
   for (int d = 0; d < ndirs_; ++d) {
-    const float2v k = reuse ? k0_[d] : k0guess_[d];
-    for (int order = 1; order < norders_; ++order, ++slot) {
+    if (!reuse) k0_[d] = k0guess_[d];
+    const float2v k = k0_[d];
+    for (int order = 1; order < norders_; ++order) {
       build_overlaps(d, 0, order, k.x, k.y);
-      const float2 kc = make_float2(k.x * order, k.y * order);
-      check(cudaMemcpyAsync(d_kcand_, &kc, sizeof(float2), cudaMemcpyHostToDevice, stream_), "cand");
-      check_launch(launch_modamp_candidates(d_pmap_, nx_, ny_, opt.ip.dxy, d_kcand_, 1, d_tables_, d_partial_,
-                                            d_xstary_, stream_, &launches_),
+      CandList kc{};
+      kc.k[0] = make_float2(k.x * order, k.y * order);
+      check_launch(launch_modamp_candidates(d_pmap_, nx_, ny_, ip.dxy, kc, 1, d_tables_, d_partial_, d_xstary_,
+                                            stream_, &launches_),
                    "modamp");
-      check_launch(launch_copy_out(d_xstary_, dh_pinned_ + 4 * slot, 4, d_sumxy_, dh_pinned_ + 4 * slot + 2, 4, stream_,
-                                   &launches_),
-                   "d2h");
+      double* slot = d_fitslots_ + (size_t)(d * norders_ + order) * 4;
+      check_launch(launch_copy_out(d_xstary_, slot, 4, d_sumxy_, slot + 2, 2, stream_, &launches_), "modamp");
     }
   }
-  check(cudaStreamSynchronize(stream_), "modamp");
-  slot = 0;
-  for (int d = 0; d < ndirs_; ++d)
-    for (int order = 1; order < norders_; ++order, ++slot) {
-      const float sx = (float)h_pinned_[4 * slot + 2];
-      pre_amp_[d][order] = float2v{(float)h_pinned_[4 * slot] / sx, (float)h_pinned_[4 * slot + 1] / sx};
-    }
+  check_launch(launch_fit_finish(d_fitslots_, fit_finish_args(), d_fit_, stream_, &launches_), "modamp");
   cur_o1_ = cur_o2_ = -1;
-  pre_amp_valid_ = true;
+  amps_on_device_only_ = true;
+}
+
+// the device's amplitudes into amp_ (waits for the stream)
+void SIM_Reconstructor::sync_amps() const
+{
+  if (!amps_on_device_only_) return;
+  FitDev f;
+  check(cudaStreamSynchronize(stream_), "fit results");
+  check(cudaMemcpy(&f, d_fit_, sizeof(FitDev), cudaMemcpyDeviceToHost), "fit results");
+  for (int d = 0; d < ndirs_; ++d)
+    for (int o = 0; o < norders_; ++o) amp_[d][o] = float2v{f.amp[d * norders_ + o].x, f.amp[d * norders_ + o].y};
+  amps_on_device_only_ = false;
 }
 
 // ------------------------------------------------------ filter + assembly
+// zdistcutoff of every order after filtering (filterbands,
+// gpuFunctionsImpl.cu:1253-1289): the kz planes each band keeps
+void SIM_Reconstructor::filter_zdc(int* zdc) const
+{
+  const ReconParams& p = opt.p;
+  const ImageParams& ip = opt.ip;
+  float dkz = ip.dz > 0 ? (1 / (nz_ * ip.dz)) : p.dkzotf;
+  float lambdaem = (ip.wave[0] / p.nimm) / 1000.0;
+  float lambdaexc = 0.88 * lambdaem;
+  float alpha = asinf(p.na / p.nimm);
+  for (int o = 0; o < kMaxOrders; ++o) zdc[o] = 0;
+  zdc[0] = (int)ceil(((1 - cosf(alpha)) / lambdaem) / dkz);
+  zdc[norders_ - 1] = 1.3 * zdc[0];
+  if (norders_ >= 3)
+    for (int order = 1; order < norders_ - 1; order++) zdc[order] = (1 + lambdaem / lambdaexc) * zdc[0];
+  for (int order = 0; order < norders_; order++)
+    if (zdc[order] >= nz_ / 2) zdc[order] = ((nz_ / 2 - 1) > 0 ? (nz_ / 2 - 1) : 0);
+}
+
+// the geometry part of the assembly arguments (no buffers but the tables)
+AssembleArgs SIM_Reconstructor::asm_geometry() const
+{
+  AssembleArgs aa{};
+  aa.ndirs = ndirs_;
+  aa.norders = norders_;
+  aa.nphases = nph_;
+  aa.nx = nx_;
+  aa.ny = ny_;
+  aa.nz = nz_;
+  aa.X = X_;
+  aa.Y = Y_;
+  aa.Z = Z_;
+  aa.tables = d_asmtab_;
+  return aa;
+}
+
+size_t SIM_Reconstructor::asm_table_bytes() const { return assemble_tables_bytes(asm_geometry()); }
+
+bool SIM_Reconstructor::asm_tables_current(const AssembleArgs& aa) const
+{
+  return asm_tables_valid_ && std::equal(aa.zdc, aa.zdc + kMaxOrders, asm_tables_zdc_);
+}
+
+// Upload the assembly's slot tables when the in-band planes changed (the
+// first volume, or options changed through SR_getReconParams).  Synchronous:
+// called before a volume's launches, never inside a captured graph.
+void SIM_Reconstructor::prepare_asm_tables()
+{
+  AssembleArgs aa = asm_geometry();
+  filter_zdc(aa.zdc);
+  if (asm_tables_current(aa)) return;
+  check(cudaStreamSynchronize(stream_), "assembly tables");
+  check_launch(assemble_tables_upload(aa), "assembly tables");
+  std::copy(aa.zdc, aa.zdc + kMaxOrders, asm_tables_zdc_);
+  asm_tables_valid_ = true;
+}
+
 void SIM_Reconstructor::filter_and_assemble()
 {
   TimerScope ts(this);
@@ -1088,12 +1198,9 @@ void SIM_Reconstructor::filter_and_assemble()
   float rdistcutoff = (p.na * 2 / (ip.wave[0] / 1000.0));
   if (rdistcutoff > 1. / (2. * dxy)) rdistcutoff = 1. / (2. * dxy);
   int zdc[kMaxOrders] = {0};
-  zdc[0] = (int)ceil(((1 - cosf(alpha)) / lambdaem) / dkz);
-  zdc[norders_ - 1] = 1.3 * zdc[0];
-  if (norders_ >= 3)
-    for (int order = 1; order < norders_ - 1; order++) zdc[order] = (1 + lambdaem / lambdaexc) * zdc[0];
-  for (int order = 0; order < norders_; order++)
-    if (zdc[order] >= nz_ / 2) zdc[order] = ((nz_ / 2 - 1) > 0 ? (nz_ / 2 - 1) : 0);
+  filter_zdc(zdc);
+  (void)alpha;
+  (void)lambdaexc;
   float apocutoff = rdistcutoff + k0mag * (norders_ - 1);
   float zapocutoff = norders_ > 1 ? zdc[1] : 0;
   fa.dkx = 1. / (nx_ * dxy);
@@ -1105,11 +1212,9 @@ void SIM_Reconstructor::filter_and_assemble()
   for (int o = 0; o < norders_; ++o) fa.zdc[o] = zdc[o];
   for (int d = 0; d < ndirs_; ++d) {
     fa.k0[d] = make_float2(k0_[d].x, k0_[d].y);
-    for (int o = 0; o < norders_; ++o) {
-      fa.ampmag2[d * norders_ + o] = amp_[d][o].x * amp_[d][o].x + amp_[d][o].y * amp_[d][o].y;
-      fa.noisevar[d * norders_ + o] = noisevar_[d * norders_ + o];
-    }
+    for (int o = 0; o < norders_; ++o) fa.noisevar[d * norders_ + o] = noisevar_[d * norders_ + o];
   }
+  fa.fit = d_fit_;
   fa.suppress = p.bSuppress_singularities;
   fa.supp_radius = p.suppression_radius;
   fa.dampen0 = p.bDampenOrder0;
@@ -1127,17 +1232,15 @@ void SIM_Reconstructor::filter_and_assemble()
       fa.otf.otf[o] = d_otf_ + ((size_t)dir_ * norders_ + o) * p.nxotf * p.nzotf;
     fa.dir = d;
     fa.bands = d_spec_ + (size_t)d * nph_ * nz_ * ny_ * nxh_;
-    for (int o = 0; o < norders_; ++o) fa.conjamp[o] = make_float2(amp_[d][o].x, -amp_[d][o].y);
     check_launch(launch_filter(fa, stream_, &launches_), "filterbands");
   }
   stage_end("filter", ev, l0);
 
   stage_begin("assemble", &ev, &l0);
-  std::vector<float2> k0h(kMaxDirs, make_float2(0, 0));
-  for (int d = 0; d < ndirs_; ++d) k0h[d] = make_float2(k0_[d].x, k0_[d].y);
-  check(cudaMemcpyAsync(d_k0_, k0h.data(), kMaxDirs * sizeof(float2), cudaMemcpyHostToDevice, stream_), "k0");
+  K0List k0l{};
+  for (int d = 0; d < ndirs_; ++d) k0l.k[d] = make_float2(k0_[d].x, k0_[d].y);
   float fact = p.explodefact / 0.5;
-  check_launch(launch_ramp_tables(d_k0_, ndirs_, norders_, X_, Y_, dxy / p.zoomfact, fact, d_ex_, d_ey_, stream_,
+  check_launch(launch_ramp_tables(k0l, ndirs_, norders_, X_, Y_, dxy / p.zoomfact, fact, d_ex_, d_ey_, stream_,
                                   &launches_),
                "ramp");
   AssembleArgs aa{};
@@ -1158,18 +1261,21 @@ void SIM_Reconstructor::filter_and_assemble()
   aa.tcap = tcap_;
   aa.S = d_S_;
   aa.out = d_out_;
+  aa.tables = d_asmtab_;
+  if (!asm_tables_current(aa)) throw std::runtime_error("assembly tables not prepared for this geometry");
   check_launch(launch_assemble(aa, stream_, &launches_), "assemble");
   stage_end("assemble", ev, l0);
 }
 
 // processOneVolume (cudaSirecon.cpp:1264-1321)
-int SIM_Reconstructor::process_one_volume()
+int SIM_Reconstructor::process_one_volume(bool sync)
 {
   if (!have_raw_) throw std::runtime_error("processOneVolume before setRaw/setFile");
+  prepare_asm_tables();
   separate();
   fit_all();
   filter_and_assemble();
-  check(cudaStreamSynchronize(stream_), "processOneVolume");
+  if (sync) check(cudaStreamSynchronize(stream_), "processOneVolume");
   have_raw_ = false;  // the bands are consumed (filtered in place)
   return 1;
 }
@@ -1232,8 +1338,9 @@ void SIM_Reconstructor::set_fitted_k0(const float* k0)
   }
 }
 
-void SIM_Reconstructor::get_fit(float* k0, float* amps) const
+void SIM_Reconstructor::get_fit(float* k0, float* amps)
 {
+  if (amps) sync_amps();
   for (int d = 0; d < ndirs_; ++d) {
     if (k0) {
       k0[2 * d] = k0_[d].x;
@@ -1244,6 +1351,63 @@ void SIM_Reconstructor::get_fit(float* k0, float* amps) const
         amps[2 * (d * norders_ + o)] = amp_[d][o].x;
         amps[2 * (d * norders_ + o) + 1] = amp_[d][o].y;
       }
+  }
+}
+
+// A volume whose fit makes no host decision (k0 reused from time 0, or no
+// search) is one fixed sequence of launches: ingest, bleach correction,
+// separation, modamp evaluation and device-side amplitude finish, filter and
+// assembly.  It is captured once per raw/output buffer pair as a CUDA graph
+// and replayed, with the "raw buffer free" event recorded inside the graph
+// right after ingest.
+bool SIM_Reconstructor::capture_volume(int b, void* raw, float* out, int t, cudaEvent_t raw_free)
+{
+  VolumeGraph& g = graphs_[b];
+  const bool tnz = t != 0;
+  if (g.exec && g.raw == raw && g.out == out && g.t_nonzero == tnz && g.u16 == raw_u16_) return true;
+  if (g.exec) {
+    cudaGraphExecDestroy(g.exec);
+    g.exec = nullptr;
+  }
+  prepare_asm_tables();  // synchronous upload, outside the capture
+  d_raw_ = raw;
+  d_out_ = out;
+  const long long l0 = launches_;
+  check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeRelaxed), "graph capture");
+  cudaGraph_t graph = nullptr;
+  try {
+    have_raw_ = true;
+    ingest();
+    check(cudaEventRecordWithFlags(raw_free, stream_, cudaEventRecordExternal), "graph event");
+    load_and_rescale(t, 0);
+    set_cur_time(t);
+    separate();
+    fit_all();
+    filter_and_assemble();
+  } catch (...) {
+    cudaStreamEndCapture(stream_, &graph);
+    if (graph) cudaGraphDestroy(graph);
+    launches_ = l0;
+    throw;
+  }
+  check(cudaStreamEndCapture(stream_, &graph), "graph capture");
+  cudaError_t e = cudaGraphInstantiate(&g.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  check(e, "graph instantiate");
+  g.launches = launches_ - l0;
+  launches_ = l0;
+  g.raw = raw;
+  g.out = out;
+  g.t_nonzero = tnz;
+  g.u16 = raw_u16_;
+  return true;
+}
+
+void SIM_Reconstructor::drop_graphs()
+{
+  for (VolumeGraph& g : graphs_) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = VolumeGraph{};
   }
 }
 
@@ -1280,36 +1444,56 @@ void SIM_Reconstructor::process_series(const void* const* raws, bool u16, float*
   upload(0);
   if (n > 1) upload(1);
   raw_u16_ = u16;
+  // graphs are captured per call: options changed between calls through
+  // SR_getReconParams take effect on the next call
+  drop_graphs();
   try {
     for (int i = 0; i < n; ++i) {
       const int b = i & 1;
-      check(cudaStreamWaitEvent(stream_, ev_raw_ready_[b], 0), "series wait");
-      d_raw_ = raw_buf[b];
-      have_raw_ = true;
-      ingest();  // returns after the ingest kernels finished: raw buffer b is free
-      check(cudaEventRecord(ev_raw_free_[b], stream_), "series event");
-      if (i + 2 < n) upload(i + 2);
       const int t = standalone ? 0 : t0 + i;
-      load_and_rescale(t, 0);
-      set_cur_time(t);
+      check(cudaStreamWaitEvent(stream_, ev_raw_ready_[b], 0), "series wait");
       check(cudaStreamWaitEvent(stream_, ev_out_free_[b], 0), "series wait");
-      d_out_ = out_buf[b];
-      process_one_volume();
+      set_cur_time(t);
+      // the t > 0 volumes of a series with k0 reuse, or every volume without
+      // a k0 search; the rescale step differs between t = 0 and t > 0 only
+      const bool graph_ok = !profiling_ && fit_without_search();
+      if (graph_ok) {
+        capture_volume(b, raw_buf[b], out_buf[b], t, ev_raw_free_[b]);
+        check(cudaGraphLaunch(graphs_[b].exec, stream_), "graph launch");
+        launches_ += graphs_[b].launches;
+        amps_on_device_only_ = true;
+        have_raw_ = false;
+        rescaled_ = true;
+      } else {
+        d_raw_ = raw_buf[b];
+        d_out_ = out_buf[b];
+        have_raw_ = true;
+        ingest();
+        check(cudaEventRecord(ev_raw_free_[b], stream_), "series event");
+        load_and_rescale(t, 0);
+        set_cur_time(t);
+        process_one_volume(false);
+      }
+      if (i + 2 < n) upload(i + 2);
       check(cudaEventRecord(ev_out_ready_[b], stream_), "series event");
       check(cudaStreamWaitEvent(d2h_stream_, ev_out_ready_[b], 0), "series wait");
       check(cudaMemcpyAsync(outs[i], out_buf[b], out_bytes, cudaMemcpyDeviceToHost, d2h_stream_), "series download");
       check(cudaEventRecord(ev_out_free_[b], d2h_stream_), "series event");
     }
   } catch (...) {
+    cudaStreamSynchronize(stream_);
     cudaStreamSynchronize(h2d_stream_);
     cudaStreamSynchronize(d2h_stream_);
+    drop_graphs();
     d_raw_ = raw_buf[0];
     d_out_ = out_buf[0];
     d_out_alt_ = out_buf[1];
     throw;
   }
+  check(cudaStreamSynchronize(stream_), "series compute");
   check(cudaStreamSynchronize(h2d_stream_), "series upload");
   check(cudaStreamSynchronize(d2h_stream_), "series download");
+  drop_graphs();
   // getResult after the series returns the last volume; keep the arena's raw
   // buffer as the one setRaw uses
   d_raw_ = raw_buf[0];

@@ -24,13 +24,17 @@ class SIM_Reconstructor {
   // construction paths (interface.cpp:13-17, 54-57)
   static SIM_Reconstructor* from_shape(int nx, int ny, int nimages, const std::string& config, std::string* err);
   static SIM_Reconstructor* from_argv(int argc, char** argv, std::string* err);
+  // device bytes a from_shape handle of this shape and configuration can
+  // hold (arena, time-series buffers, calibration), found without allocating
+  static bool plan_bytes(int nx, int ny, int nimages, const std::string& config, size_t* bytes, std::string* err);
   ~SIM_Reconstructor();
 
   void set_raw_float(const float* raw, int nx, int ny, int nz);
   void set_raw_u16(const uint16_t* raw, int nx, int ny, int nz);
   void load_and_rescale(int it, int iw);
   void set_cur_time(int it) { opt.ip.curTimeIdx = (unsigned short)it; }
-  int process_one_volume();
+  // sync = false leaves the volume's work queued on the handle's stream
+  int process_one_volume(bool sync = true);
   void get_result(float* out);
   // n volumes: per volume i the same as setRaw(raws[i]) ->
   // loadAndRescaleImage(t0+i) -> setCurTimeIdx(t0+i) -> processOneVolume ->
@@ -51,7 +55,7 @@ class SIM_Reconstructor {
   void set_fitted_k0(const float* k0);
 
   // introspection / performance
-  void get_fit(float* k0, float* amps) const;
+  void get_fit(float* k0, float* amps);
   int prepare();  // separate bands without fitting (for stage checks)
   int get_band(int dir, int b, float* out);
   double bench_device(int steps);
@@ -69,6 +73,7 @@ class SIM_Reconstructor {
 
  private:
   SIM_Reconstructor() = default;
+  bool init_shape(int nx, int ny, int nimages, const std::string& config, std::string* err);
   bool setup(int nx, int ny, int nimages, int nwaves, const simrecon::Stack* otf, std::string* err);
   bool load_otf_tiff(const std::string& path, simrecon::Stack* out, std::string* err);
   bool load_corr(std::string* err);
@@ -77,8 +82,20 @@ class SIM_Reconstructor {
   void separate();
   void fit_all();
   void fit_direction(int d);
+  bool fit_without_search() const;
+  void fit_on_device();
+  simrecon::FitFinishArgs fit_finish_args() const;
+  int upload_amps();
+  void sync_amps() const;
   void filter_and_assemble();
-  void check(cudaError_t e, const char* what);
+  void filter_zdc(int* zdc) const;
+  simrecon::AssembleArgs asm_geometry() const;
+  size_t asm_table_bytes() const;
+  bool asm_tables_current(const simrecon::AssembleArgs& aa) const;
+  void prepare_asm_tables();
+  bool capture_volume(int b, void* raw, float* out, int t, cudaEvent_t raw_free);
+  void drop_graphs();
+  static void check(cudaError_t e, const char* what);
   void check_launch(int rc, const char* what);
 
   // fitting helpers (gpuFunctionsImpl.cu:306-1148 semantics)
@@ -89,7 +106,6 @@ class SIM_Reconstructor {
   void findk0(int d);
   void fitk0andmodamps(int d);
   float2v findrealspacemodamp(int d, int o1, int o2, float k0x, float k0y, int redo);
-  void modamps_at_k0(bool reuse);
   void prefetch_line(int o1, int o2, bool angle_axis, float fixed, float start, float step, int count, int dir);
 
   // geometry
@@ -100,6 +116,8 @@ class SIM_Reconstructor {
   bool otf_dk_from_header_ = false;  // MRC OTF: dkr / dkz taken from its header
   cudaStream_t stream_ = nullptr;
   int device_ = 0;
+  bool dry_run_ = false;      // setup computes planned_bytes_ and allocates nothing
+  size_t planned_bytes_ = 0;
 
   // device arena
   char* arena_ = nullptr;
@@ -122,11 +140,14 @@ class SIM_Reconstructor {
   float* d_bval_ = nullptr;
   int* d_bidx_ = nullptr;
   float* d_peak_ = nullptr;
-  float2* d_kcand_ = nullptr;
   float2* d_tables_ = nullptr;
   double* d_partial_ = nullptr;
   double* d_xstary_ = nullptr;
-  float2* d_k0_ = nullptr;
+  simrecon::FitDev* d_fit_ = nullptr;  // amplitudes + filter weights of the last fit
+  double* d_fitslots_ = nullptr;       // [ndirs * norders][4]: XStarY re, im, sum |X|^2 per order
+  void* d_asmtab_ = nullptr;           // assembly slot tables
+  bool asm_tables_valid_ = false;
+  int asm_tables_zdc_[simrecon::kMaxOrders] = {0};
   float2* d_ex_ = nullptr;
   float2* d_ey_ = nullptr;
   float2* d_T_ = nullptr;
@@ -152,10 +173,19 @@ class SIM_Reconstructor {
   std::vector<float> sepmat_;
   std::vector<float> noisevar_;
   std::vector<float2v> k0_, k0_time0_, k0guess_;
-  std::vector<std::vector<float2v>> amp_;
-  // modamps of the no-search branch, evaluated for all directions at once
-  std::vector<std::vector<float2v>> pre_amp_;
-  bool pre_amp_valid_ = false;
+  // amp_ is the host copy of the device fit results; after a fit on the
+  // device it is refreshed on demand (sync_amps)
+  mutable std::vector<std::vector<float2v>> amp_;
+  mutable bool amps_on_device_only_ = false;
+  // per raw/output buffer pair of process_series: the captured volume
+  struct VolumeGraph {
+    cudaGraphExec_t exec = nullptr;
+    void* raw = nullptr;
+    float* out = nullptr;
+    bool t_nonzero = false, u16 = false;
+    long long launches = 0;
+  };
+  VolumeGraph graphs_[2];
   bool raw_u16_ = false;
   bool have_raw_ = false;
   bool rescaled_ = false;

@@ -6,12 +6,16 @@
 //
 // Handles are pooled per (configuration, nx, ny, nimages): a worker reuses an
 // idle handle of the request's shape, else creates one.  Device memory is
-// bounded by the budget: after a handle is created, idle handles are deleted
-// least recently used first until the handles in use fit (at most the newest
-// handle's size above the budget while every other handle is busy).  If the
-// creation itself runs out of device memory, all idle handles are deleted and
-// the creation is tried once more.
+// admitted by the budget before anything is allocated: a handle's bytes are
+// planned from its shape and configuration (SIM_Reconstructor::plan_bytes,
+// every buffer it can come to hold) and reserved against the budget first;
+// while they do not fit, idle handles are deleted least recently used first,
+// and when none is idle the request waits until a busy handle is released.
+// The handles' reserved bytes therefore never exceed the budget.  A request
+// whose handle alone exceeds the budget fails with an error.
 #include "server.h"
+
+#include <cuda_runtime.h>
 
 #include <algorithm>
 #include <chrono>
@@ -30,6 +34,8 @@ double now_s()
 
 ReconServer::ReconServer(int workers, size_t hbm_budget) : budget_(hbm_budget)
 {
+  // the workers run on the device that is current where the server is made
+  if (cudaGetDevice(&device_) != cudaSuccess) device_ = 0;
   if (workers < 1) workers = 1;
   for (int i = 0; i < workers; ++i) workers_.emplace_back([this] { worker_loop(); });
 }
@@ -159,7 +165,18 @@ int ReconServer::wait(long long ticket, double* latency_ms, std::string* err)
     *err = "wait: unknown ticket";
     return -1;
   }
-  cv_done_.wait(lk, [&] { return done_[ticket].done; });
+  // each ticket is waited for once: a second waiter of the same ticket (whose
+  // entry the first one erases) gets an error instead of blocking forever
+  bool gone = false;
+  cv_done_.wait(lk, [&] {
+    auto it = done_.find(ticket);
+    gone = it == done_.end();
+    return gone || it->second.done;
+  });
+  if (gone) {
+    *err = "wait: ticket already waited for";
+    return -1;
+  }
   Done d = done_[ticket];
   done_.erase(ticket);
   if (latency_ms) *latency_ms = d.latency_ms;
@@ -179,8 +196,10 @@ int ReconServer::reserve(int config, int nx, int ny, int nimages, int count, std
   const Key k{config, nx, ny, nimages};
   std::vector<Handle*> got;
   for (int i = 0; i < count; ++i) {
-    // hold the handles taken so far busy, so that each round makes a new one
-    Handle* h = acquire(k, err);
+    // hold the handles taken so far busy, so that each round makes a new one;
+    // never wait for memory here (the handles this call holds would not be
+    // released while it waits)
+    Handle* h = acquire(k, err, false);
     if (!h) break;
     got.push_back(h);
   }
@@ -214,16 +233,51 @@ size_t ReconServer::device_bytes_in_use()
   return in_use_;
 }
 
-void ReconServer::counters(long long* created, long long* evicted)
+void ReconServer::counters(long long* created, long long* evicted, long long* admission_waits)
 {
   std::lock_guard<std::mutex> lk(mu_);
   if (created) *created = created_;
   if (evicted) *evicted = evicted_;
+  if (admission_waits) *admission_waits = admission_waits_;
 }
 
-ReconServer::Handle* ReconServer::acquire(const Key& k, std::string* err)
+size_t ReconServer::device_bytes_held()
+{
+  std::lock_guard<std::mutex> lk(mu_);
+  size_t n = 0;
+  for (auto& h : handles_) n += h->sr->device_bytes();
+  return n;
+}
+
+int ReconServer::device() const { return device_; }
+
+bool ReconServer::planned_bytes(int config, int nx, int ny, int nimages, size_t* bytes, std::string* err)
+{
+  const Key k{config, nx, ny, nimages};
+  std::string cfg;
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    if (config < 0 || config >= (int)configs_.size()) {
+      *err = "plannedBytes: unknown configuration";
+      return false;
+    }
+    auto it = planned_.find(k);
+    if (it != planned_.end()) {
+      *bytes = it->second;
+      return true;
+    }
+    cfg = configs_[config];
+  }
+  if (!SIM_Reconstructor::plan_bytes(nx, ny, nimages, cfg, bytes, err)) return false;
+  std::lock_guard<std::mutex> lk(mu_);
+  planned_[k] = *bytes;
+  return true;
+}
+
+ReconServer::Handle* ReconServer::acquire(const Key& k, std::string* err, bool wait_for_memory)
 {
   std::string cfg;
+  size_t need = 0;
   {
     std::lock_guard<std::mutex> lk(mu_);
     for (auto& h : handles_)
@@ -232,40 +286,63 @@ ReconServer::Handle* ReconServer::acquire(const Key& k, std::string* err)
         return h.get();
       }
     cfg = configs_[std::get<0>(k)];
+    auto it = planned_.find(k);
+    if (it != planned_.end()) need = it->second;
   }
-  auto create = [&](std::string* e) {
-    return SIM_Reconstructor::from_shape(std::get<1>(k), std::get<2>(k), std::get<3>(k), cfg, e);
-  };
-  // deletes idle handles, least recently used first, until the handles fit
-  // the budget (or all idle ones)
-  auto evict_idle = [&](bool all) {
-    std::vector<SIM_Reconstructor*> doomed;
+  if (!need) {
+    if (!SIM_Reconstructor::plan_bytes(std::get<1>(k), std::get<2>(k), std::get<3>(k), cfg, &need, err))
+      return nullptr;
+    std::lock_guard<std::mutex> lk(mu_);
+    planned_[k] = need;
+  }
+  if (need > budget_) {
+    *err = "request needs " + std::to_string(need >> 20) + " MiB of device memory, more than the server's budget";
+    return nullptr;
+  }
+  // admission: reserve `need` bytes within the budget, deleting idle handles
+  // (least recently used first) or waiting for busy ones to be released
+  for (;;) {
+    SIM_Reconstructor* doomed = nullptr;
     {
-      std::lock_guard<std::mutex> lk(mu_);
-      while (all || in_use_ > budget_) {
-        Handle* lru = nullptr;
-        size_t idx = 0;
-        for (size_t i = 0; i < handles_.size(); ++i)
-          if (!handles_[i]->busy && (!lru || handles_[i]->last_used < lru->last_used)) {
-            lru = handles_[i].get();
-            idx = i;
-          }
-        if (!lru) break;
+      std::unique_lock<std::mutex> lk(mu_);
+      for (auto& h : handles_)  // a handle of this shape may have been released meanwhile
+        if (!h->busy && h->key == k) {
+          h->busy = true;
+          return h.get();
+        }
+      if (in_use_ + need <= budget_) {
+        in_use_ += need;
+        break;
+      }
+      Handle* lru = nullptr;
+      size_t idx = 0;
+      for (size_t i = 0; i < handles_.size(); ++i)
+        if (!handles_[i]->busy && (!lru || handles_[i]->last_used < lru->last_used)) {
+          lru = handles_[i].get();
+          idx = i;
+        }
+      if (lru) {
         in_use_ -= lru->bytes;
         ++evicted_;
-        doomed.push_back(lru->sr);
+        doomed = lru->sr;
         handles_.erase(handles_.begin() + idx);
+      } else if (!wait_for_memory) {
+        *err = "the server's device-memory budget is taken by busy handles";
+        return nullptr;
+      } else {
+        ++admission_waits_;
+        cv_release_.wait(lk);
+        continue;
       }
     }
-    for (auto* sr : doomed) delete sr;
-  };
-  std::string e1;
-  SIM_Reconstructor* sr = create(&e1);
-  if (!sr) {
-    evict_idle(true);
-    sr = create(&e1);
+    delete doomed;  // outside the lock: frees device memory
   }
+  std::string e1;
+  SIM_Reconstructor* sr = SIM_Reconstructor::from_shape(std::get<1>(k), std::get<2>(k), std::get<3>(k), cfg, &e1);
   if (!sr) {
+    std::lock_guard<std::mutex> lk(mu_);
+    in_use_ -= need;
+    cv_release_.notify_all();
     *err = e1;
     return nullptr;
   }
@@ -273,30 +350,27 @@ ReconServer::Handle* ReconServer::acquire(const Key& k, std::string* err)
   h->key = k;
   h->sr = sr;
   h->busy = true;
-  h->bytes = sr->device_bytes();
+  h->bytes = need;
   Handle* raw = h.get();
-  {
-    std::lock_guard<std::mutex> lk(mu_);
-    in_use_ += h->bytes;
-    ++created_;
-    handles_.push_back(std::move(h));
-  }
-  evict_idle(false);
+  std::lock_guard<std::mutex> lk(mu_);
+  ++created_;
+  handles_.push_back(std::move(h));
   return raw;
 }
 
 void ReconServer::release(Handle* h)
 {
-  std::lock_guard<std::mutex> lk(mu_);
-  const size_t nb = h->sr->device_bytes();  // grows when a chunk first used the series buffers
-  in_use_ = in_use_ - h->bytes + nb;
-  h->bytes = nb;
-  h->busy = false;
-  h->last_used = now_s();
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    h->busy = false;
+    h->last_used = now_s();
+  }
+  cv_release_.notify_all();
 }
 
 void ReconServer::worker_loop()
 {
+  cudaSetDevice(device_);
   for (;;) {
     Request r;
     {

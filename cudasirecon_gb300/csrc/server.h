@@ -41,9 +41,18 @@ class ReconServer {
   int set_k0_reuse(int config, bool on, std::string* err);
   // the recorded k0 of a configuration (2 floats per direction); false if none
   bool recorded_k0(int config, std::vector<float>* k0);
+  // device bytes reserved against the budget by the pooled handles (each
+  // handle's planned maximum); never above the budget
   size_t device_bytes_in_use();
-  // handles created and deleted (budget evictions) since construction
-  void counters(long long* created, long long* evicted);
+  // device bytes the pooled handles actually hold now (at most the reserved)
+  size_t device_bytes_held();
+  // handles created and deleted (budget evictions) since construction, and
+  // how often a request waited for device memory to be released
+  void counters(long long* created, long long* evicted, long long* admission_waits = nullptr);
+  int device() const;
+  // planned device bytes of a handle for this configuration and shape (what
+  // admission reserves for it); false with the error if it cannot be planned
+  bool planned_bytes(int config, int nx, int ny, int nimages, size_t* bytes, std::string* err);
   // create handles for a shape up front so that the first requests of that
   // shape do not pay for their creation; returns how many were created
   int reserve(int config, int nx, int ny, int nimages, int count, std::string* err);
@@ -89,7 +98,7 @@ class ReconServer {
     size_t bytes = 0;
   };
   void worker_loop();
-  Handle* acquire(const Key& k, std::string* err);
+  Handle* acquire(const Key& k, std::string* err, bool wait_for_memory = true);
   long long enqueue(Request r);
   void release(Handle* h);
 
@@ -100,13 +109,15 @@ class ReconServer {
   };
   std::vector<ConfigState> cstate_;
   std::mutex mu_;
-  std::condition_variable cv_work_, cv_done_;
+  std::condition_variable cv_work_, cv_done_, cv_release_;
   std::deque<Request> queue_;
   std::map<long long, Done> done_;
   std::vector<std::unique_ptr<Handle>> handles_;
   size_t budget_, in_use_ = 0;
+  std::map<Key, size_t> planned_;  // planned device bytes per (configuration, shape)
+  int device_ = 0;
   long long next_ticket_ = 1;
-  long long created_ = 0, evicted_ = 0;
+  long long created_ = 0, evicted_ = 0, admission_waits_ = 0;
   bool stop_ = false;
   std::vector<std::thread> workers_;
 };

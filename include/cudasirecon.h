@@ -216,19 +216,25 @@ int SRX_pinHost(void* ptr, size_t bytes);
 int SRX_fftSelfTest(float* data, int n, int nlines, int inverse, int columns);
 
 /* No counterpart in the reference.  The same line transform for callers
- * that must not allocate device memory (code running inside a CUDA graph
- * capture, real-time acquisition loops, plug-in hosts that own the device's
- * memory): `in` and `out` are host arrays of nlines x n complex values; the
- * device staging buffer and twiddle table live in a fixed 16 MiB file-scope
- * device array, so no cudaMalloc/cudaFree is made.  At most 2 Mi complex
- * values per call and n <= 8192; larger requests return -1 without running.
- * Calls share the array: calls that overlap on the GPU race.  The first call
- * on a device looks up the array's address; make it before any stream
- * capture.  Returns 0 on success; SRX_fftLinesNoAllocError() describes a
- * failure. */
+ * that must not allocate device memory (real-time acquisition loops, where an
+ * allocation's implicit synchronisation stalls the camera pipeline, and
+ * plug-in hosts that own the device's memory): `in` and `out` are host arrays
+ * of nlines x n complex values; the device staging buffer and twiddle table
+ * live in a fixed 16 MiB file-scope device array, so no cudaMalloc/cudaFree
+ * is made.  A synchronous host-to-host call (blocking copies and launches on
+ * the default stream).  At most 2 Mi complex values per call and n <= 8192
+ * (in the column layout n <= 7264, the per-CTA shared-memory limit); larger
+ * requests return -1 without running and leave `out` unwritten.  Calls share
+ * the array: calls that overlap on the GPU race.  The first call on a device
+ * looks up the array's address; make it before any stream capture.  Returns
+ * 0 on success; SRX_fftLinesNoAllocError() describes a failure. */
 int SRX_fftLinesNoAlloc(const float* in, float* out, int n, int nlines, int inverse, int columns);
 const char* SRX_fftLinesNoAllocError(void);
 int SRX_unpinHost(void* ptr);
+
+/* No counterpart in the reference.  Free and total device memory of the
+ * current device (cudaMemGetInfo); returns 0 on success. */
+int SRX_deviceMemInfo(size_t* free_bytes, size_t* total_bytes);
 
 /* No counterpart in the reference.  Reconstruct n volumes of a time series:
  * for volume i the same as SR_setRaw(raws[i]) (SR_setRawU16 when
@@ -247,8 +253,8 @@ int SRX_processSeries(SIM_Reconstructor* sr, const void* const* raws, int raw_is
  * different shapes and acquisition configurations: worker threads run the
  * SR_* flow on pooled handles (one per configuration, shape and worker, each
  * with its own CUDA stream), so requests overlap on the GPU; the handles are
- * kept within hbm_budget_bytes of device memory (idle ones evicted least
- * recently used first).  A configuration is a reference-style config file
+ * admitted within hbm_budget_bytes of device memory (idle ones evicted least
+ * recently used first, else the request waits for a busy one to finish).  A configuration is a reference-style config file
  * that names its OTF (otf-file=).  Each request is one volume in the
  * SR_setRaw layout, processed as a time-0 volume (k0 fitted), its result
  * written in the SR_getResult layout; raw and out stay the caller's and must
@@ -286,7 +292,16 @@ int SRX_serverRunBatch(SRX_Server* s, const SRX_BatchItem* items, int n);
  * workers, without running it (no GPU needed): chunk_of_item[i] = the chunk
  * (in execution order) of item i; returns the number of chunks, or -1. */
 int SRX_batchPlan(const SRX_BatchItem* items, int n, int workers, int* chunk_of_item);
+/* Device bytes reserved against the budget by the pooled handles: a handle's
+ * bytes are planned from its shape and configuration before it is created
+ * (every buffer it can come to hold) and a request waits until they fit, so
+ * this never exceeds hbm_budget_bytes.  DeviceBytesHeld: what the handles
+ * actually hold now (at most the reserved bytes). */
 size_t SRX_serverDeviceBytes(SRX_Server* s);
+size_t SRX_serverDeviceBytesHeld(SRX_Server* s);
+/* The bytes admission reserves for a handle of this configuration and shape
+ * (planned without allocating); 0 on error (SR_getLastError). */
+size_t SRX_serverPlannedBytes(SRX_Server* s, int config, int nx, int ny, int nimages);
 /* k0 kept per acquisition configuration (off by default).  With it on, the
  * first submitted request of the configuration to finish searches k0 as
  * usual and the server records it; every later submitted request of that
@@ -301,6 +316,8 @@ int SRX_serverSetK0Reuse(SRX_Server* s, int config, int on);
 int SRX_serverRecordedK0(SRX_Server* s, int config, float* k0, int ndirs);
 /* Handles created, and handles deleted to stay within the budget, so far. */
 void SRX_serverCounters(SRX_Server* s, long long* created, long long* evicted);
+/* How often a request waited for busy handles to release device memory. */
+long long SRX_serverAdmissionWaits(SRX_Server* s);
 void SRX_serverDestroy(SRX_Server* s);
 
 /* makeotf.  The reference's makeotf is a program, not a library call

@@ -23,24 +23,78 @@ def plain(case):
     return out
 
 
-@pytest.mark.parametrize("budget", [150e9, 1.0], ids=["roomy", "evict-every-time"])
-def test_server_matches_plain(budget):
+@pytest.mark.parametrize("budget", ["roomy", "one-handle"])
+def test_server_matches_plain_within_budget(budget):
+    """Every result equals the plain flow's, alone or in the mix.  With room
+    for only the largest handle, requests of other shapes wait for it to be
+    released and idle handles are deleted: the reserved bytes, polled while
+    the requests run, never exceed the budget, and the bytes actually held
+    never exceed the reserved ones."""
+    import threading
     cases = {n: load(n)[0] for n in CASES}
     want = {n: plain(c) for n, c in cases.items()}
-    srv = sr.Server(workers=3, hbm_budget=budget)
+    probe = sr.Server(workers=1)
+    pcfg = {n: probe.add_config(c["config"], c["otf"]) for n, c in cases.items()}
+    planned = {n: probe.planned_bytes(pcfg[n], c["nx"], c["ny"], c["raw"].shape[1]) for n, c in cases.items()}
+    probe.close()
+    cap = 150e9 if budget == "roomy" else max(planned.values())
+    srv = sr.Server(workers=3, hbm_budget=cap)
     cfg = {n: srv.add_config(c["config"], c["otf"]) for n, c in cases.items()}
+    seen, stop = [], threading.Event()
+
+    def poll():
+        while not stop.is_set():
+            seen.append((srv.device_bytes(), srv.device_bytes_held()))
+
+    th = threading.Thread(target=poll)
+    th.start()
     jobs = []
-    for rep in range(3):
-        for n, c in cases.items():
-            raw = np.ascontiguousarray(c["raw"][0])
-            out = np.zeros(want[n].shape, np.float32)
-            jobs.append((n, out, srv.submit(cfg[n], raw, out)))
-    for n, out, t in jobs:
-        lat = srv.wait(t)
-        assert lat > 0
-        assert np.array_equal(out, want[n]), n
-    if budget > 1e9:
-        assert srv.device_bytes() > 0  # handles stay pooled for the next requests
+    try:
+        for rep in range(3):
+            for n, c in cases.items():
+                raw = np.ascontiguousarray(c["raw"][0])
+                out = np.zeros(want[n].shape, np.float32)
+                jobs.append((n, out, srv.submit(cfg[n], raw, out)))
+        for n, out, t in jobs:
+            lat = srv.wait(t)
+            assert lat > 0
+            assert np.array_equal(out, want[n]), n
+    finally:
+        stop.set()
+        th.join()
+    assert seen and max(r for r, _ in seen) <= cap
+    assert all(h <= r for r, h in seen)
+    assert srv.device_bytes() > 0  # handles stay pooled for the next requests
+    if budget == "one-handle":
+        c = srv.counters()
+        assert c["evicted"] > 0 and c["admission_waits"] > 0, c
+    srv.close()
+
+
+def test_server_request_larger_than_budget_fails_cleanly():
+    case, _ = load("c3d_64")
+    srv = sr.Server(workers=1, hbm_budget=1 << 20)
+    cid = srv.add_config(case["config"], case["otf"])
+    raw = np.ascontiguousarray(case["raw"][0])
+    out = np.zeros((24, 128, 128), np.float32)
+    t = srv.submit(cid, raw, out)
+    with pytest.raises(sr.SIReconError, match="budget"):
+        srv.wait(t)
+    assert srv.device_bytes() == 0
+    srv.close()
+
+
+def test_server_second_wait_on_a_ticket_is_an_error():
+    case, _ = load("c3d_64")
+    want = plain(case)
+    srv = sr.Server(workers=1)
+    cid = srv.add_config(case["config"], case["otf"])
+    raw = np.ascontiguousarray(case["raw"][0])
+    out = np.zeros(want.shape, np.float32)
+    t = srv.submit(cid, raw, out)
+    srv.wait(t)
+    with pytest.raises(sr.SIReconError):
+        srv.wait(t)
     srv.close()
 
 
