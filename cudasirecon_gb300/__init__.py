@@ -75,6 +75,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.SRX_benchDevice.restype = ip
     lib.SRX_benchDevice.argtypes = [vp, ip, C.POINTER(C.c_double)]
     lib.SRX_setProfiling.argtypes = [vp, ip]
+    lib.SRX_setFilterFusion.restype = None
+    lib.SRX_setFilterFusion.argtypes = [vp, ip]
     lib.SRX_getProfile.restype = ip
     lib.SRX_getProfile.argtypes = [vp, C.c_char_p, ip]
     lib.SRX_resetProfile.argtypes = [vp]
@@ -323,6 +325,11 @@ class Reconstructor:
 
     def set_profiling(self, on: bool = True):
         self.lib.SRX_setProfiling(self.h, int(on))
+
+    def set_filter_fusion(self, on: bool = True):
+        """Wiener filter inside the assembly's band load (default) or as its
+        own pass (SRX_setFilterFusion)."""
+        self.lib.SRX_setFilterFusion(self.h, int(on))
 
     def profile(self) -> dict:
         import json

@@ -49,8 +49,24 @@ struct FilterK {
   float rdkrotf;                       // 1 / dkrotf
   float min_dkr, rmin_dkr, supp_r;     // suppression radius (1/um) and its unit
   float rrcut;                         // 1 / rdistcutoff
-  float cut2hi;                        // rdistcutoff^2 (1 + 1e-6): rejects only terms outside the support
+  // exact squared-radius forms of the reference's float-radius decisions
+  // (sqrtf is correctly rounded and monotonic): sqrtf(r2) < rdistcutoff
+  // <=> r2 < r2_in, sqrtf(r2) <= suppRadius <=> r2 <= r2_supp
+  float r2_in, r2_supp;
+  float rapo, rzapo;                   // 1 / apocutoff, 1 / zapocutoff
+  // every direction's order-0 noise factor is the same (the reference's are
+  // all 1): the order-0 Wiener denominator is then one sum for all directions
+  int order0_shared;
 };
+
+// hardware square root (about 1 ulp): only for the continuous OTF
+// interpolation index, never for a decision
+__device__ __forceinline__ float sqrt_approx(float x)
+{
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
 
 // Wiener scale of pixel (x1f, y1f, z0) of band (dir, order): the body of
 // filterbands_kernel1 (gpuFunctionsImpl.cu:1504-1592) without the final
@@ -80,13 +96,12 @@ __device__ __forceinline__ float2 filter_otf(const FilterArgs& a, const float2* 
 // registers on the compile-time paths); ampmag2: |amp|^2 of this band.
 template <int ND, int NO, bool CLAMP, bool TAB, int FL>
 __device__ __forceinline__ float2 filter_scale(const FilterArgs& a, const FilterK& k, const float* termw,
-                                               float ampmag2, int order, int z0, float rdist1, float x1f, float y1f,
-                                               const float2* tabz)
+                                               float ampmag2, int dir, int order, int z0, float rdist1, float x1f,
+                                               float y1f, const float2* tabz)
 {
   const bool suppress = FL >= 0 ? (FL & 1) != 0 : a.suppress != 0;
   const bool dampen0 = FL >= 0 ? (FL & 2) != 0 : a.dampen0 != 0;
   const bool filteroverlaps = FL >= 0 ? (FL & 4) != 0 : a.filteroverlaps != 0;
-  const int dir = a.dir;
   const int nd = ND ? ND : a.ndirs, no = NO ? NO : a.norders;
   const float xabs = x1f + k.kxo[dir * no + order], yabs = y1f + k.kyo[dir * no + order];
   const OtfKz kzi = otf_kz(a.otf, z0);
@@ -119,14 +134,13 @@ __device__ __forceinline__ float2 filter_scale(const FilterArgs& a, const Filter
       const float sy = order2 < 0 ? -k.kyo[dir2 * no + ao2] : k.kyo[dir2 * no + ao2];
       const float x2 = xabs - sx, y2 = yabs - sy;
       const float r2 = x2 * x2 + y2 * y2;
-      if (r2 >= k.cut2hi) continue;  // far outside: the exact test below would fail too
-      const float rdist2 = sqrtf(r2);
-      if (rdist2 < a.rdistcutoff) {
+      if (r2 < k.r2_in) {  // rdist2 < rdistcutoff
+        const float rdist2 = sqrt_approx(r2);
         const float2 otf2 = filter_otf<CLAMP, TAB>(a, tabz, ao2, rdist2 * k.rdkrotf, kzi);
         float w = (otf2.x * otf2.x + otf2.y * otf2.y) * termw[dir2 * no + ao2];
-        if (suppress && order2 != 0 && rdist2 <= k.supp_r)
+        if (suppress && order2 != 0 && r2 <= k.r2_supp)
           w *= dev_suppress(rdist2 * k.rmin_dkr);
-        else if (!dampen0 && suppress && order2 == 0 && rdist2 <= k.supp_r)
+        else if (!dampen0 && suppress && order2 == 0 && r2 <= k.r2_supp)
           w *= dev_suppress(rdist2 * k.rmin_dkr);
         else if (dampen0 && order2 == 0) {
           const float rf = rdist2 * k.rrcut;
@@ -144,11 +158,13 @@ __device__ __forceinline__ float2 filter_scale(const FilterArgs& a, const Filter
     float rdistabs = sqrtf(xabs * xabs + yabs * yabs);
     float rho;
     float zdistabs = abs(z0);
-    if (a.zapocutoff > 0)
-      rho = sqrtf((rdistabs / a.apocutoff) * (rdistabs / a.apocutoff) +
-                  (zdistabs / a.zapocutoff) * (zdistabs / a.zapocutoff));
-    else
-      rho = sqrtf((rdistabs / a.apocutoff) * (rdistabs / a.apocutoff));
+    const float ra = rdistabs * k.rapo;
+    if (a.zapocutoff > 0) {
+      const float rz = zdistabs * k.rzapo;
+      rho = sqrtf(ra * ra + rz * rz);
+    } else {
+      rho = ra;
+    }
     if (rho > 1.f) rho = 1.0f;
     float apofact = 1.f;
     if (a.apodizeoutput == 1) apofact = cosf(1.57079632679f * rho);
@@ -226,37 +242,39 @@ __global__ void __launch_bounds__(kThreads) k_filter(const __grid_constant__ Fil
     if (b2) b2[ind] = make_float2(0.f, 0.f);
     return;
   }
-  // the fitted amplitudes' weights, read once per thread
-  constexpr int kTw = ND > 0 && NO > 0 ? ND * NO : 1;
-  float twr[kTw];
-  const float* termw = a.fit->termw;
-  if (ND > 0 && NO > 0) {
-#pragma unroll
-    for (int i = 0; i < kTw; ++i) twr[i] = __ldg(a.fit->termw + i);
-    termw = twr;
-  }
   const float ampmag2 = __ldg(a.fit->ampmag2 + a.dir * a.norders + order);
   const float2 amp = __ldg(a.fit->amp + a.dir * a.norders + order);
   const float2 conjamp = make_float2(amp.x, -amp.y);
-  float2 s1 = filter_scale<ND, NO, CLAMP, TAB, FL>(a, k, termw, ampmag2, order, z0, rdist1, x1f, y1f, tab);
-  if (order == 0) {
-    b1[ind] = cmul(b1[ind], s1);
-    return;
+  auto body = [&](const float* termw) {
+    float2 s1 = filter_scale<ND, NO, CLAMP, TAB, FL>(a, k, termw, ampmag2, a.dir, order, z0, rdist1, x1f, y1f, tab);
+    if (order == 0) {
+      b1[ind] = cmul(b1[ind], s1);
+      return;
+    }
+    float2 re = b1[ind], im = b2[ind];
+    apply_side(re, im, cmul(s1, conjamp), false);
+    if (jin >= 1 && jin <= nx / 2 - 1) {
+      // second pass: the conjugate pixel (-jin, -y, -z0)
+      const int y2 = (iin <= ny / 2) ? -iin : ny - iin;
+      const int x2 = -jin;
+      float x2f = x2 * a.dkx, y2f = y2 * a.dky;
+      float rdist2 = sqrtf(x2f * x2f + y2f * y2f);
+      float2 s2 = filter_scale<ND, NO, CLAMP, TAB, FL>(a, k, termw, ampmag2, a.dir, order, -z0, rdist2, x2f, y2f,
+                                                       tab + (TAB ? NO * a.otf.nxotf : 0));
+      apply_side(re, im, cmul(s2, conjamp), true);
+    }
+    b1[ind] = re;
+    b2[ind] = im;
+  };
+  // the fitted amplitudes' weights: in registers on the compile-time paths
+  if constexpr (ND > 0 && NO > 0) {
+    float twr[ND * NO];
+#pragma unroll
+    for (int i = 0; i < ND * NO; ++i) twr[i] = __ldg(a.fit->termw + i);
+    body(twr);
+  } else {
+    body(a.fit->termw);
   }
-  float2 re = b1[ind], im = b2[ind];
-  apply_side(re, im, cmul(s1, conjamp), false);
-  if (jin >= 1 && jin <= nx / 2 - 1) {
-    // second pass: the conjugate pixel (-jin, -y, -z0)
-    const int y2 = (iin <= ny / 2) ? -iin : ny - iin;
-    const int x2 = -jin;
-    float x2f = x2 * a.dkx, y2f = y2 * a.dky;
-    float rdist2 = sqrtf(x2f * x2f + y2f * y2f);
-    float2 s2 = filter_scale<ND, NO, CLAMP, TAB, FL>(a, k, termw, ampmag2, order, -z0, rdist2, x2f, y2f,
-                                                     tab + (TAB ? NO * a.otf.nxotf : 0));
-    apply_side(re, im, cmul(s2, conjamp), true);
-  }
-  b1[ind] = re;
-  b2[ind] = im;
 }
 
 // One transformed plane: band (dir, order) at signed kz, summed into output
@@ -468,6 +486,170 @@ __global__ void __launch_bounds__(kThreads, 2) k_asm_y4(AssembleArgs a, const Sl
   float2* dst = a.T + (size_t)blockIdx.y * Y * nx + c0;
   colfft_stage2<Y, R1, W, +1>(sm, [&](int yr, int w, float2 v) {
     if (c0 + w < nx) dst[(size_t)yr * nx + w] = v;
+  });
+}
+
+// k_asm_y4 with the Wiener filter fused into its band load (filterbands,
+// gpuFunctionsImpl.cu:1222-1675, feeding move_kernel, 1853-1913): the bands
+// are read unfiltered, once, and no filter pass writes them back.
+//
+// The reference's first filter pass scales only the plus part (re + i im) of
+// a stored element and its second pass only the minus part (re - i im, the
+// conjugate pixel), so the assembled value needs one scale per read: at the
+// pixel (kx, ky', kz) for the plus part (kx >= 0) and for the conjugate part
+// (kx < 0) alike, where ky' = ky except ky' = -ny/2 for the stored row ny/2
+// (both filter passes index rows as y in [-ny/2, ny/2-1]).  Order 0 is
+// filtered at its stored element's own pixel and conjugated for kx < 0, summed
+// over the directions; with equal order-0 noise factors the directions share
+// one Wiener denominator (each direction's own term equals the order-0 term of
+// the other directions' sums), so it is evaluated once.  Pixels outside the lateral support are zero and not
+// read; planes outside each order's zdistcutoff are never assembled.
+//
+// Phase A: the filtered band values of the CTA's 8 columns on the ny data
+// rows, row-major in shared memory (a runtime loop: one copy of the filter
+// code).  Stage 1 then reads its strided rows from there (the zero-padding
+// rows read as zero; one barrier between the reads and the stage-1 stores into
+// the same buffer), stage 2 as k_asm_y4.  The per-kz OTF radial tables of the
+// filter (for kz and, for order 0, -kz) follow the transform buffer.
+template <int Y, int NO, int FL>
+__global__ void __launch_bounds__(kThreads, 2) k_asm_y4f(AssembleArgs a, const Slot* __restrict__ slots,
+                                                     const float2* __restrict__ tw,
+                                                     const __grid_constant__ FilterArgs fa,
+                                                     const __grid_constant__ FilterK fk)
+{
+  constexpr int ND = 3;
+  constexpr int R1 = colfft_r1(Y), W = 8;
+  using CF = ColFft<Y, R1, W>;
+  constexpr int R2 = CF::R2;
+  static_assert(R2 * W <= kThreads, "one stage-1 item per thread");
+  static_assert(Y * W <= CF::kSmemElems, "phase A fits the transform buffer");
+  extern __shared__ float2 sm[];
+  float2* tab = sm + CF::kSmemElems;  // [2][NO][nxotf]
+  const Slot sl = slots[blockIdx.y];
+  const int nx = a.nx, ny = a.ny, nz = a.nz, nxh = nx / 2 + 1;
+  const int c0 = blockIdx.x * W;
+  const size_t plane = (size_t)ny * nxh;
+  const int order = sl.order;
+  const int d0 = sl.dir < 0 ? 0 : sl.dir;
+  const float2* br = a.bands + ((size_t)d0 * a.nphases + (order == 0 ? 0 : 2 * order - 1)) * nz * plane;
+  const float2* bi = order == 0 ? nullptr : a.bands + ((size_t)d0 * a.nphases + 2 * order) * nz * plane;
+  const size_t dstride = (size_t)a.nphases * nz * plane;  // next direction's band 0
+  const int ylo = ny / 2 - 1;                              // ky in [-ylo, ny/2]
+  {  // OTF of every order interpolated to kz (pass 0) and -kz (pass 1) along kr
+    const int nxo = fa.otf.nxotf, nzo = fa.otf.nzotf;
+    for (int t = threadIdx.x; t < 2 * NO * nxo; t += blockDim.x) {
+      const int pass = t / (NO * nxo), r = t - pass * NO * nxo, o = r / nxo, ir = r - o * nxo;
+      const OtfKz kz = otf_kz(fa.otf, pass ? -sl.kz : sl.kz);
+      const float2 va = __ldg(fa.otf.otf[o] + ir * nzo + kz.iz), vb = __ldg(fa.otf.otf[o] + ir * nzo + kz.izp);
+      tab[t] = make_float2(va.x * (1 - kz.az) + vb.x * kz.az, va.y * (1 - kz.az) + vb.y * kz.az);
+    }
+  }
+  float termw[ND * NO];
+#pragma unroll
+  for (int i = 0; i < ND * NO; ++i) termw[i] = __ldg(fa.fit->termw + i);
+  float ampmag2 = 0.f;
+  float2 conjamp = make_float2(1.f, 0.f);
+  if (order != 0) {
+    ampmag2 = __ldg(fa.fit->ampmag2 + d0 * NO + order);
+    const float2 am = __ldg(fa.fit->amp + d0 * NO + order);
+    conjamp = make_float2(am.x, -am.y);
+  }
+  __syncthreads();
+  // phase A over the ny data rows (ky in [-ylo, ny/2]); not unrolled (two
+  // copies of the filter code in flight measured 46 % slower)
+  for (int t = threadIdx.x; t < ny * W; t += blockDim.x) {
+    const int r = t / W, w = t - r * W;
+    const int yr = r <= ny / 2 ? r : r + (Y - ny);
+    const int ky = r <= ny / 2 ? r : r - ny;
+    const int c = c0 + w;
+    float2 v = make_float2(0.f, 0.f);
+    if (c < nx) {
+      const int kx = c - (nx / 2 - 1);
+      const int kyf = ky == ny / 2 ? -(ny / 2) : ky;
+      const float x1f = kx * fa.dkx, y1f = kyf * fa.dky;
+      const float rdist1 = sqrtf(x1f * x1f + y1f * y1f);
+      if (rdist1 <= fa.rdistcutoff) {
+        int x = kx, y = ky, z = sl.kz;
+        const bool conj = x < 0;
+        if (conj) {
+          x = -x;
+          y = -y;
+          z = -z;
+        }
+        if (y < 0) y += ny;
+        if (z < 0) z += nz;
+        const size_t indin = (size_t)z * plane + (size_t)y * nxh + x;
+        if (order == 0) {
+          // each direction's order-0 band at the stored element's own pixel
+          const float xs = conj ? -x1f : x1f;
+          const float ys = conj ? (float)(-ky) * fa.dky : y1f;
+          const int zs = conj ? -sl.kz : sl.kz;
+          const float2* tz = tab + (conj ? NO * fa.otf.nxotf : 0);
+          if (fk.order0_shared) {
+            // one denominator for every direction: direction d's own term and
+            // the (d, 0) term its sum skips are the same OTF value
+            const float2 sc = filter_scale<ND, NO, false, true, FL>(fa, fk, termw, 0.f, 0, 0, zs, rdist1, xs, ys, tz);
+            float2 b = br[indin];
+#pragma unroll
+            for (int d = 1; d < ND; ++d) {
+              const float2 u = br[d * dstride + indin];
+              b.x += u.x;
+              b.y += u.y;
+            }
+            v = cmul(b, sc);
+          } else {
+#pragma unroll 1
+            for (int d = 0; d < ND; ++d) {
+              const float2 sc =
+                  filter_scale<ND, NO, false, true, FL>(fa, fk, termw, 0.f, d, 0, zs, rdist1, xs, ys, tz);
+              const float2 b = br[d * dstride + indin];
+              v.x += b.x * sc.x - b.y * sc.y;
+              v.y += b.x * sc.y + b.y * sc.x;
+            }
+          }
+          if (conj) v.y = -v.y;
+        } else {
+          const float2 sc = filter_scale<ND, NO, false, true, FL>(fa, fk, termw, ampmag2, d0, order, sl.kz, rdist1,
+                                                                   x1f, y1f, tab);
+          float2 re = br[indin], im = bi[indin];
+          if (conj) {
+            re.y = -re.y;
+            im.y = -im.y;
+          }
+          v = cmul(make_float2(re.x - im.y, re.y + im.x), cmul(sc, conjamp));
+        }
+      }
+    }
+    sm[yr * W + w] = v;
+  }
+  __syncthreads();
+  // stage 1 from the row-major values (zero-padding rows read as zero)
+  const int it = threadIdx.x;
+  const bool has1 = it < R2 * W;
+  const int cc = it % W, j = it / W;
+  float2 v[R1];
+#pragma unroll
+  for (int e = 0; e < R1; ++e) {
+    const int yr = j + R2 * e;
+    const bool data = yr <= ny / 2 || yr >= Y - ylo;
+    v[e] = has1 && data ? sm[yr * W + cc] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  if (has1) {
+    reg_dft<R1, +1>(v);
+#pragma unroll
+    for (int k1 = 1; k1 < R1; ++k1) {
+      float2 w = __ldg(tw + j * k1);
+      w.y = -w.y;
+      v[k1] = cmul(v[k1], w);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < R1; ++k1) sm[k1 * CF::LD1 + j * W + cc] = v[k1];
+  }
+  __syncthreads();
+  float2* dst = a.T + (size_t)blockIdx.y * Y * nx + c0;
+  colfft_stage2<Y, R1, W, +1>(sm, [&](int yr, int w, float2 val) {
+    if (c0 + w < nx) dst[(size_t)yr * nx + w] = val;
   });
 }
 
@@ -748,10 +930,28 @@ DevTables dev_tables(const AssembleArgs& a, const HostTables& t)
 
 }  // namespace
 
-int launch_filter(const FilterArgs& a, cudaStream_t s, long long* launches)
+namespace {
+// smallest float t with sqrtf(t) >= c: for every float r2, r2 < t <=> sqrtf(r2) < c
+float r2_below(float c)
 {
-  const int nxh = a.nx / 2 + 1;
-  dim3 g((a.ny * nxh + kThreads - 1) / kThreads, a.nz, a.norders);
+  float t = c * c;
+  while (t > 0.f && std::sqrt(t) >= c) t = std::nextafter(t, 0.f);
+  while (std::sqrt(t) < c) t = std::nextafter(t, INFINITY);
+  return t;
+}
+
+// largest float t with sqrtf(t) <= c: r2 <= t <=> sqrtf(r2) <= c
+float r2_atmost(float c)
+{
+  if (!(c >= 0.f)) return -1.f;
+  float t = c * c;
+  while (t > 0.f && std::sqrt(t) > c) t = std::nextafter(t, 0.f);
+  while (std::sqrt(std::nextafter(t, INFINITY)) <= c) t = std::nextafter(t, INFINITY);
+  return t;
+}
+
+FilterK make_filter_k(const FilterArgs& a)
+{
   FilterK k{};
   const int no = a.norders;
   for (int d = 0; d < a.ndirs; ++d)
@@ -766,12 +966,41 @@ int launch_filter(const FilterArgs& a, cudaStream_t s, long long* launches)
   k.rmin_dkr = 1.f / k.min_dkr;
   k.supp_r = a.supp_radius * k.min_dkr;
   k.rrcut = 1.f / a.rdistcutoff;
-  k.cut2hi = (float)((double)a.rdistcutoff * a.rdistcutoff * (1.0 + 1e-6));
-  // every looked-up radius is <= rdistcutoff, so the table is never left
-  // when floor(rdistcutoff / dkrotf) + 2 <= nxotf
-  // (and no kz index, |kz| <= nz/2, leaves it along kz)
-  const bool clamp = !(std::floor(a.rdistcutoff * k.rdkrotf) + 2 <= a.otf.nxotf) ||
-                     !(a.nz == 1 || (a.nz / 2) * (double)a.otf.kzscale + 1.0 < a.otf.nzotf);
+  k.r2_in = r2_below(a.rdistcutoff);
+  k.r2_supp = r2_atmost(k.supp_r);
+  k.rapo = 1.f / a.apocutoff;
+  k.rzapo = a.zapocutoff > 0 ? 1.f / a.zapocutoff : 0.f;
+  k.order0_shared = 1;
+  for (int d = 1; d < a.ndirs; ++d)
+    if (a.noisevar[d * no] != a.noisevar[0]) k.order0_shared = 0;
+  return k;
+}
+
+// Every looked-up radius is <= rdistcutoff, so the table is never left when
+// floor(rdistcutoff / dkrotf) + 3 <= nxotf (+ 3: a cross term's interpolation
+// radius comes from an approximate square root and may pass rdistcutoff by
+// an ulp) and no kz index, |kz| <= nz/2, leaves it along kz; otherwise the
+// lookups clamp
+bool filter_needs_clamp(const FilterArgs& a, const FilterK& k)
+{
+  return !(std::floor(a.rdistcutoff * k.rdkrotf) + 3 <= a.otf.nxotf) ||
+         !(a.nz == 1 || (a.nz / 2) * (double)a.otf.kzscale + 1.0 < a.otf.nzotf);
+}
+
+// the switches fixed at compile time on the table path
+int filter_flags(const FilterArgs& a)
+{
+  return (a.suppress ? 1 : 0) | (a.dampen0 ? 2 : 0) | (a.filteroverlaps ? 4 : 0);
+}
+}  // namespace
+
+int launch_filter(const FilterArgs& a, cudaStream_t s, long long* launches)
+{
+  const int nxh = a.nx / 2 + 1;
+  dim3 g((a.ny * nxh + kThreads - 1) / kThreads, a.nz, a.norders);
+  const FilterK k = make_filter_k(a);
+  const int no = a.norders;
+  const bool clamp = filter_needs_clamp(a, k);
   KernelTimer* kt = kernel_timer();
   if (kt) kt->begin(s);
   // per-plane radial tables when the lookups stay inside the table and the
@@ -779,7 +1008,7 @@ int launch_filter(const FilterArgs& a, cudaStream_t s, long long* launches)
   const size_t tabb = 2 * (size_t)no * a.otf.nxotf * sizeof(float2);
   const bool tab = !clamp && tabb <= 48 * 1024;
   // the table path with the three switches fixed at compile time
-  const int fl = (a.suppress ? 1 : 0) | (a.dampen0 ? 2 : 0) | (a.filteroverlaps ? 4 : 0);
+  const int fl = filter_flags(a);
   auto tab_path = [&]<int NO>() {
     auto go = [&]<int FL>() { k_filter<3, NO, false, true, FL><<<g, kThreads, tabb, s>>>(a, k); };
     switch (fl) {
@@ -861,7 +1090,36 @@ int assemble_tables_upload(const AssembleArgs& a)
   return (int)e;
 }
 
+namespace {
+constexpr size_t kFusedTabMax = 32 * 1024;  // OTF tables of the fused kernel (two CTAs per SM stay resident)
+
+int assemble_impl(const AssembleArgs& a, const FilterArgs* filt, cudaStream_t s, long long* launches);
+}  // namespace
+
+bool assemble_filter_fusable(const AssembleArgs& a, const FilterArgs& f, bool one_otf)
+{
+  if (!one_otf || f.bessel || a.ndirs != 3 || f.ndirs != 3 || a.norders != f.norders) return false;
+  if (f.norders != 2 && f.norders != 3) return false;
+  if (!(a.Y == 1024 || a.Y == 512 || a.Y == 256) || a.nx != f.nx || a.ny != f.ny || a.nz != f.nz) return false;
+  const FilterK k = make_filter_k(f);
+  if (filter_needs_clamp(f, k)) return false;
+  return 2 * (size_t)f.norders * f.otf.nxotf * sizeof(float2) <= kFusedTabMax;
+}
+
+int launch_assemble_filtered(const AssembleArgs& a, const FilterArgs& f, bool one_otf, cudaStream_t s,
+                             long long* launches)
+{
+  if (!assemble_filter_fusable(a, f, one_otf)) return -10;
+  return assemble_impl(a, &f, s, launches);
+}
+
 int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
+{
+  return assemble_impl(a, nullptr, s, launches);
+}
+
+namespace {
+int assemble_impl(const AssembleArgs& a, const FilterArgs* filt, cudaStream_t s, long long* launches)
 {
   FFTPlan py, px, pz;
   if (!get_fft_plan(a.Y, &py) || !get_fft_plan(a.X, &px) || !get_fft_plan(a.Z, &pz)) return -1;
@@ -906,7 +1164,35 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
     AssembleArgs ay = a;
     KernelTimer* kt = kernel_timer();
     if (kt) kt->begin(s);
-    if (colfft_r1(a.Y)) {
+    if (filt) {
+      const FilterK fk = make_filter_k(*filt);
+      const int fl = filter_flags(*filt);
+      const size_t tabb = 2 * (size_t)filt->norders * filt->otf.nxotf * sizeof(float2);
+      auto go = [&]<int YN, int NO, int FL>() {
+        const size_t bytes = ColFft<YN, colfft_r1(YN), 8>::kSmemElems * sizeof(float2) + tabb;
+        allow_dynamic_smem((const void*)k_asm_y4f<YN, NO, FL>, bytes);
+        k_asm_y4f<YN, NO, FL><<<dim3((nx + 7) / 8, nsl), kThreads, bytes, s>>>(ay, d_slots + first, py.tw, *filt, fk);
+      };
+      auto by_fl = [&]<int YN, int NO>() {
+        switch (fl) {
+          case 0: go.template operator()<YN, NO, 0>(); break;
+          case 1: go.template operator()<YN, NO, 1>(); break;
+          case 2: go.template operator()<YN, NO, 2>(); break;
+          case 3: go.template operator()<YN, NO, 3>(); break;
+          case 4: go.template operator()<YN, NO, 4>(); break;
+          case 5: go.template operator()<YN, NO, 5>(); break;
+          case 6: go.template operator()<YN, NO, 6>(); break;
+          default: go.template operator()<YN, NO, 7>(); break;
+        }
+      };
+      auto by_no = [&]<int YN>() {
+        if (filt->norders == 3) by_fl.template operator()<YN, 3>();
+        else by_fl.template operator()<YN, 2>();
+      };
+      if (a.Y == 1024) by_no.template operator()<1024>();
+      else if (a.Y == 512) by_no.template operator()<512>();
+      else by_no.template operator()<256>();
+    } else if (colfft_r1(a.Y)) {
       auto go = [&]<int YN>() {
         const size_t bytes = ColFft<YN, colfft_r1(YN), 8>::kSmemElems * sizeof(float2);
         allow_dynamic_smem((const void*)k_asm_y4<YN>, bytes);
@@ -925,7 +1211,7 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
       double rd = 0;
       for (int q = first; q < first + nsl; ++q)
         rd += (slots[q].dir < 0 ? a.ndirs : (slots[q].order == 0 ? 1 : 2)) * (double)a.ny * nx * 8;
-      kt->end("k_asm_y", s, rd + (double)nsl * per_slot * sizeof(float2));
+      kt->end(filt ? "k_asm_y_filter" : "k_asm_y", s, rd + (double)nsl * per_slot * sizeof(float2));
     }
     // k_asm_x reads T[(slot - first)]: pass a shifted T base
     AssembleArgs ax = a;
@@ -987,5 +1273,6 @@ int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches)
   if (launches) *launches += nl;
   return (int)cudaGetLastError();
 }
+}  // namespace
 
 }  // namespace simrecon

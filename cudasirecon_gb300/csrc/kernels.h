@@ -179,6 +179,14 @@ size_t assemble_tables_bytes(const AssembleArgs& a);
 // timed/captured work, again whenever zdc changes).
 int assemble_tables_upload(const AssembleArgs& a);
 int launch_assemble(const AssembleArgs& a, cudaStream_t s, long long* launches);
+// Filter and assembly in one pass: the Wiener filter of every direction
+// applied in the assembly's band load (the bands are left unfiltered in
+// memory).  Available for 3 directions, 2 or 3 orders, one OTF for all
+// directions, zoomed y lengths 256/512/1024 and OTF lookups that stay inside
+// the table; returns -10 (nothing launched) otherwise.
+bool assemble_filter_fusable(const AssembleArgs& a, const FilterArgs& f, bool one_otf);
+int launch_assemble_filtered(const AssembleArgs& a, const FilterArgs& f, bool one_otf, cudaStream_t s,
+                             long long* launches);
 
 // Phase-ramp tables for assembly: ex[d*no+o][j] = exp(i fact pi (j - X/2) o k0x_d dxyz),
 // ey likewise along y (computed in double precision).

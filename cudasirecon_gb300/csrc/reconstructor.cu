@@ -1226,23 +1226,9 @@ void SIM_Reconstructor::filter_and_assemble()
   fa.otf.nxotf = p.nxotf;
   fa.otf.dkrotf = p.dkrotf;
   fa.otf.kzscale = kzscale;
-  for (int d = 0; d < ndirs_; ++d) {
-    const int dir_ = p.bOneOTFperAngle ? d : 0;
-    for (int o = 0; o < norders_; ++o)
-      fa.otf.otf[o] = d_otf_ + ((size_t)dir_ * norders_ + o) * p.nxotf * p.nzotf;
-    fa.dir = d;
-    fa.bands = d_spec_ + (size_t)d * nph_ * nz_ * ny_ * nxh_;
-    check_launch(launch_filter(fa, stream_, &launches_), "filterbands");
-  }
-  stage_end("filter", ev, l0);
+  for (int o = 0; o < norders_; ++o) fa.otf.otf[o] = d_otf_ + (size_t)o * p.nxotf * p.nzotf;
+  const bool one_otf = !p.bOneOTFperAngle || ndirs_otf_ == 1;
 
-  stage_begin("assemble", &ev, &l0);
-  K0List k0l{};
-  for (int d = 0; d < ndirs_; ++d) k0l.k[d] = make_float2(k0_[d].x, k0_[d].y);
-  float fact = p.explodefact / 0.5;
-  check_launch(launch_ramp_tables(k0l, ndirs_, norders_, X_, Y_, dxy / p.zoomfact, fact, d_ex_, d_ey_, stream_,
-                                  &launches_),
-               "ramp");
   AssembleArgs aa{};
   aa.bands = d_spec_;
   aa.ndirs = ndirs_;
@@ -1263,7 +1249,29 @@ void SIM_Reconstructor::filter_and_assemble()
   aa.out = d_out_;
   aa.tables = d_asmtab_;
   if (!asm_tables_current(aa)) throw std::runtime_error("assembly tables not prepared for this geometry");
-  check_launch(launch_assemble(aa, stream_, &launches_), "assemble");
+  // the filter runs inside the assembly's band load where it can; else as
+  // its own in-place pass per direction (filterbands_kernel1 x 2 + kernel3)
+  const bool fused = filter_fusion_ && assemble_filter_fusable(aa, fa, one_otf);
+  if (!fused)
+    for (int d = 0; d < ndirs_; ++d) {
+      const int dir_ = p.bOneOTFperAngle ? d : 0;
+      for (int o = 0; o < norders_; ++o)
+        fa.otf.otf[o] = d_otf_ + ((size_t)dir_ * norders_ + o) * p.nxotf * p.nzotf;
+      fa.dir = d;
+      fa.bands = d_spec_ + (size_t)d * nph_ * nz_ * ny_ * nxh_;
+      check_launch(launch_filter(fa, stream_, &launches_), "filterbands");
+    }
+  stage_end("filter", ev, l0);
+
+  stage_begin("assemble", &ev, &l0);
+  K0List k0l{};
+  for (int d = 0; d < ndirs_; ++d) k0l.k[d] = make_float2(k0_[d].x, k0_[d].y);
+  float fact = p.explodefact / 0.5;
+  check_launch(launch_ramp_tables(k0l, ndirs_, norders_, X_, Y_, dxy / p.zoomfact, fact, d_ex_, d_ey_, stream_,
+                                  &launches_),
+               "ramp");
+  if (fused) check_launch(launch_assemble_filtered(aa, fa, one_otf, stream_, &launches_), "filter + assemble");
+  else check_launch(launch_assemble(aa, stream_, &launches_), "assemble");
   stage_end("assemble", ev, l0);
 }
 

@@ -60,6 +60,9 @@ class SIM_Reconstructor {
   int get_band(int dir, int b, float* out);
   double bench_device(int steps);
   void set_profiling(bool on) { profiling_ = on; }
+  // Wiener filter inside the assembly's band load where supported (default),
+  // or always as its own pass; both give the same volume within float rounding
+  void set_filter_fusion(bool on) { filter_fusion_ = on; }
   std::string profile_json();
   void reset_profile();
   long long launches() const { return launches_; }
@@ -116,6 +119,7 @@ class SIM_Reconstructor {
   bool otf_dk_from_header_ = false;  // MRC OTF: dkr / dkz taken from its header
   cudaStream_t stream_ = nullptr;
   int device_ = 0;
+  bool filter_fusion_ = true;
   bool dry_run_ = false;      // setup computes planned_bytes_ and allocates nothing
   size_t planned_bytes_ = 0;
 

@@ -203,6 +203,14 @@ void SRX_setProfiling(SIM_Reconstructor* sr, int on);
 int SRX_getProfile(SIM_Reconstructor* sr, char* json, int maxlen);
 void SRX_resetProfile(SIM_Reconstructor* sr);
 
+/* Wiener filter placement (default on): inside the band load of the
+ * assembly's y transform where supported (3 directions, one OTF, zoomed y
+ * 256/512/1024), else -- or with on = 0 -- as its own in-place pass over the
+ * bands, as the reference's filterbands does.  Both give the same volume
+ * within float rounding.  After SR_processOneVolume the band contents
+ * (SRX_getBand) are unspecified. */
+void SRX_setFilterFusion(SIM_Reconstructor* sr, int on);
+
 /* Number of this library's kernels launched since the handle was created. */
 long long SRX_kernelLaunches(SIM_Reconstructor* sr);
 
