@@ -88,6 +88,10 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.SRX_pinHost.argtypes = [vp, C.c_size_t]
     lib.SRX_unpinHost.restype = ip
     lib.SRX_unpinHost.argtypes = [vp]
+    lib.SRX_hostAlloc.restype = vp
+    lib.SRX_hostAlloc.argtypes = [C.c_size_t]
+    lib.SRX_hostFree.restype = None
+    lib.SRX_hostFree.argtypes = [vp]
     lib.SRX_processSeries.restype = ip
     lib.SRX_processSeries.argtypes = [vp, C.POINTER(vp), ip, C.POINTER(vp), ip, ip]
     lib.SRX_serverCreate.restype = vp
@@ -374,6 +378,35 @@ def pin(array: np.ndarray) -> None:
 def unpin(array: np.ndarray) -> None:
     lib = load_library()
     lib.SRX_unpinHost(array.ctypes.data)
+
+
+class _HostBlock:
+    """Owner of one SRX_hostAlloc block; freed when the last view goes."""
+
+    def __init__(self, lib, nbytes: int):
+        self.lib = lib
+        self.ptr = lib.SRX_hostAlloc(nbytes)
+        if not self.ptr:
+            raise SIReconError(_err(lib))
+
+    def __del__(self):
+        try:
+            self.lib.SRX_hostFree(C.c_void_p(self.ptr))
+        except Exception:
+            pass
+
+
+def host_empty(shape, dtype=np.float32) -> np.ndarray:
+    """A numpy array in page-locked memory from the CUDA runtime
+    (SRX_hostAlloc): the fastest source and destination for raw stacks and
+    results.  The memory is freed with the array."""
+    lib = load_library()
+    dt = np.dtype(dtype)
+    count = int(np.prod(shape))
+    blk = _HostBlock(lib, count * dt.itemsize)
+    buf = (C.c_char * max(count * dt.itemsize, 1)).from_address(blk.ptr)
+    buf._owner = blk  # the block lives as long as the buffer, the buffer as long as the array
+    return np.frombuffer(buf, dtype=dt, count=count).reshape(shape)
 
 
 def fft_selftest(x: np.ndarray, inverse: bool = False, columns: bool = False) -> np.ndarray:

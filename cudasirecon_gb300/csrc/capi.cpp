@@ -453,6 +453,22 @@ int SRX_pinHost(void* ptr, size_t bytes)
   return 0;
 }
 
+void* SRX_hostAlloc(size_t bytes)
+{
+  void* p = nullptr;
+  cudaError_t e = cudaHostAlloc(&p, bytes ? bytes : 1, cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    g_last_error = std::string("cudaHostAlloc: ") + cudaGetErrorString(e);
+    return nullptr;
+  }
+  return p;
+}
+
+void SRX_hostFree(void* ptr)
+{
+  if (ptr) cudaFreeHost(ptr);
+}
+
 int SRX_deviceMemInfo(size_t* free_bytes, size_t* total_bytes)
 {
   if (!free_bytes || !total_bytes) {
