@@ -161,6 +161,31 @@ def make_workload(nx, ny, nz, nvol, seed=5):
     return vols, otf, cfg
 
 
+def alg_bytes_per_volume(nx, ny, nz, n_mo, n_red, ndirs=3, nph=5, zoom=2):
+    """The measurement's ideal one-pass-per-logical-stage byte count of one
+    volume: raw uint16 in, bands out, n_mo overlap builds (3 bands in, 2
+    overlaps out), n_red reductions over the overlap pair, bands into the
+    filter/assembly, float result out."""
+    I, N = ndirs * nph, nx * ny * nz
+    hb = (nx // 2 + 1) * ny * nz * 8
+    ov = 8 * N
+    nout = zoom * zoom * N
+    return 2 * I * N + I * hb + n_mo * (3 * hb + 2 * ov) + n_red * 2 * ov + I * hb + 4 * nout
+
+
+def step_roofline(nx, ny, nz, counts0, counts1, steps, ms_per_step, peak, peak_kind):
+    n_mo = (counts1["overlap_builds"] - counts0["overlap_builds"]) / steps
+    n_red = (counts1["reductions"] - counts0["reductions"]) / steps
+    b = alg_bytes_per_volume(nx, ny, nz, n_mo, n_red)
+    ach = b / (ms_per_step / 1e3) / 1e9
+    return {"alg_bytes_per_step": int(b), "n_mo": n_mo, "n_red": n_red,
+            "k0_searches_per_step": (counts1["k0_searches"] - counts0["k0_searches"]) / steps,
+            "achieved": round(ach, 1), "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4),
+            "peak_source": peak_kind,
+            "what": "whole step: the algorithmic bytes of one volume (raw in, bands, n_mo overlap builds, n_red "
+                    "overlap-pair reductions, bands into filter/assembly, result out) over the step time"}
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -181,6 +206,17 @@ def ncu_limiter(kernel):
     if not e or "issue_active_pct" not in e:
         return None
     return {k: e[k] for k in ("issue_active_pct", "dram_throughput_pct", "sm_throughput_pct", "full_capture") if k in e}
+
+
+def ncu_limiter_name(kernel):
+    """What bounds `kernel` according to its committed full ncu capture
+    ("fp32 issue", "latency", "hbm"), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            e = json.load(f).get(kernel)
+    except Exception:
+        return None
+    return e.get("limiter") if e else None
 
 
 def ncu_traffic(kernel, workload, alg_bytes_per_launch):
@@ -238,6 +274,7 @@ def run_gb300(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
     r.set_cur_time(t_idx)
     r.bench_device(args.warmup)
     l0 = r.kernel_launches()
+    fc0 = r.fit_counts()
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
     barrier(dist)
@@ -245,6 +282,7 @@ def run_gb300(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
     barrier(dist)
     clk = clocks.stop()
     launches = r.kernel_launches() - l0
+    fc1 = r.fit_counts()
     dev_ms = max_over_ranks(dist, dev_ms)
     # per-kernel times from a separate pass of the same steps (the events
     # around every launch would otherwise add to the timed region)
@@ -316,6 +354,7 @@ def run_gb300(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
         ach = st["alg_bytes"] / (st["ms"] / 1e3) / 1e9
         tr = ncu_traffic(name, args.workload, st["alg_bytes"] / max(1, st["launches"]))
         roof = {"kernel": name, "bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                "limiter": ncu_limiter_name(name),
                 "frac": round(ach / peak, 4), "peak_source": peak_kind,
                 "traffic": tr, "alg_bytes_per_launch": st["alg_bytes"] / max(1, st["launches"]),
                 "avg_launch_ms": st["ms"] / max(1, st["launches"]),
@@ -330,6 +369,8 @@ def run_gb300(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
         "config": {"workload": args.workload, "nx": nx, "ny": ny, "nz": nz, "images_per_volume": nimg,
                    "output": list(r.out_shape), "k0": "fitted at t=0, reused" if reuse else "searched every step",
                    "l2": "flushed between steps (256 MiB write); raw stack 377 MB > L2",
+                   "timed_volumes": "two synthetic time points (t = 0 and t = 1 of the drifting, bleaching scene) "
+                                    "alternated; every step reconstructs its volume from the raw stack",
                    "description": WORKLOADS[args.workload][3]},
         "e2e": {"value": round(e2e, 1), "unit": "Mvoxels/s",
                 "h2d_bytes_per_step": int(host[0].nbytes), "d2h_bytes_per_step": int(out.nbytes),
@@ -342,6 +383,7 @@ def run_gb300(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
         "gpu_launches": int(launches),
         "clocks": clk,
         "roofline": roof,
+        "step_roofline": step_roofline(nx, ny, nz, fc0, fc1, args.steps, dev_ms / args.steps, peak, peak_kind),
         "kernels": {k: {"ms_per_step": round(v["ms"] / args.steps, 4), "launches_per_step": v["launches"] / args.steps,
                         "GB_per_s": round(v["alg_bytes"] / (v["ms"] / 1e3) / 1e9, 1) if v["ms"] > 0 else None}
                     for k, v in kern.items()},
@@ -384,6 +426,7 @@ def run_reference(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
     try:
         for i in range(args.warmup):
             step(i)
+        fc0 = r.fit_counts()
         clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
         clocks.start()
         barrier(dist)
@@ -393,6 +436,7 @@ def run_reference(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
         barrier(dist)
         dt = max_over_ranks(dist, time.perf_counter() - t0)
         clk = clocks.stop()
+        fc1 = r.fit_counts()
     finally:
         import ctypes
         ctypes.CDLL(None).fflush(None)  # flush the reference's C stdio before restoring stdout
@@ -401,14 +445,21 @@ def run_reference(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
         os.close(devnull)
     value = world * args.steps * outvox / dt / 1e6
     r.close()
+    peak, peak_kind = peaks()
     return {
         "impl": "reference",
         "metric": "Recon output Mvoxels/s (SIM 3-beam, 512x512x48x15 -> 1024x1024x48)",
         "value": round(value, 1), "unit": "Mvoxels/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "nx": nx, "ny": ny, "nz": nz, "images_per_volume": nimg},
-        "e2e": {"value": round(value, 1), "unit": "Mvoxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "config": {"workload": args.workload, "nx": nx, "ny": ny, "nz": nz, "images_per_volume": nimg,
+                   "k0": "fitted at t=0, reused" if reuse else "searched every step",
+                   "timed_volumes": "the same two synthetic time points as the gb300 arm, alternated"},
+        "e2e": {"value": round(value, 1), "unit": "Mvoxels/s", "h2d_bytes_per_step": int(fl[0].nbytes),
+                "d2h_bytes_per_step": int(out.nbytes),
+                "api": "the reference's SR_setRaw (float32 stack) -> loadAndRescaleImage -> processOneVolume -> "
+                       "getResult, host memory in and out"},
+        "step_roofline": step_roofline(nx, ny, nz, fc0, fc1, args.steps, dt * 1e3 / args.steps, peak, peak_kind),
         "cpu_baseline": {"value": round(value, 1), "unit": "Mvoxels/s", "cores": 1, "kind": "reference",
                          "sample": "the reference's own CUDA build (gpuFunctionsImpl.cu kernels + cuFFT, host "
                                    "orchestration restated from cudaSirecon.cpp) through its SR_* flow on the full "
@@ -454,22 +505,32 @@ def serving_requests(seed=8):
     return types
 
 
-def run_serving(args):
-    """Plain one-at-a-time vs served (SRX_server*, Poisson arrivals)."""
+def _locked_copy(sr, a):
+    """a copied into page-locked host memory from the library (SRX_hostAlloc)."""
+    h = sr.host_empty(a.shape, a.dtype)
+    h[...] = a
+    return h
+
+
+def run_serving(args, compact=False):
+    """Plain one-at-a-time vs served (SRX_server*, Poisson arrivals).
+    compact: the summary the default benchmark line carries (100 plain
+    requests, one saturated run each with and without k0 kept per
+    configuration, Poisson arrivals at 100 req/s)."""
     import threading
     import cudasirecon_gb300 as sr
     sr.load_library()
     types = serving_requests()
-    for t in types:  # inputs page-locked for both arms; outputs pageable in both
-        sr.pin(t["raw"])
+    for t in types:  # inputs and result buffers page-locked for both arms
+        t["raw"] = _locked_copy(sr, t["raw"])
     rng = np.random.default_rng(8)
     workers = int(os.environ.get("SIRECON_SERVE_WORKERS", "6"))  # 6 measured faster than 4
     # ---- plain: one handle per type, requests one after another
     hs = {}
     for i, t in enumerate(types):
         r = sr.Reconstructor(t["nx"], t["ny"], t["raw"].shape[0], t["cfg"], t["otf"])
-        o = np.full(r.out_shape, 0.0, np.float32)
-        sr.pin(o)
+        o = sr.host_empty(r.out_shape, np.float32)
+        o[...] = 0.0
         hs[i] = (r, o)
 
     def plain(i):
@@ -482,7 +543,7 @@ def run_serving(args):
 
     for i in range(len(types)):
         plain(i)
-    seq = rng.integers(0, len(types), 200)
+    seq = rng.integers(0, len(types), 100 if compact else 200)
     t0 = time.perf_counter()
     lat = []
     for i in seq:
@@ -493,7 +554,6 @@ def run_serving(args):
     plain_vox = sum(types[int(i)]["outvox"] for i in seq)
     for r, o in hs.values():
         r.close()
-        sr.unpin(o)
     plain_line = {"requests": len(seq), "req_per_s": round(len(seq) / plain_s, 1),
                   "mvox_per_s": round(plain_vox / plain_s / 1e6, 1),
                   "p50_ms": round(float(np.percentile(lat, 50)), 2), "p99_ms": round(float(np.percentile(lat, 99)), 2)}
@@ -516,11 +576,11 @@ def run_serving(args):
     # driver's staging buffers, which concurrent workers share); requests of
     # one type share the input, so a buffer written by two requests in flight
     # still ends up with their (identical) result
-    pool = [[np.full(shapes[i], 0.0, np.float32) for _ in range(8)] for i in range(len(types))]
+    pool = [[sr.host_empty(shapes[i], np.float32) for _ in range(8)] for i in range(len(types))]
     for bufs in pool:
         for b in bufs:
-            sr.pin(b)
-    dur = float(os.environ.get("SIRECON_SERVE_SECONDS", "3"))
+            b[...] = 0.0
+    dur = float(os.environ.get("SIRECON_SERVE_SECONDS", "2" if compact else "3"))
 
     def poisson(lams):
         res = []
@@ -576,22 +636,27 @@ def run_serving(args):
     # served throughput; latency here is mostly queueing), searching k0 and
     # with k0 kept per configuration, alternated
     sat = {False: [], True: []}
-    for on in (False, True, False, True):
+    for on in ((False, True) if compact else (False, True, False, True)):
         set_reuse(on)
         sat[on].append(saturated_run())
     set_reuse(False)
     saturated = max(sat[False], key=lambda d: d["req_per_s"])
-    served = poisson((5, 20, 50, 100, 200))
+    served = poisson((100,) if compact else (5, 20, 50, 100, 200))
     set_reuse(True)
     reuse_saturated = max(sat[True], key=lambda d: d["req_per_s"])
-    reuse_served = poisson((20, 100, 200))
+    reuse_served = [] if compact else poisson((20, 100, 200))
     dev = srv.device_bytes()
     srv.close()
-    for t in types:
-        sr.unpin(t["raw"])
-    for bufs in pool:
-        for b in bufs:
-            sr.unpin(b)
+    if compact:
+        return {"what": "4 acquisition configurations (two 3D 256^2x32 / 512^2x32, two 2D 512^2 / 1024^2), "
+                        f"{workers} workers, 150 GB HBM admission budget; every request a standalone volume",
+                "plain_req_per_s": plain_line["req_per_s"], "plain_p50_ms": plain_line["p50_ms"],
+                "plain_p99_ms": plain_line["p99_ms"],
+                "served_saturated_req_per_s": saturated["req_per_s"],
+                "served_vs_plain": round(saturated["req_per_s"] / plain_line["req_per_s"], 3),
+                "served_k0_kept_saturated_req_per_s": reuse_saturated["req_per_s"],
+                "served_k0_kept_vs_plain": round(reuse_saturated["req_per_s"] / plain_line["req_per_s"], 3),
+                "poisson_100_req_s": served[0], "handles_bytes": dev}
     return {"metric": "Served recon latency (p50/p95/p99) and throughput vs plain one-at-a-time",
             "unit": "ms / Mvoxels/s", "impl": "gb300", "n_gpus": 1, "data": "synthetic",
             "config": {"workload": "serving",
@@ -599,7 +664,7 @@ def run_serving(args):
                                  f"{t['nx']}x{t['ny']}x{t['nz']}" for t in types],
                        "workers": workers, "hbm_budget_bytes": 150e9, "handles_bytes": dev,
                        "request": "standalone volume, k0 searched", "arrivals": "Poisson, seeded",
-                       "buffers": "raw stacks and result buffers page-locked (both arms)"},
+                       "buffers": "raw stacks and result buffers page-locked, SRX_hostAlloc (both arms)"},
             "plain": plain_line, "served_saturated": saturated, "served": served,
             "k0_reuse_per_config": {"served_saturated": reuse_saturated, "served": reuse_served},
             "saturated_repeats_req_per_s": {"search": [d["req_per_s"] for d in sat[False]],
@@ -661,15 +726,15 @@ def uneven_items(n2d=500, n3d=60):
     return [order[k] for k in perm], stacks, cfgs
 
 
-def run_uneven(args):
+def run_uneven(args, compact=False):
     """C4: the uneven 2D/3D batch, plain one-volume-at-a-time SR_* flow vs
     SRX_serverRunBatch (per-shape chunks, copies overlapped, shapes
-    concurrent on the workers' streams)."""
+    concurrent on the workers' streams).  compact: 100 2D frames and 12 3D
+    volumes of the same size distributions (the default line's summary)."""
     import cudasirecon_gb300 as sr
     sr.load_library()
-    order, stacks, cfgs = uneven_items()
-    for a in stacks.values():
-        sr.pin(a)
+    order, stacks, cfgs = uneven_items(100, 12) if compact else uneven_items()
+    stacks = {k: _locked_copy(sr, a) for k, a in stacks.items()}
     outvox = {k: 4 * k[1] * k[1] * k[2] for k in stacks}
     total_vox = sum(outvox[k] for k in order)
     # ---- plain: one handle per shape (created before the timed run)
@@ -690,7 +755,7 @@ def run_uneven(args):
     for k in stacks:
         plain(k)
     plain_s = []
-    for _ in range(2):
+    for _ in range(1 if compact else 2):
         t0 = time.perf_counter()
         for k in order:
             plain(k)
@@ -713,7 +778,7 @@ def run_uneven(args):
     srv.run_batch(items)  # warm-up: creates the handles of every shape
     warm_counts = srv.counters()
     batch_s = []
-    for _ in range(max(1, min(args.steps, 3))):
+    for _ in range(2 if compact else max(1, min(args.steps, 3))):
         t0 = time.perf_counter()
         srv.run_batch(items)
         batch_s.append(time.perf_counter() - t0)
@@ -723,10 +788,13 @@ def run_uneven(args):
     counts = srv.counters()
     timed_counts = {k: counts[k] - warm_counts[k] for k in counts}
     srv.close()
-    for a in stacks.values():
-        sr.unpin(a)
     bs, ps = statistics.median(batch_s), statistics.median(plain_s)
     n2 = sum(1 for k in order if k[0])
+    if compact:
+        return {"what": f"{n2} 2D frames (256^2-2048^2) and {len(order) - n2} 3D volumes (256^2-768^2, nz 16-64), "
+                        "standalone acquisitions, one batch call vs one SR_* flow per item",
+                "batched_mvox_per_s": round(total_vox / bs / 1e6, 1), "plain_mvox_per_s": round(total_vox / ps / 1e6, 1),
+                "batched_vs_plain": round(ps / bs, 3), "identical_to_plain": bool(same), "shapes": len(stacks)}
     return {"metric": "Recon output Mvoxels/s, uneven 2D/3D batch (batched vs plain)", "impl": "gb300",
             "value": round(total_vox / bs / 1e6, 1), "unit": "Mvoxels/s", "higher_is_better": True, "n_gpus": 1,
             "data": "synthetic", "dtype": "f32",
@@ -736,7 +804,7 @@ def run_uneven(args):
                        "shapes": len(stacks), "workers": workers, "hbm_budget_bytes": budget, "handles_bytes": dev,
                        "handles_created_evicted_in_timed_runs": timed_counts,
                        "request": "standalone acquisition, k0 searched",
-                       "buffers": "raw stacks page-locked, results pageable (both arms)"}}
+                       "buffers": "raw stacks page-locked (SRX_hostAlloc), results pageable (both arms)"}}
 
 
 def main():
@@ -747,6 +815,8 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=list(WORKLOADS) + ["serving", "uneven"], default="timeseries_512x512x48")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="leave out the serving and uneven-batch summaries of the default line")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local, dist = dist_init()
@@ -770,6 +840,12 @@ def main():
         line = run_gb300(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox)
         if rank == 0 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(vols[0], otf, cfg, nx, ny, nz)
+        if rank == 0 and not args.no_extras and world == 1:
+            del vols
+            t0 = time.perf_counter()
+            line["serving"] = run_serving(args, compact=True)
+            line["uneven_batch"] = run_uneven(args, compact=True)
+            line["extras_wall_s"] = round(time.perf_counter() - t0, 1)
     if rank == 0:
         print(json.dumps(line), flush=True)
 

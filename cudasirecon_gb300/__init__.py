@@ -75,6 +75,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.SRX_benchDevice.restype = ip
     lib.SRX_benchDevice.argtypes = [vp, ip, C.POINTER(C.c_double)]
     lib.SRX_setProfiling.argtypes = [vp, ip]
+    lib.SRX_fitCounts.restype = None
+    lib.SRX_fitCounts.argtypes = [vp, C.POINTER(C.c_longlong)]
     lib.SRX_setFilterFusion.restype = None
     lib.SRX_setFilterFusion.argtypes = [vp, ip]
     lib.SRX_getProfile.restype = ip
@@ -329,6 +331,13 @@ class Reconstructor:
 
     def set_profiling(self, on: bool = True):
         self.lib.SRX_setProfiling(self.h, int(on))
+
+    def fit_counts(self) -> dict:
+        """Overlap builds, overlap-pair reductions and k0 searches executed
+        since creation (SRX_fitCounts)."""
+        c = (C.c_longlong * 3)()
+        self.lib.SRX_fitCounts(self.h, c)
+        return {"overlap_builds": c[0], "reductions": c[1], "k0_searches": c[2]}
 
     def set_filter_fusion(self, on: bool = True):
         """Wiener filter inside the assembly's band load (default) or as its

@@ -196,6 +196,11 @@ void SRX_resetProfile(SIM_Reconstructor* sr)
   if (need(sr)) guarded([&] { sr->reset_profile(); });
 }
 
+void SRX_fitCounts(SIM_Reconstructor* sr, long long* out3)
+{
+  if (need(sr) && out3) sr->fit_counts(out3);
+}
+
 void SRX_setFilterFusion(SIM_Reconstructor* sr, int on)
 {
   if (need(sr)) sr->set_filter_fusion(on != 0);

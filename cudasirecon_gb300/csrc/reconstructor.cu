@@ -740,6 +740,7 @@ void SIM_Reconstructor::build_overlaps(int d, int o1, int o2, float k0x, float k
   a.pmap = d_pmap_;
   a.sumxy = d_sumxy_;
   check_launch(launch_overlaps(a, stream_, &launches_), "makeoverlaps");
+  ++fit_counts_[0];
   cur_o1_ = o1;
   cur_o2_ = o2;
   cache_.clear();
@@ -764,6 +765,7 @@ void SIM_Reconstructor::eval_candidates(int o1, int o2, const std::vector<std::p
     check_launch(launch_modamp_candidates(d_pmap_, nx_, ny_, opt.ip.dxy, kc, (int)nc, d_tables_, d_partial_,
                                           d_xstary_, stream_, &launches_),
                  "modamp");
+    fit_counts_[1] += (long long)nc;
     check_launch(launch_copy_out(d_xstary_, dh_pinned_, nc * 4, d_sumxy_, dh_pinned_ + 2 * kMaxCand, 4, stream_,
                                  &launches_),
                  "d2h");
@@ -817,6 +819,7 @@ float2v SIM_Reconstructor::findrealspacemodamp(int d, int o1, int o2, float k0x,
   check_launch(launch_modamp_candidates(d_pmap_, nx_, ny_, opt.ip.dxy, kc, 1, d_tables_, d_partial_, d_xstary_,
                                         stream_, &launches_),
                "modamp");
+  ++fit_counts_[1];
   check_launch(launch_copy_out(d_xstary_, dh_pinned_, 4, d_sumxy_, dh_pinned_ + 2, 4, stream_, &launches_), "d2h");
   check(cudaStreamSynchronize(stream_), "modamp");
   float sx = (float)h_pinned_[2];
@@ -831,6 +834,7 @@ void SIM_Reconstructor::findk0(int d)
   build_overlaps(d, 0, fitorder2, k0.x, k0.y);
   check_launch(launch_crosscorr_peak(d_pmap_, d_cc_, nx_, ny_, d_bval_, d_bidx_, d_peak_, stream_, &launches_),
                "crosscorr");
+  ++fit_counts_[1];  // the cross-correlation reads the overlap pair once, like a modamp reduction
   float* pk = (float*)(h_pinned_ + 256);
   check_launch(launch_copy_out(d_peak_, dh_pinned_ + 256, 7, nullptr, nullptr, 0, stream_, &launches_), "d2h");
   check(cudaStreamSynchronize(stream_), "findk0");
@@ -984,6 +988,7 @@ void SIM_Reconstructor::fit_direction(int direction)
   const ImageParams& ip = opt.ip;
   k0_[direction] = k0guess_[direction];
   cur_o1_ = cur_o2_ = -1;  // overlaps belong to another direction
+  ++fit_counts_[2];
   findk0(direction);
   p.recalcarrays = 1;
   fitk0andmodamps(direction);
@@ -1094,6 +1099,7 @@ void SIM_Reconstructor::fit_on_device()
       check_launch(launch_modamp_candidates(d_pmap_, nx_, ny_, ip.dxy, kc, 1, d_tables_, d_partial_, d_xstary_,
                                             stream_, &launches_),
                    "modamp");
+      ++fit_counts_[1];
       double* slot = d_fitslots_ + (size_t)(d * norders_ + order) * 4;
       check_launch(launch_copy_out(d_xstary_, slot, 4, d_sumxy_, slot + 2, 2, stream_, &launches_), "modamp");
     }
@@ -1381,6 +1387,8 @@ bool SIM_Reconstructor::capture_volume(int b, void* raw, float* out, int t, cuda
   d_raw_ = raw;
   d_out_ = out;
   const long long l0 = launches_;
+  long long fc0[3];
+  std::copy(fit_counts_, fit_counts_ + 3, fc0);
   check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeRelaxed), "graph capture");
   cudaGraph_t graph = nullptr;
   try {
@@ -1396,6 +1404,7 @@ bool SIM_Reconstructor::capture_volume(int b, void* raw, float* out, int t, cuda
     cudaStreamEndCapture(stream_, &graph);
     if (graph) cudaGraphDestroy(graph);
     launches_ = l0;
+    std::copy(fc0, fc0 + 3, fit_counts_);
     throw;
   }
   check(cudaStreamEndCapture(stream_, &graph), "graph capture");
@@ -1404,6 +1413,10 @@ bool SIM_Reconstructor::capture_volume(int b, void* raw, float* out, int t, cuda
   check(e, "graph instantiate");
   g.launches = launches_ - l0;
   launches_ = l0;
+  for (int i = 0; i < 3; ++i) {
+    g.fit_counts[i] = fit_counts_[i] - fc0[i];
+    fit_counts_[i] = fc0[i];
+  }
   g.raw = raw;
   g.out = out;
   g.t_nonzero = tnz;
@@ -1469,6 +1482,7 @@ void SIM_Reconstructor::process_series(const void* const* raws, bool u16, float*
         capture_volume(b, raw_buf[b], out_buf[b], t, ev_raw_free_[b]);
         check(cudaGraphLaunch(graphs_[b].exec, stream_), "graph launch");
         launches_ += graphs_[b].launches;
+        for (int c = 0; c < 3; ++c) fit_counts_[c] += graphs_[b].fit_counts[c];
         amps_on_device_only_ = true;
         have_raw_ = false;
         rescaled_ = true;

@@ -66,6 +66,13 @@ class SIM_Reconstructor {
   std::string profile_json();
   void reset_profile();
   long long launches() const { return launches_; }
+  // executed overlap builds (makeoverlaps), reductions over an overlap pair
+  // (modamp evaluations and the cross-correlation) and k0 searches since
+  // creation: the n_mo / n_red of the algorithmic-bytes model
+  void fit_counts(long long* out3) const
+  {
+    for (int i = 0; i < 3; ++i) out3[i] = fit_counts_[i];
+  }
   size_t out_elems() const { return (size_t)X_ * Y_ * Z_; }
   size_t device_bytes() const  // device memory the handle holds
   {
@@ -188,6 +195,7 @@ class SIM_Reconstructor {
     float* out = nullptr;
     bool t_nonzero = false, u16 = false;
     long long launches = 0;
+    long long fit_counts[3] = {0, 0, 0};
   };
   VolumeGraph graphs_[2];
   bool raw_u16_ = false;
@@ -237,6 +245,7 @@ class SIM_Reconstructor {
     ~TimerScope();
   };
   long long launches_ = 0;
+  long long fit_counts_[3] = {0, 0, 0};
   void stage_begin(const char* name, cudaEvent_t* a, long long* l0);
   void stage_end(const char* name, cudaEvent_t a, long long l0);
 };

@@ -203,6 +203,12 @@ void SRX_setProfiling(SIM_Reconstructor* sr, int on);
 int SRX_getProfile(SIM_Reconstructor* sr, char* json, int maxlen);
 void SRX_resetProfile(SIM_Reconstructor* sr);
 
+/* No counterpart in the reference.  Fit work executed since the handle was
+ * created: out3[0] overlap builds (the reference's makeoverlaps), out3[1]
+ * reductions over an overlap pair (modamp evaluations, the k0
+ * cross-correlation), out3[2] k0 searches (findk0 + fitk0andmodamps). */
+void SRX_fitCounts(SIM_Reconstructor* sr, long long* out3);
+
 /* Wiener filter placement (default on): inside the band load of the
  * assembly's y transform where supported (3 directions, one OTF, zoomed y
  * 256/512/1024), else -- or with on = 0 -- as its own in-place pass over the

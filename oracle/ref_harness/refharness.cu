@@ -81,6 +81,11 @@ struct Harness {
   int zoffset = 0;
   std::vector<float> raw;   // [nImages][ny][nx] as given to setRaw
   int nImages = 0;
+  // executed fit work (for the measurement's algorithmic-bytes model): each
+  // findrealspacemodamp with redo builds the overlaps once and reduces them
+  // once; a k0 search (findk0 + fitk0andmodamps) runs an unobserved number
+  // of both inside the reference's own functions and is only counted
+  long long n_overlap_builds = 0, n_reductions = 0, n_searches = 0;
 };
 
 // SetDefaultParams, cudaSirecon.cpp:16-72, then the program_options defaults
@@ -438,6 +443,7 @@ void stage_fit(Harness* h)
     cuFloatComplex amp_inv, amp_combo;
     int dir_ = params->bOneOTFperAngle ? direction : 0;
     if (params->bSearchforvector && !(ip.ntimes > 1 && ip.curTimeIdx > 0 && params->bUseTime0k0)) {
+      ++h->n_searches;
       findk0(bands, &data->overlap0, &data->overlap1, ip.nx, ip.ny, ip.nz0, params->norders,
              &(data->k0[direction]), ip.dxy, ip.dz, &(data->otf[dir_]), ip.wave[0], params);
       params->recalcarrays = 1;
@@ -453,6 +459,7 @@ void stage_fit(Harness* h)
       if (ip.ntimes > 1 && ip.curTimeIdx > 0 && dist > 2 * K0_WARNING_THRESH) {
         data->k0[direction] = data->k0_time0[direction];
         for (int order = 1; order < params->norders; ++order) {
+          h->n_overlap_builds++, h->n_reductions++;
           if (ip.nz0 > 1)
             findrealspacemodamp(bands, &data->overlap0, &data->overlap1, ip.nx, ip.ny, ip.nz0, 0, order,
                                 data->k0[direction], ip.dxy, ip.dz, &(data->otf[dir_]), ip.wave[0],
@@ -464,10 +471,12 @@ void stage_fit(Harness* h)
         }
       }
     } else {
-      for (int order = 1; order < params->norders; ++order)
+      for (int order = 1; order < params->norders; ++order) {
+        h->n_overlap_builds++, h->n_reductions++;
         findrealspacemodamp(bands, &data->overlap0, &data->overlap1, ip.nx, ip.ny, ip.nz0, 0, order,
                             data->k0[direction], ip.dxy, ip.dz, &(data->otf[dir_]), ip.wave[0],
                             &data->amp[direction][order], &amp_inv, &amp_combo, 1, params);
+      }
     }
     if (ip.nz == 1)
       for (int order = 2; order < params->norders; ++order)
@@ -636,6 +645,15 @@ void refh_get_k0guess(void* hv, float* k0)
     k0[2 * d] = h->d.k0guess[d].x;
     k0[2 * d + 1] = h->d.k0guess[d].y;
   }
+}
+
+// executed overlap builds, reductions and k0 searches since creation
+void refh_fit_counts(void* hv, long long* out3)
+{
+  Harness* h = (Harness*)hv;
+  out3[0] = h->n_overlap_builds;
+  out3[1] = h->n_reductions;
+  out3[2] = h->n_searches;
 }
 
 int refh_norders(void* hv) { return ((Harness*)hv)->p.norders; }

@@ -47,6 +47,7 @@ def load(build: bool = True):
     lib.refh_norders.restype = ip
     lib.refh_nz.argtypes = [vp]
     lib.refh_nz.restype = ip
+    lib.refh_fit_counts.argtypes = [vp, C.POINTER(C.c_longlong)]
     _lib = lib
     return lib
 
@@ -121,6 +122,12 @@ class RefRecon:
         amp = np.empty((self.ndirs, self.norders, 2), np.float32)
         self.lib.refh_get_fit(self.h, _fptr(k0), _fptr(amp))
         return k0, amp[..., 0] + 1j * amp[..., 1]
+
+    def fit_counts(self) -> dict:
+        """Overlap builds, reductions and k0 searches executed since creation."""
+        c = (C.c_longlong * 3)()
+        self.lib.refh_fit_counts(self.h, c)
+        return {"overlap_builds": c[0], "reductions": c[1], "k0_searches": c[2]}
 
     def k0guess(self):
         k0 = np.empty((self.ndirs, 2), np.float32)
