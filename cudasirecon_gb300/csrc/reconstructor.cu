@@ -268,6 +268,7 @@ SIM_Reconstructor* SIM_Reconstructor::from_argv(int argc, char** argv, std::stri
     h.zlen /= p.z_zoom;
     h.next = 0;
     r->out_hdr_ = h;
+    memcpy(r->in_label0_, r->mrc_in_.hdr.label[0], 80);
     r->out_path_ = p.ofiles;
     r->mrc_out_.open(p.ofiles, std::ios::binary | std::ios::trunc);
     if (!r->mrc_out_) {
@@ -1613,20 +1614,46 @@ void SIM_Reconstructor::write_result(int it, int iw)
   }
 }
 
-// closeFiles (cudaSirecon.cpp:1702-1713 and saveCommandLineToHeader, mrc.h:62-74)
+// closeFiles (cudaSirecon.cpp:1702-1713) -> saveCommandLineToHeader
+// (mrc.h:62-74).  The two IM-library calls it makes are restated from the
+// Priism IM library's documented behaviour (the library is not part of the
+// reference tree):
+//  * IMAlLab(stream, titles, strlen(titles)/80 + 1) with bWriteTitle: the
+//    header's labels become that many 80-byte records cut from `titles`, the
+//    arguments after the three positional ones, each followed by a space, in
+//    a 1000-byte buffer.  The bytes the reference copies past the string's
+//    terminator are its uninitialised stack; they are written as zeros here.
+//  * IMWrHdr(stream, header.label, 1, amin, amax, amean): the title argument
+//    is the first label of the header the program keeps (the input file's
+//    first label, m_in_out_header); ntflag = 1 appends it to the labels,
+//    dropping the oldest when all ten are in use; amin/amax are the values of
+//    writeResult's scan of time point 0 and amean the input's.
 void SIM_Reconstructor::close_files()
 {
   if (opt.p.bTIFF || !mrc_out_.is_open()) return;
   if (opt.p.bWriteTitle) {
-    std::string titles;
-    for (size_t i = 3; i < argv_.size(); ++i) titles += argv_[i] + " ";
-    if (out_hdr_.nlab < 10) {
-      char* lab = out_hdr_.label[out_hdr_.nlab];
-      memset(lab, ' ', 80);
-      memcpy(lab, titles.data(), std::min<size_t>(80, titles.size()));
-      out_hdr_.nlab++;
-    }
+    char titles[1000];
+    memset(titles, 0, sizeof(titles));
+    size_t len = 0;
+    for (size_t i = 3; i < argv_.size(); ++i)
+      for (const std::string& piece : {argv_[i], std::string(" ")})
+        for (char c : piece)
+          if (len + 1 < sizeof(titles)) titles[len++] = c;
+    int nl = (int)(len / 80) + 1;
+    if (nl > 10) nl = 10;
+    memset(out_hdr_.label, 0, sizeof(out_hdr_.label));
+    for (int l = 0; l < nl; ++l) memcpy(out_hdr_.label[l], titles + 80 * l, 80);
+    out_hdr_.nlab = nl;
   }
+  char title[80];
+  memcpy(title, in_label0_, 80);
+  if (out_hdr_.nlab < 0) out_hdr_.nlab = 0;
+  if (out_hdr_.nlab >= 10) {
+    memmove(out_hdr_.label[0], out_hdr_.label[1], 9 * 80);
+    out_hdr_.nlab = 9;
+  }
+  memcpy(out_hdr_.label[out_hdr_.nlab], title, 80);
+  out_hdr_.nlab++;
   mrc_out_.seekp(0);
   mrc_out_.write((const char*)&out_hdr_, sizeof(MrcHeader));
   mrc_out_.close();

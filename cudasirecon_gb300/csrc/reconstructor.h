@@ -213,6 +213,7 @@ class SIM_Reconstructor {
   std::string out_path_;
   std::ofstream mrc_out_;
   simrecon::MrcHeader out_hdr_{};
+  char in_label0_[80] = {0};  // the input file's first label (closeFiles appends it)
   std::vector<float> host_raw_;
   std::vector<std::string> argv_;
 

@@ -105,3 +105,70 @@ def test_cli_mrc_input_and_output_match_reference(tmp_path):
     assert got.shape == want.shape
     assert rel_l2(got, want) < 1e-4
     assert np.abs(got - want).max() / np.abs(want).max() < 1e-3
+
+
+def write_mrc_full(path, stack, dxy, dz, wave, labels, amean, ext_bytes=0):
+    """DV/MRC input with labels, a mean and an extended header: fields the
+    output header carries over or rewrites."""
+    import struct
+    nz, ny, nx = stack.shape
+    h = bytearray(1024)
+    struct.pack_into("<4i", h, 0, nx, ny, nz, 2)
+    struct.pack_into("<3i", h, 28, nx, ny, nz)
+    struct.pack_into("<3f", h, 40, dxy * nx, dxy * ny, dz * nz)
+    struct.pack_into("<3f", h, 52, 90.0, 90.0, 90.0)
+    struct.pack_into("<3i", h, 64, 1, 2, 3)
+    struct.pack_into("<3f", h, 76, -3.5, 4321.0, amean)
+    struct.pack_into("<i", h, 92, ext_bytes)
+    struct.pack_into("<h", h, 96, -16224)
+    struct.pack_into("<hh", h, 128, 0, 2)  # nint, nreal
+    struct.pack_into("<hh", h, 180, 1, 0)  # num_times, interleaved
+    struct.pack_into("<hh", h, 196, 1, wave)
+    struct.pack_into("<3f", h, 208, 1.5, -2.25, 3.0)
+    struct.pack_into("<i", h, 220, len(labels))
+    for i, lab in enumerate(labels):
+        h[224 + 80 * i:224 + 80 * i + len(lab)] = lab.encode()
+    # xlen/ylen/zlen of a DV header are the pixel sizes (loadHeader reads dxy from ylen)
+    struct.pack_into("<3f", h, 40, dxy, dxy, dz)
+    with open(path, "wb") as f:
+        f.write(bytes(h))
+        f.write(bytes(range(256)) * (ext_bytes // 256) + bytes(ext_bytes % 256))
+        f.write(np.ascontiguousarray(stack, np.float32).tobytes())
+
+
+@pytest.mark.parametrize("title,nlab_in", [(False, 2), (True, 2), (False, 10), (True, 10)],
+                         ids=["labels-kept", "long-title", "ten-labels", "long-title-ten-labels"])
+def test_cli_mrc_output_header_every_field(tmp_path, title, nlab_in):
+    """Every byte of the output header against the restatement of
+    setOutputHeader, writeResult's min/max scan and saveCommandLineToHeader
+    (oracle/mrc_header.py), with a title longer than 80 characters; label
+    bytes the reference takes from uninitialised memory are skipped."""
+    import struct
+    from oracle.mrc_header import expected_header
+    case, _ = load("c3d_64")
+    labels = [f"input label {i} " + "x" * (20 + 3 * i) for i in range(nlab_in)]
+    inp, out = tmp_path / "cell.dv", tmp_path / "cell_proc.dv"
+    write_mrc_full(inp, case["raw"][0].astype(np.float32), 0.08, 0.125, 528, labels, amean=777.25, ext_bytes=512)
+    otf = tmp_path / "otf.tif"
+    sr.load_library()
+    sr.write_tiff_float(str(otf), case["otf"])
+    cfgdir = tmp_path / ("configuration_folder_with_a_long_name_" + "y" * 40)
+    cfgdir.mkdir()
+    cfg = cfgdir / "config"
+    cfg.write_text(case["config"])
+    extra = ["-c", str(cfg)] + (["--writeTitle"] if title else [])
+    run_cli([str(inp), str(out), str(otf)] + extra)
+    got, hdr = read_mrc(out)
+    with open(inp, "rb") as f:
+        in_hdr = f.read(1024)
+    nz = got.shape[0]
+    argv3 = [str(otf)] + extra  # the title starts at argv[3], the OTF file
+    want, mask = expected_header(in_hdr, got, 2.0, 1, nz, argv3, title)
+    if title:
+        assert len(" ".join(argv3) + " ") > 80  # two title records
+    assert hdr[:224] == want[:224], [i for i in range(224) if hdr[i] != want[i]]
+    lab_got = np.frombuffer(hdr[224:], np.uint8)
+    lab_want = np.frombuffer(want[224:], np.uint8)
+    assert np.array_equal(lab_got[mask], lab_want[mask])
+    nlab = struct.unpack_from("<i", hdr, 220)[0]
+    assert nlab == (min(10, len(" ".join(argv3) + " ") // 80 + 1) + 1 if title else min(10, nlab_in + 1))

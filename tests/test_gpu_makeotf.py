@@ -14,10 +14,21 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 pytestmark = pytest.mark.gpu
 
 FIXTURES = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "mo_*.npz")))
-# float32 FFT on the GPU against the reference run with a float64 DFT; the
-# OTF is normalised to 1 at the origin
-REL_L2 = 2e-5
-MAX_ABS = 2e-5
+# the makeotf parity bar: OTF rel-L2 <= 1e-5 (float32 FFT on the GPU against
+# the reference program run with a float64 DFT), and max-abs <= 1e-5 of the
+# OTF's peak (1 at the origin unless -rescale is off).  Achieved on the
+# fixtures: rel-L2 0.6e-7 to 1.6e-7; printed by each test (pytest -s).
+REL_L2 = 1e-5
+MAX_ABS_OF_PEAK = 1e-5
+
+
+def check(got, want, what):
+    d = got - want
+    rel = float(np.linalg.norm(d) / np.linalg.norm(want))
+    mx = float(np.abs(d).max() / np.abs(want).max())
+    print(f"\nmakeotf {what}: rel-L2 {rel:.3e}, max-abs {mx:.3e} of peak")
+    assert rel <= REL_L2, rel
+    assert mx <= MAX_ABS_OF_PEAK, mx
 
 
 def load(path):
@@ -37,9 +48,7 @@ def test_makeotf_matches_reference_program(lib, path):
     psf, args, ref = load(path)
     got = lib.make_otf(psf, args)
     assert got.shape == ref.shape
-    d = got - ref
-    assert np.linalg.norm(d) / np.linalg.norm(ref) <= REL_L2
-    assert np.abs(d).max() <= MAX_ABS
+    check(got, ref, os.path.basename(path))
 
 
 def test_makeotf_matches_oracle_fresh_input(lib):
@@ -50,9 +59,7 @@ def test_makeotf_matches_oracle_fresh_input(lib):
             "-wavelength", "528", "-fixorigin", "3", "20"]
     got = lib.make_otf(psf, args)
     want = mo.makeotf(psf, mo.MakeOTFOptions.from_args(args))
-    d = got - want
-    assert np.linalg.norm(d) / np.linalg.norm(want) <= REL_L2
-    assert np.abs(d).max() <= MAX_ABS
+    check(got, want, "fresh 96x96x40 PSF vs the oracle")
 
 
 def test_makeotf_deterministic(lib):
@@ -71,7 +78,7 @@ def test_makeotf_cli_tiff_roundtrip(lib, tmp_path):
     assert r.returncode == 0, r.stderr
     got = lib.read_tiff_float(opath)
     assert got.shape == ref.shape
-    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) <= REL_L2
+    check(got, ref, "bin/makeotf on TIFF files")
     view = lib.read_tiff_float(str(tmp_path / "otf_OnlyForViewing.tif"))
     c = got[..., 0::2] + 1j * got[..., 1::2]
     assert np.allclose(view, np.sqrt(np.abs(c)), rtol=1e-6, atol=1e-7)
