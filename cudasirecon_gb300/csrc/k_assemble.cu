@@ -25,6 +25,7 @@
 #include "col_fft.cuh"
 #include "kernels.h"
 #include "reg_fft.cuh"
+#include "thresholds.h"
 
 namespace simrecon {
 
@@ -59,14 +60,6 @@ struct FilterK {
   int order0_shared;
 };
 
-// hardware square root (about 1 ulp): only for the continuous OTF
-// interpolation index, never for a decision
-__device__ __forceinline__ float sqrt_approx(float x)
-{
-  float r;
-  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
-  return r;
-}
 
 // Wiener scale of pixel (x1f, y1f, z0) of band (dir, order): the body of
 // filterbands_kernel1 (gpuFunctionsImpl.cu:1504-1592) without the final
@@ -934,25 +927,6 @@ DevTables dev_tables(const AssembleArgs& a, const HostTables& t)
 }  // namespace
 
 namespace {
-// smallest float t with sqrtf(t) >= c: for every float r2, r2 < t <=> sqrtf(r2) < c
-float r2_below(float c)
-{
-  float t = c * c;
-  while (t > 0.f && std::sqrt(t) >= c) t = std::nextafter(t, 0.f);
-  while (std::sqrt(t) < c) t = std::nextafter(t, INFINITY);
-  return t;
-}
-
-// largest float t with sqrtf(t) <= c: r2 <= t <=> sqrtf(r2) <= c
-float r2_atmost(float c)
-{
-  if (!(c >= 0.f)) return -1.f;
-  float t = c * c;
-  while (t > 0.f && std::sqrt(t) > c) t = std::nextafter(t, 0.f);
-  while (std::sqrt(std::nextafter(t, INFINITY)) <= c) t = std::nextafter(t, INFINITY);
-  return t;
-}
-
 FilterK make_filter_k(const FilterArgs& a)
 {
   FilterK k{};

@@ -75,6 +75,11 @@ struct OverlapArgs {
   float kx, ky;         // k0 * (order2 - order1), 1/um
   float dkx, dky;
   float rdistcutoff, otfcutoff, order0_2_factor;
+  // exact squared forms of makeoverlaps' float decisions (set by
+  // launch_overlaps): sqrtf(r2) <= rdistcutoff <=> r2 <= r2_le,
+  // sqrtf(r2) < rdistcutoff <=> r2 < r2_lt, sqrtf(m) > otfcutoff <=> m > m_le,
+  // sqrtf(m) * order0_2_factor > otfcutoff <=> m >= m_f
+  float r2_le, r2_lt, m_le, m_f;
   int zdc;              // planes -zdc..zdc are built
   int nokz0;
   OTFView otf;

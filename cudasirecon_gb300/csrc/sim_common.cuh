@@ -23,6 +23,15 @@ struct OTFView {
 };
 
 #ifdef __CUDACC__
+// hardware square root (about 1 ulp): only for continuous quantities such as
+// the OTF interpolation index, never for a decision
+__device__ __forceinline__ float sqrt_approx(float x)
+{
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // Bilinear lookup in a rotationally averaged OTF (the interpolation of
 // dev_otfinterpolate, gpuFunctionsImpl.cu:1677-1715).  Indices are clamped
 // to the table so a lookup at the very edge of the support never reads past
