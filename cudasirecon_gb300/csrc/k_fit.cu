@@ -148,10 +148,11 @@ struct OvlLanes {
 };
 constexpr int kOvlWarps = 4;
 
-// Four CTAs per SM (at most 128 registers, no spills): the kernel is bound
-// by its resident warps (0.64 -> 0.55 ms per 512^2 x 48 volume against three)
+// Five CTAs per SM (at most 96 registers, no spills): the kernel is bound by
+// its resident warps (per 512^2 x 48 volume: 0.64 ms with three CTAs, 0.55
+// with four, 0.51 with five, 0.54 with six and spills)
 template <int N>
-__global__ void __launch_bounds__(kOvlWarps * 32, 4) k_ovl_build_xw(OverlapArgs a, const float2* __restrict__ twr)
+__global__ void __launch_bounds__(kOvlWarps * 32, 5) k_ovl_build_xw(OverlapArgs a, const float2* __restrict__ twr)
 {
   constexpr int P = OvlLanes<N>::P, E = N / P, G = 32 / P;
   constexpr int XB = (P + 1) * E + 1;
