@@ -77,6 +77,10 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.SRX_setProfiling.argtypes = [vp, ip]
     lib.SRX_fitCounts.restype = None
     lib.SRX_fitCounts.argtypes = [vp, C.POINTER(C.c_longlong)]
+    lib.SRX_tuneFFT.restype = ip
+    lib.SRX_tuneFFT.argtypes = [vp, ip, C.c_char_p, ip]
+    lib.SRX_fftPlanChoice.restype = ip
+    lib.SRX_fftPlanChoice.argtypes = [ip, ip, C.c_char_p, ip]
     lib.SRX_setFilterFusion.restype = None
     lib.SRX_setFilterFusion.argtypes = [vp, ip]
     lib.SRX_getProfile.restype = ip
@@ -120,6 +124,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.SRX_serverDeviceBytes.argtypes = [vp]
     lib.SRX_serverDeviceBytesHeld.restype = C.c_size_t
     lib.SRX_serverDeviceBytesHeld.argtypes = [vp]
+    lib.SRX_serverMemory.restype = None
+    lib.SRX_serverMemory.argtypes = [vp, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
     lib.SRX_serverPlannedBytes.restype = C.c_size_t
     lib.SRX_serverPlannedBytes.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
     lib.SRX_serverAdmissionWaits.restype = C.c_longlong
@@ -339,6 +345,17 @@ class Reconstructor:
         self.lib.SRX_fitCounts(self.h, c)
         return {"overlap_builds": c[0], "reductions": c[1], "k0_searches": c[2]}
 
+    def tune_fft(self, reps: int = 2) -> dict:
+        """Time both FFT paths at every site/length of this handle's volume on
+        the staged raw stack and record the faster ones in the plan cache
+        (SRX_tuneFFT)."""
+        import json
+        buf = C.create_string_buffer(1 << 16)
+        n = self.lib.SRX_tuneFFT(self.h, int(reps), buf, len(buf))
+        if n < 0:
+            raise SIReconError(_err(self.lib))
+        return json.loads(buf.value.decode())
+
     def set_filter_fusion(self, on: bool = True):
         """Wiener filter inside the assembly's band load (default) or as its
         own pass (SRX_setFilterFusion)."""
@@ -416,6 +433,20 @@ def host_empty(shape, dtype=np.float32) -> np.ndarray:
     buf = (C.c_char * max(count * dt.itemsize, 1)).from_address(blk.ptr)
     buf._owner = blk  # the block lives as long as the buffer, the buffer as long as the array
     return np.frombuffer(buf, dtype=dt, count=count).reshape(shape)
+
+
+FFT_SITES = {"ingest_x": 0, "ingest_y": 1, "separate_z": 2, "overlap_x": 3, "overlap_y": 4, "crosscorr_rows": 5,
+             "crosscorr_cols": 6, "assemble_y": 7, "assemble_x": 8, "assemble_z": 9, "makeotf": 10}
+
+
+def fft_plan_choice(site: str, n: int):
+    """(register path?, source) the FFT call site uses for length n."""
+    lib = load_library()
+    buf = C.create_string_buffer(64)
+    r = lib.SRX_fftPlanChoice(FFT_SITES[site], int(n), buf, len(buf))
+    if r < 0:
+        raise SIReconError("unknown FFT site")
+    return bool(r), buf.value.decode()
 
 
 def fft_selftest(x: np.ndarray, inverse: bool = False, columns: bool = False) -> np.ndarray:
@@ -548,6 +579,12 @@ class Server:
         if b == 0:
             raise SIReconError(_err(self.lib))
         return b
+
+    def memory(self):
+        """(reserved, held) device bytes, taken together."""
+        r, h = C.c_size_t(0), C.c_size_t(0)
+        self.lib.SRX_serverMemory(self.h, C.byref(r), C.byref(h))
+        return r.value, h.value
 
     def device_bytes_held(self) -> int:
         """Device bytes the pooled handles actually hold now."""

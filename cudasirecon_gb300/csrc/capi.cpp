@@ -201,6 +201,32 @@ void SRX_fitCounts(SIM_Reconstructor* sr, long long* out3)
   if (need(sr) && out3) sr->fit_counts(out3);
 }
 
+int SRX_tuneFFT(SIM_Reconstructor* sr, int reps, char* json, int maxlen)
+{
+  if (!need(sr)) return -1;
+  int rc = -1;
+  guarded([&] {
+    const std::string j = sr->tune_fft(reps);
+    if (json && maxlen > 0) {
+      std::strncpy(json, j.c_str(), (size_t)maxlen - 1);
+      json[maxlen - 1] = '\0';
+    }
+    rc = (int)j.size();
+  });
+  return rc;
+}
+
+int SRX_fftPlanChoice(int site, int n, char* source, int maxlen)
+{
+  const char* src = "";
+  const int r = simrecon::fft_plan_choice(site, n, &src);
+  if (source && maxlen > 0) {
+    std::strncpy(source, src, (size_t)maxlen - 1);
+    source[maxlen - 1] = '\0';
+  }
+  return r;
+}
+
 void SRX_setFilterFusion(SIM_Reconstructor* sr, int on)
 {
   if (need(sr)) sr->set_filter_fusion(on != 0);
@@ -420,6 +446,14 @@ int SRX_batchPlan(const SRX_BatchItem* items, int n, int workers, int* chunk_of_
 size_t SRX_serverDeviceBytes(SRX_Server* s) { return s ? ((simrecon::ReconServer*)s)->device_bytes_in_use() : 0; }
 
 size_t SRX_serverDeviceBytesHeld(SRX_Server* s) { return s ? ((simrecon::ReconServer*)s)->device_bytes_held() : 0; }
+
+void SRX_serverMemory(SRX_Server* s, size_t* reserved, size_t* held)
+{
+  size_t r = 0, h = 0;
+  if (s) ((simrecon::ReconServer*)s)->memory_snapshot(&r, &h);
+  if (reserved) *reserved = r;
+  if (held) *held = h;
+}
 
 size_t SRX_serverPlannedBytes(SRX_Server* s, int config, int nx, int ny, int nimages)
 {

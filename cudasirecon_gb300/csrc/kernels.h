@@ -4,6 +4,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <set>
+#include <string>
+#include <utility>
+
 #include "sim_common.cuh"
 
 namespace simrecon {
@@ -31,6 +35,18 @@ bool get_fft_plan(int n, FFTPlan* plan);
 bool fft_length_ok(int n);
 // radix sequence of length n into radix[kMaxStages] (no allocation)
 bool fft_radix_plan(int n, int* radix, int* nstages);
+
+// FFT path choice per call site and length (register path or Stockham
+// stages).  The tuner forces a choice on the calling thread, tracks which
+// (site, length) pairs a run queries, and records measured choices in the
+// on-disk plan cache that every process reads.
+void fft_site_force(int site, bool reg);
+void fft_site_unforce();
+void fft_sites_track(std::set<std::pair<int, int>>* seen);  // nullptr stops tracking
+const char* fft_site_name(int site);
+bool fft_plan_record(int site, int n, bool reg, double ms_reg, double ms_stockham, std::string* err);
+int fft_plan_choice(int site, int n, const char** source);
+std::string fft_plan_cache_path();
 
 // -------------------------------------------------------------------- ingest
 struct IngestArgs {

@@ -4,6 +4,7 @@
 // stream; the host only steers the k0 / modamp search, reading back a few
 // scalars per search step.
 #include "reconstructor.h"
+#include "reg_fft.cuh"
 
 #include <algorithm>
 #include <cfloat>
@@ -12,6 +13,7 @@
 #include <cstring>
 #include <dirent.h>
 #include <regex>
+#include <set>
 #include <sstream>
 #include <stdexcept>
 #include <sys/stat.h>
@@ -619,6 +621,7 @@ void SIM_Reconstructor::stage_raw(const void* raw, bool u16)
   raw_u16_ = u16;
   check(cudaMemcpyAsync(d_raw_, raw, n * (u16 ? 2 : 4), cudaMemcpyHostToDevice, stream_), "raw upload");
   have_raw_ = true;
+  raw_staged_ = true;
   ingest();
   // setRaw copies the caller's stack (interface.cpp:19-25): return once the
   // upload and the ingest kernels are done with it
@@ -1558,6 +1561,84 @@ double SIM_Reconstructor::bench_device(int steps)
   cudaEventDestroy(b);
   have_raw_ = true;
   return total;
+}
+
+// ------------------------------------------------------------- FFT tuning
+// The kernel (as reported to the per-kernel timer) that runs each FFT site
+static const char* site_kernel(int site)
+{
+  switch (site) {
+    case kSiteIngestX: return "k_ingest_x";
+    case kSiteIngestY: return "k_fft_y";
+    case kSiteSeparateZ: return "k_separate";
+    case kSiteOvlX: return "k_ovl_build_x";
+    case kSiteOvlY: return "k_ovl_y_accum";
+    case kSiteCorrRows:
+    case kSiteCorrCols: return "k_crosscorr";
+    case kSiteAsmY: return "k_asm_y";
+    case kSiteAsmX: return "k_asm_x";
+    case kSiteAsmZ: return "k_asm_z";
+    default: return nullptr;
+  }
+}
+
+// Measure, for every (FFT site, length) a volume of this handle queries and
+// the register path supports, the site's kernel time with the register path
+// and with the Stockham stages, on the staged raw stack (each run restarts
+// from it), and record the faster choice in the plan cache.  The volume runs
+// as time point 0 (k0 search) so that the search's transforms are included.
+std::string SIM_Reconstructor::tune_fft(int reps)
+{
+  if (!raw_staged_) throw std::runtime_error("tuneFFT: no raw stack staged (SR_setRaw first)");
+  const unsigned short t_saved = opt.ip.curTimeIdx;
+  const bool prof_saved = profiling_;
+  std::set<std::pair<int, int>> seen;
+  std::ostringstream out;
+  out.precision(6);
+  out << "{\"cache\": \"" << fft_plan_cache_path() << "\", \"sites\": [";
+  try {
+    set_cur_time(0);
+    profiling_ = false;
+    fft_sites_track(&seen);
+    bench_device(1);
+    fft_sites_track(nullptr);
+    bool first = true;
+    for (auto [site, n] : seen) {
+      const char* kname = site_kernel(site);
+      if (!kname || !reg_fft_lanes(n)) continue;
+      double best[2] = {1e30, 1e30};  // [stockham, register]
+      for (int rep = 0; rep < std::max(1, reps); ++rep)
+        for (int reg = 1; reg >= 0; --reg) {
+          fft_site_force(site, reg != 0);
+          profiling_ = true;
+          reset_profile();
+          bench_device(1);
+          profile_json();
+          profiling_ = false;
+          fft_site_unforce();
+          auto it = kprof_.find(kname);
+          if (it != kprof_.end()) best[reg] = std::min(best[reg], it->second.ms);
+        }
+      const bool reg = best[1] <= best[0];
+      std::string err;
+      if (!fft_plan_record(site, n, reg, best[1], best[0], &err)) throw std::runtime_error(err);
+      out << (first ? "" : ", ") << "{\"site\": \"" << fft_site_name(site) << "\", \"n\": " << n
+          << ", \"kernel\": \"" << kname << "\", \"register_ms\": " << best[1] << ", \"stockham_ms\": " << best[0]
+          << ", \"choice\": \"" << (reg ? "register" : "stockham") << "\"}";
+      first = false;
+    }
+  } catch (...) {
+    fft_sites_track(nullptr);
+    fft_site_unforce();
+    profiling_ = prof_saved;
+    set_cur_time(t_saved);
+    throw;
+  }
+  out << "]}";
+  reset_profile();
+  profiling_ = prof_saved;
+  set_cur_time(t_saved);
+  return out.str();
 }
 
 // ------------------------------------------------------------------ files

@@ -63,6 +63,9 @@ class SIM_Reconstructor {
   // Wiener filter inside the assembly's band load where supported (default),
   // or always as its own pass; both give the same volume within float rounding
   void set_filter_fusion(bool on) { filter_fusion_ = on; }
+  // time both FFT paths at every site and length this handle's volume uses
+  // (best of `reps`), record the faster in the plan cache; returns JSON
+  std::string tune_fft(int reps);
   std::string profile_json();
   void reset_profile();
   long long launches() const { return launches_; }
@@ -199,6 +202,7 @@ class SIM_Reconstructor {
   };
   VolumeGraph graphs_[2];
   bool raw_u16_ = false;
+  bool raw_staged_ = false;  // d_raw_ holds a stack staged by setRaw/setFile
   bool have_raw_ = false;
   bool rescaled_ = false;
   // overlap state for the candidate evaluator

@@ -243,10 +243,18 @@ void ReconServer::counters(long long* created, long long* evicted, long long* ad
 
 size_t ReconServer::device_bytes_held()
 {
+  size_t r, h;
+  memory_snapshot(&r, &h);
+  return h;
+}
+
+void ReconServer::memory_snapshot(size_t* reserved, size_t* held)
+{
   std::lock_guard<std::mutex> lk(mu_);
   size_t n = 0;
   for (auto& h : handles_) n += h->sr->device_bytes();
-  return n;
+  *reserved = in_use_;
+  *held = n;
 }
 
 int ReconServer::device() const { return device_; }

@@ -46,6 +46,8 @@ class ReconServer {
   size_t device_bytes_in_use();
   // device bytes the pooled handles actually hold now (at most the reserved)
   size_t device_bytes_held();
+  // both under one lock: a consistent pair (held <= reserved)
+  void memory_snapshot(size_t* reserved, size_t* held);
   // handles created and deleted (budget evictions) since construction, and
   // how often a request waited for device memory to be released
   void counters(long long* created, long long* evicted, long long* admission_waits = nullptr);

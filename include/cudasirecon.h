@@ -209,6 +209,24 @@ void SRX_resetProfile(SIM_Reconstructor* sr);
  * cross-correlation), out3[2] k0 searches (findk0 + fitk0andmodamps). */
 void SRX_fitCounts(SIM_Reconstructor* sr, long long* out3);
 
+/* No counterpart in the reference.  FFT plan autotuning.  The library's FFT
+ * call sites (site ids: 0 ingest x, 1 ingest y, 2 separation z, 3 overlap x,
+ * 4 overlap y, 5/6 cross-correlation rows/columns, 7/8/9 assembly y/x/z,
+ * 10 makeotf) run a length either with the register path (lengths 32, 48,
+ * 64, 96, 128, 256, 512, 1024) or with the shared-memory Stockham stages.
+ * SRX_tuneFFT runs the handle's staged raw stack (SR_setRaw first) once per
+ * choice and repeat for every site and length its volume uses, times the
+ * site's kernel with CUDA events, and records the faster choice in the plan
+ * cache file (SIMRECON_FFT_PLAN_CACHE, else ~/.cache/cudasirecon_gb300/
+ * fft_plans.tsv; one line per GPU model, site and length) that every process
+ * then uses.  It leaves the handle's fit state as after processing that stack
+ * at time point 0.  Returns the length of the JSON report written to json
+ * (truncated to maxlen), or -1 (SR_getLastError).
+ * SRX_fftPlanChoice: 1 register path, 0 Stockham, -1 bad site, with the
+ * choice's source ("tuned", "built-in", "environment", "stockham-only"). */
+int SRX_tuneFFT(SIM_Reconstructor* sr, int reps, char* json, int maxlen);
+int SRX_fftPlanChoice(int site, int n, char* source, int maxlen);
+
 /* Wiener filter placement (default on): inside the band load of the
  * assembly's y transform where supported (3 directions, one OTF, zoomed y
  * 256/512/1024), else -- or with on = 0 -- as its own in-place pass over the
@@ -321,6 +339,8 @@ int SRX_batchPlan(const SRX_BatchItem* items, int n, int workers, int* chunk_of_
  * actually hold now (at most the reserved bytes). */
 size_t SRX_serverDeviceBytes(SRX_Server* s);
 size_t SRX_serverDeviceBytesHeld(SRX_Server* s);
+/* Both figures taken together (a consistent pair: held <= reserved). */
+void SRX_serverMemory(SRX_Server* s, size_t* reserved, size_t* held);
 /* The bytes admission reserves for a handle of this configuration and shape
  * (planned without allocating); 0 on error (SR_getLastError). */
 size_t SRX_serverPlannedBytes(SRX_Server* s, int config, int nx, int ny, int nimages);

@@ -44,7 +44,7 @@ def test_server_matches_plain_within_budget(budget):
 
     def poll():
         while not stop.is_set():
-            seen.append((srv.device_bytes(), srv.device_bytes_held()))
+            seen.append(srv.memory())
 
     th = threading.Thread(target=poll)
     th.start()
