@@ -227,6 +227,8 @@ int SRX_fftPlanChoice(int site, int n, char* source, int maxlen)
   return r;
 }
 
+int SRX_lastProcessResult(SIM_Reconstructor* sr) { return need(sr) ? sr->last_process_result() : -1; }
+
 void SRX_setFilterFusion(SIM_Reconstructor* sr, int on)
 {
   if (need(sr)) sr->set_filter_fusion(on != 0);

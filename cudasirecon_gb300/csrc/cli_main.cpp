@@ -33,7 +33,7 @@ int main(int argc, char** argv)
       SR_loadAndRescaleImage(r, it, iw);
       SR_setCurTimeIdx(r, it);
       SR_processOneVolume(r);
-      SR_writeResult(r, it, iw);
+      if (SRX_lastProcessResult(r) == 1) SR_writeResult(r, it, iw);
       if (*SR_getLastError()) {
         std::cerr << "\n!!Error occurred: " << SR_getLastError() << std::endl;
         SR_delete(r);

@@ -690,6 +690,42 @@ int launch_crosscorr_peak(const float2* pmap, float2* cc, int nx, int ny, float*
 }
 
 namespace {
+__global__ void k_ovl_scatter(const float2* __restrict__ ovl, int nx, int ny, int nz, int zdc, float2* vol)
+{
+  const size_t plane = (size_t)nx * ny, n = 2 * (size_t)nz * plane;
+  const int nzb = 2 * zdc + 1;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t ov = i / ((size_t)nz * plane), r = i - ov * nz * plane;
+    const int z = (int)(r / plane);
+    const size_t e = r - (size_t)z * plane;
+    const int z0 = z <= nz / 2 ? z : z - nz;
+    const int zb = z0 + zdc;
+    vol[i] = (zb >= 0 && zb < nzb) ? ovl[(ov * nzb + zb) * plane + e] : make_float2(0.f, 0.f);
+  }
+}
+}  // namespace
+
+int launch_overlap_volumes(const OverlapArgs& a, float2* vol, cudaStream_t s)
+{
+  FFTPlan py, pz;
+  if (!get_fft_plan(a.ny, &py) || !get_fft_plan(a.nz, &pz)) return -1;
+  const size_t plane = (size_t)a.nx * a.ny;
+  k_ovl_scatter<<<1216, 256, 0, s>>>(a.ovl, a.nx, a.ny, a.nz, a.zdc, vol);
+  auto cols = [&](float2* data, int n, int ncol, const FFTPlan& p) {
+    const int W = std::max(1, std::min(32, kMaxElems / n));
+    const size_t sm = fft_stage_smem(n, W, (W + 1) * n, kThreads);
+    allow_dynamic_smem((const void*)k_fft_cols2<+1, 0>, sm);
+    k_fft_cols2<+1, 0><<<(ncol + W - 1) / W, kThreads, sm, s>>>(data, n, ncol, p, W);
+  };
+  for (int ov = 0; ov < 2; ++ov) {
+    float2* v = vol + (size_t)ov * a.nz * plane;
+    for (int z = 0; z < a.nz; ++z) cols(v + (size_t)z * plane, a.ny, a.nx, py);  // y
+    if (a.nz > 1) cols(v, a.nz, (int)plane, pz);                                 // z
+  }
+  return (int)cudaGetLastError();
+}
+
+namespace {
 __global__ void k_copy_out(const unsigned* __restrict__ s1, unsigned* d1, int n1, const unsigned* __restrict__ s2,
                            unsigned* d2, int n2)
 {

@@ -107,6 +107,13 @@ struct OverlapArgs {
 };
 int launch_overlaps(OverlapArgs& a, cudaStream_t s, long long* launches);
 
+// The two overlaps of the last launch_overlaps as full real-space volumes,
+// [2][nz][ny][nx] complex (the reference's overlap0/overlap1 after
+// makeoverlaps' inverse 3D FFT): the x-transformed rows of the built kz
+// planes scattered into every kz plane (zero outside +-zdc), then inverse
+// FFTs along y and z.  For the debug dump only; vol is the caller's.
+int launch_overlap_volumes(const OverlapArgs& a, float2* vol, cudaStream_t s);
+
 // crosscorr = FFT2(conj(pmap)); intensity argmax with the two-neighbour
 // values along x and y (wrap-around) written to peak[0..6]:
 // {ix, iy, a1x, a2, a3x, a1y, a3y}

@@ -279,6 +279,10 @@ SIM_Reconstructor* SIM_Reconstructor::from_argv(int argc, char** argv, std::stri
       return nullptr;
     }
     r->mrc_out_.write((const char*)&r->out_hdr_, sizeof(MrcHeader));
+    if (!r->open_debug_files(err)) {
+      delete r;
+      return nullptr;
+    }
   }
   return r;
 }
@@ -745,6 +749,7 @@ void SIM_Reconstructor::build_overlaps(int d, int o1, int o2, float k0x, float k
   a.sumxy = d_sumxy_;
   check_launch(launch_overlaps(a, stream_, &launches_), "makeoverlaps");
   ++fit_counts_[0];
+  last_ovl_ = a;
   cur_o1_ = o1;
   cur_o2_ = o2;
   cache_.clear();
@@ -1289,6 +1294,13 @@ void SIM_Reconstructor::filter_and_assemble()
 int SIM_Reconstructor::process_one_volume(bool sync)
 {
   if (!have_raw_) throw std::runtime_error("processOneVolume before setRaw/setFile");
+  if (debug_requested()) {  // dumps, then no reconstruction (cudaSirecon.cpp:1264-1321)
+    separate();
+    last_result_ = debug_volume();
+    have_raw_ = false;
+    return last_result_;
+  }
+  last_result_ = 1;
   prepare_asm_tables();
   separate();
   fit_all();
@@ -1561,6 +1573,176 @@ double SIM_Reconstructor::bench_device(int steps)
   cudaEventDestroy(b);
   have_raw_ = true;
   return total;
+}
+
+// ------------------------------------------------------------ debug dumps
+namespace {
+// IMWrHdr(..., title, ntflag = 1, ...) restated: the title becomes a new
+// 80-byte label after the others (the oldest dropped when all ten are used)
+void append_label(MrcHeader& h, const char* title, size_t len)
+{
+  if (h.nlab < 0) h.nlab = 0;
+  if (h.nlab >= 10) {
+    memmove(h.label[0], h.label[1], 9 * 80);
+    h.nlab = 9;
+  }
+  memset(h.label[h.nlab], 0, 80);
+  memcpy(h.label[h.nlab], title, std::min<size_t>(len, 80));
+  h.nlab++;
+}
+}  // namespace
+
+bool SIM_Reconstructor::debug_requested() const
+{
+  return opt.p.bSaveSeparated || opt.p.bSaveAlignedRaw || opt.p.bSaveOverlaps;
+}
+
+// The intermediate files of setup_common (cudaSirecon.cpp:1179-1210): MRC
+// mode only, headers copied from the input file's
+bool SIM_Reconstructor::open_debug_files(std::string* err)
+{
+  const ReconParams& p = opt.p;
+  const ImageParams& ip = opt.ip;
+  auto open = [&](DebugFile& d, const std::string& path, const MrcHeader& h) {
+    d.h = h;
+    d.f.open(path, std::ios::binary | std::ios::trunc);
+    if (!d.f) {
+      *err = "File " + path + " can not be created.";
+      return false;
+    }
+    d.f.write((const char*)&d.h, sizeof(MrcHeader));
+    d.open = true;
+    return true;
+  };
+  const MrcHeader& in = mrc_in_.hdr;
+  if (p.bSaveAlignedRaw) {
+    MrcHeader h = in;
+    h.mode = 2;
+    h.nx = ip.nx;
+    h.next = 0;
+    if (!open(dbg_aligned_, p.fileRawAligned, h)) return false;
+  }
+  if (p.bSaveSeparated) {
+    MrcHeader h = in;
+    h.nx = ip.nx / 2 + 1;  // separated half-spectrum bands
+    h.mode = 4;            // complex
+    h.next = 0;
+    if (!open(dbg_sep_, p.fileSeparated, h)) return false;
+  }
+  if (p.bSaveOverlaps) {
+    MrcHeader h = in;
+    h.nz = ip.nz * 2 * p.ndirs * ip.ntimes * ip.nwaves;
+    h.nx = ip.nx;
+    h.num_waves = 2;    // overlap 0 and 1 as waves 0 and 1
+    h.interleaved = 1;  // WZT sequence
+    h.mode = 4;         // full-complex overlaps in real space
+    h.next = 0;
+    if (!open(dbg_ovl_, p.fileOverlaps, h)) return false;
+  }
+  return true;
+}
+
+// the separated bands of direction d, each kz plane a (nx/2+1) x ny complex
+// section (cudaSirecon.cpp:275-284)
+void SIM_Reconstructor::debug_write_bands(int d)
+{
+  const size_t plane = (size_t)ny_ * nxh_;
+  std::vector<float2> buf((size_t)nph_ * nz_ * plane);
+  check(cudaMemcpy(buf.data(), d_spec_ + (size_t)d * nph_ * nz_ * plane, buf.size() * sizeof(float2),
+                   cudaMemcpyDeviceToHost),
+        "saveprefiltered");
+  dbg_sep_.f.write((const char*)buf.data(), buf.size() * sizeof(float2));
+}
+
+// The last overlap pair in real space (cudaSirecon.cpp:330-354 after findk0;
+// 433-445 in the no-search branch, whose sections start every nx*ny floats
+// of the complex buffers -- the reference's pointer arithmetic -- and so
+// overlap by half a section)
+void SIM_Reconstructor::debug_dump_overlaps(bool search_branch)
+{
+  const ReconParams& p = opt.p;
+  const size_t plane = (size_t)nx_ * ny_, vol = (size_t)nz_ * plane;
+  float2* d = nullptr;
+  check(cudaMalloc((void**)&d, 2 * vol * sizeof(float2)), "saveoverlaps buffer");
+  std::vector<float2> h(2 * vol);
+  cudaError_t e = (cudaError_t)launch_overlap_volumes(last_ovl_, d, stream_);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
+  if (e == cudaSuccess) e = cudaMemcpy(h.data(), d, h.size() * sizeof(float2), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  check(e, "saveoverlaps");
+  if (p.bTIFF) {  // [overlap0 planes, overlap1 planes], each plane 2 nx floats wide
+    std::string err;
+    if (search_branch && !tiff_write_float(p.fileOverlaps, (const float*)h.data(), 2 * nx_, ny_, 2 * nz_, &err))
+      throw std::runtime_error(err);
+    return;
+  }
+  if (!dbg_ovl_.open) return;
+  const float* f0 = (const float*)h.data();
+  const float* f1 = (const float*)(h.data() + vol);
+  for (int z = 0; z < nz_; ++z) {
+    const size_t off = search_branch ? 2 * z * plane : z * plane;  // in floats
+    dbg_ovl_.f.write((const char*)(f0 + off), 2 * plane * sizeof(float));
+    dbg_ovl_.f.write((const char*)(f1 + off), 2 * plane * sizeof(float));
+  }
+}
+
+// saveIntermediateDataForDebugging (mrc.h:76-97): titles, min/max/mean and close
+void SIM_Reconstructor::close_debug_files()
+{
+  auto fin = [&](DebugFile& d, const char* title, float amin, float amax, float amean) {
+    if (!d.open) return;
+    append_label(d.h, title, strlen(title));
+    d.h.amin = amin;
+    d.h.amax = amax;
+    d.h.amean = amean;
+    d.f.seekp(0);
+    d.f.write((const char*)&d.h, sizeof(MrcHeader));
+    d.f.close();
+    d.open = false;
+  };
+  fin(dbg_sep_, "separated bands of all directions", 0, 1, 0);
+  fin(dbg_aligned_, "drift-corrected raw images", dbg_aligned_.h.amin, dbg_aligned_.h.amax, dbg_aligned_.h.amean);
+  fin(dbg_ovl_, "overlaps in real space", 0, 1, 0);
+}
+
+// findModulationVectorsAndPhasesForAllDirections with its debug dumps
+// (cudaSirecon.cpp:194-494), then the stop of processOneVolume: returns 0
+int SIM_Reconstructor::debug_volume()
+{
+  ReconParams& p = opt.p;
+  const ImageParams& ip = opt.ip;
+  const bool reuse = ip.ntimes > 1 && ip.curTimeIdx > 0 && p.bUseTime0k0;
+  for (int d = 0; d < ndirs_; ++d) {
+    if (p.bSaveSeparated) {
+      if (p.bTIFF) {
+        std::printf("No unmixed raw images were saved in TIFF mode\n");
+      } else {
+        if (dbg_sep_.open) debug_write_bands(d);
+        continue;  // no k0 search or modamp fit for this direction
+      }
+    }
+    cur_o1_ = cur_o2_ = -1;
+    if (p.bSearchforvector && !reuse) {
+      k0_[d] = k0guess_[d];
+      findk0(d);
+      if (p.bSaveOverlaps) debug_dump_overlaps(true);
+      p.recalcarrays = 1;
+      fitk0andmodamps(d);
+      if (ip.curTimeIdx == 0) k0_time0_[d] = k0_[d];
+    } else {
+      if (!reuse) k0_[d] = k0guess_[d];
+      for (int order = 1; order < norders_; ++order) {
+        amp_[d][order] = findrealspacemodamp(d, 0, order, k0_[d].x, k0_[d].y, 1);
+        if (order == 1 && p.bSaveOverlaps) {
+          if (p.bTIFF) std::printf("No overlaps were saved in TIFF mode\n");
+          else debug_dump_overlaps(false);
+        }
+      }
+    }
+  }
+  amps_on_device_only_ = false;
+  close_debug_files();
+  return 0;
 }
 
 // ------------------------------------------------------------- FFT tuning

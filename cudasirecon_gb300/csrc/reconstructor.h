@@ -49,6 +49,9 @@ class SIM_Reconstructor {
   void set_file(int it, int iw);
   void write_result(int it, int iw);
   void close_files();
+  // what the last process_one_volume returned: 1 reconstructed, 0 stopped
+  // after the debug dumps (the reference's driver then writes no result)
+  int last_process_result() const { return last_result_; }
   int ntimes() const { return opt.ip.ntimes; }
   void set_ntimes(int n) { opt.ip.ntimes = (short)n; }
   // the k0 of every direction as if time point 0 had fitted it (k0[2 d], k0[2 d + 1])
@@ -107,6 +110,13 @@ class SIM_Reconstructor {
   bool asm_tables_current(const simrecon::AssembleArgs& aa) const;
   void prepare_asm_tables();
   bool capture_volume(int b, void* raw, float* out, int t, cudaEvent_t raw_free);
+  // debug dumps (saveprefiltered / savealignedraw / saveoverlaps)
+  bool debug_requested() const;
+  bool open_debug_files(std::string* err);
+  int debug_volume();
+  void debug_write_bands(int d);
+  void debug_dump_overlaps(bool search_branch);
+  void close_debug_files();
   void drop_graphs();
   static void check(cudaError_t e, const char* what);
   void check_launch(int rc, const char* what);
@@ -218,6 +228,14 @@ class SIM_Reconstructor {
   std::ofstream mrc_out_;
   simrecon::MrcHeader out_hdr_{};
   char in_label0_[80] = {0};  // the input file's first label (closeFiles appends it)
+  struct DebugFile {
+    std::ofstream f;
+    simrecon::MrcHeader h{};
+    bool open = false;
+  };
+  DebugFile dbg_sep_, dbg_aligned_, dbg_ovl_;
+  simrecon::OverlapArgs last_ovl_{};  // the arguments of the last overlap build
+  int last_result_ = 1;
   std::vector<float> host_raw_;
   std::vector<std::string> argv_;
 

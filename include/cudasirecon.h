@@ -227,6 +227,12 @@ void SRX_fitCounts(SIM_Reconstructor* sr, long long* out3);
 int SRX_tuneFFT(SIM_Reconstructor* sr, int reps, char* json, int maxlen);
 int SRX_fftPlanChoice(int site, int n, char* source, int maxlen);
 
+/* No counterpart in the reference.  What the last SR_processOneVolume
+ * returned in the reference's terms: 1 reconstructed, 0 stopped after the
+ * debug dumps (saveprefiltered / savealignedraw / saveoverlaps), when the
+ * reference's driver writes no result for that time point. */
+int SRX_lastProcessResult(SIM_Reconstructor* sr);
+
 /* Wiener filter placement (default on): inside the band load of the
  * assembly's y transform where supported (3 directions, one OTF, zoomed y
  * 256/512/1024), else -- or with on = 0 -- as its own in-place pass over the

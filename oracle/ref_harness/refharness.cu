@@ -86,6 +86,10 @@ struct Harness {
   // once; a k0 search (findk0 + fitk0andmodamps) runs an unobserved number
   // of both inside the reference's own functions and is only counted
   long long n_overlap_builds = 0, n_reductions = 0, n_searches = 0;
+  // the overlap pair right after findk0, per direction (the reference's
+  // saveoverlaps dump point), when capturing is on
+  bool capture_overlaps = false;
+  std::vector<std::vector<float>> captured;  // [dir][2 * nx * ny * nz0 * 2 floats]
 };
 
 // SetDefaultParams, cudaSirecon.cpp:16-72, then the program_options defaults
@@ -446,6 +450,14 @@ void stage_fit(Harness* h)
       ++h->n_searches;
       findk0(bands, &data->overlap0, &data->overlap1, ip.nx, ip.ny, ip.nz0, params->norders,
              &(data->k0[direction]), ip.dxy, ip.dz, &(data->otf[dir_]), ip.wave[0], params);
+      if (h->capture_overlaps) {
+        const size_t n = data->overlap0.getSize();
+        std::vector<float> c(2 * n / sizeof(float));
+        cudaMemcpy(c.data(), data->overlap0.getPtr(), n, cudaMemcpyDeviceToHost);
+        cudaMemcpy(c.data() + n / sizeof(float), data->overlap1.getPtr(), n, cudaMemcpyDeviceToHost);
+        if (h->captured.size() < (size_t)params->ndirs) h->captured.resize(params->ndirs);
+        h->captured[direction] = std::move(c);
+      }
       params->recalcarrays = 1;
       fitk0andmodamps(bands, &data->overlap0, &data->overlap1, ip.nx, ip.ny, ip.nz0, params->norders,
                       &(data->k0[direction]), ip.dxy, ip.dz, &(data->otf[dir_]), ip.wave[0],
@@ -645,6 +657,19 @@ void refh_get_k0guess(void* hv, float* k0)
     k0[2 * d] = h->d.k0guess[d].x;
     k0[2 * d + 1] = h->d.k0guess[d].y;
   }
+}
+
+// capture the overlap pair after each direction's findk0 (on != 0); then
+// refh_get_captured(dir) copies [overlap0 | overlap1] (complex, nz0 x ny x nx
+// each) and returns its float count, or 0 if none was captured
+void refh_capture_overlaps(void* hv, int on) { ((Harness*)hv)->capture_overlaps = on != 0; }
+
+long long refh_get_captured(void* hv, int dir, float* out)
+{
+  Harness* h = (Harness*)hv;
+  if (dir < 0 || (size_t)dir >= h->captured.size() || h->captured[dir].empty()) return 0;
+  if (out) memcpy(out, h->captured[dir].data(), h->captured[dir].size() * sizeof(float));
+  return (long long)h->captured[dir].size();
 }
 
 // executed overlap builds, reductions and k0 searches since creation

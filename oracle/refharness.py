@@ -48,6 +48,9 @@ def load(build: bool = True):
     lib.refh_nz.argtypes = [vp]
     lib.refh_nz.restype = ip
     lib.refh_fit_counts.argtypes = [vp, C.POINTER(C.c_longlong)]
+    lib.refh_capture_overlaps.argtypes = [vp, ip]
+    lib.refh_get_captured.argtypes = [vp, ip, fp]
+    lib.refh_get_captured.restype = C.c_longlong
     _lib = lib
     return lib
 
@@ -122,6 +125,22 @@ class RefRecon:
         amp = np.empty((self.ndirs, self.norders, 2), np.float32)
         self.lib.refh_get_fit(self.h, _fptr(k0), _fptr(amp))
         return k0, amp[..., 0] + 1j * amp[..., 1]
+
+    def capture_overlaps(self, on: bool = True):
+        """Keep each direction's overlap pair right after findk0."""
+        self.lib.refh_capture_overlaps(self.h, int(on))
+
+    def captured_overlaps(self, d: int):
+        """(overlap0, overlap1) of direction d after findk0, complex
+        [nz][ny][nx] each, or None."""
+        n = self.lib.refh_get_captured(self.h, d, None)
+        if n == 0:
+            return None
+        buf = np.empty(n, np.float32)
+        self.lib.refh_get_captured(self.h, d, _fptr(buf))
+        c = buf[0::2] + 1j * buf[1::2]
+        half = c.size // 2
+        return c[:half].reshape(self.nz, self.ny, self.nx), c[half:].reshape(self.nz, self.ny, self.nx)
 
     def fit_counts(self) -> dict:
         """Overlap builds, reductions and k0 searches executed since creation."""

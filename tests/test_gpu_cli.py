@@ -172,3 +172,146 @@ def test_cli_mrc_output_header_every_field(tmp_path, title, nlab_in):
     assert np.array_equal(lab_got[mask], lab_want[mask])
     nlab = struct.unpack_from("<i", hdr, 220)[0]
     assert nlab == (min(10, len(" ".join(argv3) + " ") // 80 + 1) + 1 if title else min(10, nlab_in + 1))
+
+
+# --------------------------------------------------------------- debug dumps
+# saveprefiltered / savealignedraw / saveoverlaps (cudaSirecon.cpp:270-287,
+# 330-354, 433-445, 1179-1210, mrc.h:76-97): the intermediates are written,
+# the volume is not reconstructed and no result is written.
+
+def read_mrc_sections(path):
+    """(data [nsec][ny][nx] float32 or complex64, header) of an MRC/DV file."""
+    import struct
+    with open(path, "rb") as f:
+        h = f.read(1024)
+        nx, ny, nz, mode = struct.unpack_from("<4i", h, 0)
+        f.read(max(struct.unpack_from("<i", h, 92)[0], 0))
+        body = f.read()
+    dt = np.complex64 if mode == 4 else np.float32
+    n = len(body) // (np.dtype(dt).itemsize * nx * ny)
+    return np.frombuffer(body[:n * nx * ny * np.dtype(dt).itemsize], dt).reshape(n, ny, nx), h
+
+
+def labels(h):
+    import struct
+    n = struct.unpack_from("<i", h, 220)[0]
+    return [h[224 + 80 * i:304 + 80 * i].split(b"\0")[0].decode() for i in range(n)]
+
+
+@pytest.fixture(scope="module")
+def refmod():
+    from oracle import build_ref
+    if build_ref.build() is None:
+        pytest.skip("the reference CUDA build could not be compiled")
+    from oracle import refharness
+    return refharness
+
+
+def _mrc_case(tmp_path):
+    case, _ = load("c3d_64")
+    raw = case["raw"][0].astype(np.float32)
+    inp = tmp_path / "cell.dv"
+    write_mrc_full(inp, raw, 0.08, 0.125, 528, ["acquired"], amean=5.0)
+    otf = tmp_path / "otf.tif"
+    sr.load_library()
+    sr.write_tiff_float(str(otf), case["otf"])
+    cfg = tmp_path / "config"
+    cfg.write_text(case["config"])
+    return case, raw, inp, otf, cfg
+
+
+def test_cli_saveprefiltered_writes_the_reference_bands_and_stops(tmp_path, refmod):
+    import struct
+    case, raw, inp, otf, cfg = _mrc_case(tmp_path)
+    out, sep = tmp_path / "cell_proc.dv", tmp_path / "sep.dv"
+    run_cli([str(inp), str(out), str(otf), "-c", str(cfg), "--saveprefiltered", str(sep)])
+    assert os.path.getsize(out) == 1024  # header only: the volume was not reconstructed
+    got, h = read_mrc_sections(sep)
+    nx, ny = case["nx"], case["ny"]
+    assert struct.unpack_from("<4i", h, 0) == (nx // 2 + 1, ny, raw.shape[0], 4)
+    assert struct.unpack_from("<i", h, 92)[0] == 0
+    assert struct.unpack_from("<3f", h, 76) == (0.0, 1.0, 0.0)
+    assert labels(h) == ["acquired", "separated bands of all directions"]
+    ref = refmod.RefRecon(nx, ny, raw.shape[0], case["config"], case["otf"])
+    ref.set_raw(raw)
+    ref.load_and_rescale(0)
+    ref.set_cur_time(0)
+    ref.stage_separate()
+    nz = ref.nz
+    assert got.shape[0] == 3 * 5 * nz
+    for d in range(3):
+        for b in range(5):
+            want = ref.band(d, b)
+            part = got[(d * 5 + b) * nz:(d * 5 + b + 1) * nz]
+            assert rel_l2(part, want) < 2e-5, (d, b)
+    ref.close()
+
+
+def test_cli_saveoverlaps_writes_the_reference_overlaps_and_stops(tmp_path, refmod):
+    import struct
+    case, raw, inp, otf, cfg = _mrc_case(tmp_path)
+    out, ovl = tmp_path / "cell_proc.dv", tmp_path / "ovl.dv"
+    run_cli([str(inp), str(out), str(otf), "-c", str(cfg), "--saveoverlaps", str(ovl)])
+    assert os.path.getsize(out) == 1024
+    got, h = read_mrc_sections(ovl)
+    nx, ny = case["nx"], case["ny"]
+    ref = refmod.RefRecon(nx, ny, raw.shape[0], case["config"], case["otf"])
+    ref.capture_overlaps(True)
+    ref.set_raw(raw)
+    ref.load_and_rescale(0)
+    ref.set_cur_time(0)
+    ref.stage_separate()
+    ref.stage_fit()
+    nz = ref.nz
+    assert struct.unpack_from("<4i", h, 0) == (nx, ny, nz * 2 * 3, 4)
+    assert struct.unpack_from("<hh", h, 180)[1] == 1 and struct.unpack_from("<h", h, 196)[0] == 2
+    assert labels(h) == ["acquired", "overlaps in real space"]
+    assert got.shape[0] == 3 * nz * 2  # per direction searched: z-interleaved overlap 0 / overlap 1 sections
+    for d in range(3):
+        o0, o1 = ref.captured_overlaps(d)
+        part = got[d * 2 * nz:(d + 1) * 2 * nz]
+        assert rel_l2(part[0::2], o0) < 1e-4, d
+        assert rel_l2(part[1::2], o1) < 1e-4, d
+    ref.close()
+
+
+def test_cli_saveoverlaps_tiff_mode_keeps_the_last_direction(tmp_path, refmod):
+    case, _ = load("c3d_64")
+    raw = case["raw"][0].astype(np.float32)
+    data = tmp_path / "data"
+    data.mkdir()
+    sr.load_library()
+    sr.write_tiff_float(str(data / "cell_t0.tif"), raw)
+    otf = tmp_path / "otf.tif"
+    sr.write_tiff_float(str(otf), case["otf"])
+    cfg = tmp_path / "config"
+    cfg.write_text(case["config"])
+    ovl = tmp_path / "ovl.tif"
+    run_cli([str(data), "cell", str(otf), "-c", str(cfg), "--saveoverlaps", str(ovl)])
+    assert not (data / "GPUsirecon" / "cell_t0_proc.tif").exists()
+    got = sr.read_tiff_float(str(ovl))  # [2 nz][ny][2 nx] floats: overlap 0 planes, then overlap 1
+    ref = refmod.RefRecon(case["nx"], case["ny"], raw.shape[0], case["config"], case["otf"])
+    ref.capture_overlaps(True)
+    ref.set_raw(raw)
+    ref.load_and_rescale(0)
+    ref.set_cur_time(0)
+    ref.stage_separate()
+    ref.stage_fit()
+    o0, o1 = ref.captured_overlaps(2)
+    c = got[..., 0::2] + 1j * got[..., 1::2]
+    assert c.shape == (2 * ref.nz, case["ny"], case["nx"])
+    assert rel_l2(c[:ref.nz], o0) < 1e-4 and rel_l2(c[ref.nz:], o1) < 1e-4
+    ref.close()
+
+
+def test_cli_savealignedraw_writes_a_header_and_stops(tmp_path):
+    import struct
+    case, raw, inp, otf, cfg = _mrc_case(tmp_path)
+    out, al = tmp_path / "cell_proc.dv", tmp_path / "aligned.dv"
+    run_cli([str(inp), str(out), str(otf), "-c", str(cfg), "--savealignedraw", str(al)])
+    assert os.path.getsize(out) == 1024 and os.path.getsize(al) == 1024
+    with open(al, "rb") as f:
+        h = f.read()
+    assert struct.unpack_from("<4i", h, 0) == (case["nx"], case["ny"], raw.shape[0], 2)
+    assert labels(h) == ["acquired", "drift-corrected raw images"]
+    assert struct.unpack_from("<3f", h, 76) == (-3.5, 4321.0, 5.0)  # the input header's min, max, mean
