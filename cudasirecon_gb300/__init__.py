@@ -246,14 +246,15 @@ class Reconstructor:
         self.h = self.lib.SR_new_from_shape(nx, ny, nimages, cfg.encode())
         if not self.h:
             raise SIReconError(_err(self.lib))
-        self.nx, self.ny, self.nimages = nx, ny, nimages
+        self.nx, self.ny, self.nimages = nx, ny, nimages  # the raw planes' shape
         ip = self.image_params()
         rp = self.recon_params()
         self.nz = ip.nz
         self.ndirs = rp.ndirs
         self.nphases = rp.nphases
         self.norders = rp.norders
-        self.out_shape = (rp.z_zoom * ip.nz0, int(round(rp.zoomfact * ny)), int(round(rp.zoomfact * nx)))
+        self.nx_recon = ip.nx  # after deskew / cropXY
+        self.out_shape = (rp.z_zoom * ip.nz0, int(round(rp.zoomfact * ny)), int(round(rp.zoomfact * ip.nx)))
 
     def _check(self):
         e = _err(self.lib)
@@ -319,7 +320,7 @@ class Reconstructor:
         self._check()
 
     def band(self, d: int, b: int) -> np.ndarray:
-        nxh = self.nx // 2 + 1
+        nxh = self.nx_recon // 2 + 1
         out = np.empty((self.nz, self.ny, nxh * 2), np.float32)
         self.lib.SRX_getBand(self.h, d, b, out.ctypes.data_as(C.POINTER(C.c_float)))
         self._check()

@@ -152,7 +152,10 @@ __device__ __forceinline__ float2 filter_scale(const FilterArgs& a, const Filter
     float rho;
     float zdistabs = abs(z0);
     const float ra = rdistabs * k.rapo;
-    if (a.zapocutoff > 0) {
+    if (a.zapocutoff > 0 && a.bessel) {  // gpuFunctionsImpl.cu:1572-1577
+      const float rhox = xabs * k.rrcut, rhoy = yabs * k.rapo, rhoz = zdistabs * k.rzapo;
+      rho = sqrtf(rhox * rhox + rhoy * rhoy + rhoz * rhoz);
+    } else if (a.zapocutoff > 0) {
       const float rz = zdistabs * k.rzapo;
       rho = sqrtf(ra * ra + rz * rz);
     } else {

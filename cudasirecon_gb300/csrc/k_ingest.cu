@@ -585,6 +585,60 @@ __global__ void __launch_bounds__(kThreads) k_separate4(float2* spec, const floa
   }
 }
 
+namespace {
+template <typename T>
+__global__ void k_precondition(const __grid_constant__ PrecondArgs a)
+{
+  const size_t plane = (size_t)a.ny * a.nx, n = (size_t)a.nimg * plane;
+  const T* raw = (const T*)a.raw;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int s = (int)(i / plane);
+    const size_t r = i - (size_t)s * plane;
+    const int y = (int)(r / a.nx), xo = (int)(r - (size_t)y * a.nx);
+    const T* sec = raw + (size_t)s * a.ny * a.nx_raw;
+    const float bgx = a.bgx ? a.bgx[s] : 0.f;
+    // load_and_flatfield of raw pixel (yy, k)
+    auto flat = [&](int yy, int k) {
+      const size_t q = (size_t)yy * a.nx_raw + k;
+      const float bg = a.bg ? a.bg[q] : a.bgconst;
+      const float sl = a.slope ? a.slope[q] : 1.0f;
+      return (((float)sec[q] - bg) - bgx) * sl * a.inscale;
+    };
+    float v = 0.f;
+    if (a.deskew_factor == 0.f) {
+      if (xo < a.nx_raw) v = flat(y, xo);
+    } else {
+      // z of this raw section (loadImageData's order, cudaSirecon.cpp:1374-1382)
+      const int z = a.fastSI ? s / (a.ndirs * a.nphases) : (s / a.nphases) % a.nz;
+      const float xin = (float)((double)xo - a.nx / 2. + a.extra_shift - (double)a.deskew_factor * (z - a.nz / 2.) +
+                                a.nx_raw / 2.);
+      if (xin >= 0 && xin < a.nx_raw) {
+        const int i0 = (int)floorf(xin);
+        const float off = xin - floorf(xin);
+        // the reference reads the next pixel of the section buffer: the next
+        // row's first one at the end of a row (zero past the last row)
+        const float a1 = i0 + 1 < a.nx_raw ? flat(y, i0 + 1) : (y + 1 < a.ny ? flat(y + 1, 0) : 0.f);
+        v = __fadd_rn(__fmul_rn(1.f - off, flat(y, i0)), __fmul_rn(off, a1));
+      }
+    }
+    a.out[i] = v;
+  }
+}
+}  // namespace
+
+int launch_precondition(const PrecondArgs& a, cudaStream_t s, long long* launches)
+{
+  const size_t n = (size_t)a.nimg * a.ny * a.nx;
+  const unsigned nb = (unsigned)std::min<size_t>((n + kThreads - 1) / kThreads, 152 * 16);
+  KernelTimer* kt = kernel_timer();
+  if (kt) kt->begin(s);
+  if (a.raw_is_u16) k_precondition<uint16_t><<<nb, kThreads, 0, s>>>(a);
+  else k_precondition<float><<<nb, kThreads, 0, s>>>(a);
+  if (kt) kt->end("k_precondition", s, (double)a.nimg * a.ny * a.nx_raw * (a.raw_is_u16 ? 2 : 4) + 4.0 * n);
+  if (launches) *launches += 1;
+  return (int)cudaGetLastError();
+}
+
 int launch_rescale(const float2* spec, int nx, int ny, int nz, int ndirs, int nphases, int t, int equalizez,
                    int equalizet, double* sdp0, float* scale, cudaStream_t s, long long* launches)
 {

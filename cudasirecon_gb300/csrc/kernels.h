@@ -73,6 +73,27 @@ void allow_dynamic_smem(const void* func, size_t bytes);
 
 int launch_ingest(const IngestArgs& a, cudaStream_t s, long long* launches);
 
+// The load steps before the transforms when the raw planes are not taken as
+// they are: load_and_flatfield (cudaSirecon.cpp:1715-1731) with a per-section
+// extra background, then deskewOneSection (1733-1760): a shift along x that
+// grows with z (linear interpolation), or, without deskew, the first nx
+// columns.  out = [nimg][ny][nx] float in raw section order, ready for
+// launch_ingest with no background, unit slope and unit scale.
+struct PrecondArgs {
+  const void* raw;  // [nimg][ny][nx_raw] uint16 or float
+  int raw_is_u16;
+  int nx_raw, ny, nx, nz, ndirs, nphases, fastSI, nimg;
+  const float* bg;     // [ny][nx_raw] or null (then bgconst)
+  const float* slope;  // [ny][nx_raw] or null (then 1)
+  float bgconst;
+  const float* bgx;    // [nimg] extra background per raw section
+  float inscale;
+  float deskew_factor;  // 0: no deskew
+  int extra_shift;
+  float* out;
+};
+int launch_precondition(const PrecondArgs& a, cudaStream_t s, long long* launches);
+
 // Bleach-correction ratios from the plane sums (DC terms of spec):
 // scale[d][p][z] (float); sdp0 [nz] (double) persists across time points.
 int launch_rescale(const float2* spec, int nx, int ny, int nz, int ndirs, int nphases, int t, int equalizez,

@@ -77,6 +77,9 @@ const std::map<std::string, Opt>& table()
       // extension: use the declared bool flags instead of the reference's
       // int-sized reads (default on = reference behaviour)
       {"referenceFlagBytes", {kSwitch, F(o->reference_flag_bytes), "1"}},
+      // extension: the reference sets bBgInExtHdr only through ReconParams
+      // (no option); per-section backgrounds from the MRC extended header
+      {"bgInExtHdr", {kInt, F(o->p.bBgInExtHdr), "1"}},
   };
   return t;
 }

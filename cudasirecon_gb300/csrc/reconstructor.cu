@@ -33,6 +33,23 @@ uint32_t fbits(float f)
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+// notGoodDimension / findOptimalDimension (cudaSirecon.cpp:76-97): the
+// largest size <= n that factors into 2, 3, 5 and 7
+bool not_good_dimension(unsigned num)
+{
+  if (num == 2 || num == 3 || num == 5 || num == 7) return false;
+  if (num % 2 == 0) return not_good_dimension(num / 2);
+  if (num % 3 == 0) return not_good_dimension(num / 3);
+  if (num % 5 == 0) return not_good_dimension(num / 5);
+  if (num % 7 == 0) return not_good_dimension(num / 7);
+  return true;
+}
+unsigned find_optimal_dimension(unsigned n)
+{
+  while (n > 1 && not_good_dimension(n)) --n;
+  return n;
+}
+
 float2v cmulh(float2v a, float2v b) { return float2v{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
 float cmagh(float2v a) { return sqrt(a.x * a.x + a.y * a.y); }
 
@@ -303,10 +320,32 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
     *err = "number of images (" + std::to_string(nimages) + ") is not a multiple of ndirs*nphases";
     return false;
   }
-  if (fabs(p.deskewAngle) > 0.f || p.bBessel || p.bTwolens || p.nzPadTo || p.cropXYto) {
-    *err = "deskew, Bessel, two-lens, nzPadTo and cropXY modes are not supported by this build";
+  if (p.bTwolens) {  // makeoverlaps / filterbands stop there (gpuFunctionsImpl.cu:540-543)
+    *err = "Sorry, this program doesn't handel 2-objective mode data";
     return false;
   }
+  if (p.nzPadTo) {
+    *err = "nzPadTo is not supported by this build";
+    return false;
+  }
+  // setup_common's deskew and crop (cudaSirecon.cpp:1153-1170): the width
+  // reconstructed becomes a good FFT size covering the sheared planes, dz
+  // the distance between them; cropXY keeps the first cropXYto columns
+  if (fabs(p.deskewAngle) > 0.) {
+    if (p.deskewAngle < 0) p.deskewAngle += 180.;
+    ip.nx = (int)find_optimal_dimension(
+        (unsigned)(ip.nx_raw + ip.nz0 * fabs(cos(p.deskewAngle * M_PI / 180.)) * ip.dz / ip.dxy));
+    ip.dz_raw = ip.dz;
+    ip.dz *= fabs(sin(p.deskewAngle * M_PI / 180.));
+  }
+  if (p.cropXYto > 0 && p.cropXYto < (unsigned)ip.nx) ip.nx = (int)p.cropXYto;
+  nx = ip.nx;
+  nx_raw_ = ip.nx_raw;
+  deskew_factor_ = 0.f;
+  if (fabs(p.deskewAngle) > 0.0) deskew_factor_ = cos(p.deskewAngle * M_PI / 180.) * ip.dz_raw / ip.dxy;
+  // deskew or crop change the planes' geometry; per-section backgrounds
+  // (bBgInExtHdr, also settable later through ReconParams) use the same pass
+  precondition_ = deskew_factor_ != 0.f || ip.nx != ip.nx_raw;
   p.norders = p.norders_output != 0 ? p.norders_output : p.nphases / 2 + 1;
   if (2 * p.norders - 1 != p.nphases) {
     *err = "nphases must equal 2*norders-1 (the band separation swaps nphases bands)";
@@ -418,10 +457,14 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
     float alpha = asinf(p.na / p.nimm);
     float zd = (int)ceil(((1.0 - cosf(alpha)) / lambdaem) / dkz);
     if (zd > nz_ / 2) zd = ((nz_ / 2 - 1) > 0) ? (nz_ / 2 - 1) : 0;
+    // Bessel mode: the cutoff depends on k0 and the order (overlap_zdc_bessel):
+    // buffers for the largest one
+    if (p.bBessel) zd = ((nz_ / 2 - 1) > 0) ? (nz_ / 2 - 1) : 0;
     zdc_ovl_ = (int)zd;
   }
 
   // device arena
+  const size_t nrawxy = (size_t)nx_raw_ * ny_;
   const size_t nspec = (size_t)ndirs_ * nph_ * nz_ * ny_ * nxh_;
   const int nzb = 2 * zdc_ovl_ + 1;
   const size_t nxy = (size_t)nx_ * ny_;
@@ -438,7 +481,9 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
     size_t bytes;
   };
   std::vector<Req> reqs = {
-      {&d_raw_, (size_t)nimg_ * nxy * sizeof(float)},
+      {&d_raw_, (size_t)nimg_ * nrawxy * sizeof(float)},
+      {(void**)&d_pre_, precondition_ ? (size_t)nimg_ * nxy * sizeof(float) : 0},
+      {(void**)&d_bgx_, precondition_ ? (size_t)nimg_ * sizeof(float) : 0},
       {(void**)&d_spec_, nspec * sizeof(float2)},
       {(void**)&d_scale_, (size_t)ndirs_ * nph_ * nz_ * sizeof(float)},
       {(void**)&d_sdp0_, (size_t)nz_ * sizeof(double)},
@@ -471,8 +516,8 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
   if (dry_run_) {
     // every buffer the handle can hold: the arena, process_series' second raw
     // and output buffers, the flat-field calibration
-    planned_bytes_ = total + (size_t)nimg_ * nxy * sizeof(float) + (size_t)X_ * Y_ * Z_ * sizeof(float) +
-                     (p.bUsecorr ? 2 * nxy * sizeof(float) : 0);
+    planned_bytes_ = total + (size_t)nimg_ * nrawxy * sizeof(float) + (size_t)X_ * Y_ * Z_ * sizeof(float) +
+                     (p.bUsecorr ? 2 * nrawxy * sizeof(float) : 0);
     return true;
   }
   check(cudaGetDevice(&device_), "cudaGetDevice");
@@ -486,7 +531,7 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
   arena_bytes_ = total;
   size_t off = 0;
   for (auto& r : reqs) {
-    *r.ptr = arena_ + off;
+    *r.ptr = r.bytes ? arena_ + off : nullptr;
     off += align_up(r.bytes, 256);
   }
   check(cudaHostAlloc((void**)&h_pinned_, 4096, cudaHostAllocMapped), "cudaHostAlloc");
@@ -499,6 +544,8 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
   check(cudaMemset(d_sdp0_, 0, (size_t)nz_ * sizeof(double)), "memset");
   check(cudaMemset(d_spec_, 0, nspec * sizeof(float2)), "memset");
   check(cudaMemset(d_fitslots_, 0, (size_t)kMaxDirs * kMaxOrders * 4 * sizeof(double)), "memset");
+  if (precondition_) check(cudaMemset(d_bgx_, 0, (size_t)nimg_ * sizeof(float)), "memset");
+  if (p.bBgInExtHdr) ensure_precondition_buffers();
   check_launch(upload_amps(), "fit init");
   check(cudaStreamSynchronize(stream_), "fit init");
   if (p.bUsecorr && !load_corr(err)) return false;
@@ -525,6 +572,7 @@ SIM_Reconstructor::~SIM_Reconstructor()
   if (arena_) cudaFree(arena_);
   if (d_flush_) cudaFree(d_flush_);
   if (d_bgslope_) cudaFree(d_bgslope_);
+  if (pre_own_) cudaFree(pre_own_);
   if (h_pinned_) cudaFreeHost(h_pinned_);
   if (stream_) cudaStreamDestroy(stream_);
 }
@@ -621,7 +669,7 @@ void SIM_Reconstructor::reset_profile()
 // -------------------------------------------------------------- ingestion
 void SIM_Reconstructor::stage_raw(const void* raw, bool u16)
 {
-  const size_t n = (size_t)nimg_ * nx_ * ny_;
+  const size_t n = (size_t)nimg_ * nx_raw_ * ny_;
   raw_u16_ = u16;
   check(cudaMemcpyAsync(d_raw_, raw, n * (u16 ? 2 : 4), cudaMemcpyHostToDevice, stream_), "raw upload");
   have_raw_ = true;
@@ -655,6 +703,37 @@ void SIM_Reconstructor::ingest()
   ia.napodize = opt.p.napodize;
   ia.apofact = d_apofact_;
   ia.spec = d_spec_;
+  if (precondition_ || opt.p.bBgInExtHdr) {
+    ensure_precondition_buffers();
+    // flat field with the per-section backgrounds, then deskew or crop, into
+    // d_pre_; the transforms then take those planes as they are
+    PrecondArgs pa{};
+    pa.raw = d_raw_;
+    pa.raw_is_u16 = raw_u16_;
+    pa.nx_raw = nx_raw_;
+    pa.ny = ny_;
+    pa.nx = nx_;
+    pa.nz = nz_;
+    pa.ndirs = ndirs_;
+    pa.nphases = nph_;
+    pa.fastSI = opt.p.bFastSIM;
+    pa.nimg = nimg_;
+    pa.bg = d_bgslope_;
+    pa.slope = d_bgslope_ ? d_bgslope_ + (size_t)nx_raw_ * ny_ : nullptr;
+    pa.bgconst = opt.p.constbkgd;
+    pa.bgx = d_bgx_;
+    pa.inscale = opt.ip.inscale;
+    pa.deskew_factor = deskew_factor_;
+    pa.extra_shift = opt.p.extraShift;
+    pa.out = d_pre_;
+    check_launch(launch_precondition(pa, stream_, &launches_), "deskew / crop");
+    ia.raw = d_pre_;
+    ia.raw_is_u16 = 0;
+    ia.bg = nullptr;
+    ia.slope = nullptr;
+    ia.bgconst = 0.f;
+    ia.inscale = 1.f;
+  }
   check_launch(launch_ingest(ia, stream_, &launches_), "ingest");
   // processOneVolume without loadAndRescaleImage uses unit ratios
   check_launch(launch_fill(d_scale_, (size_t)ndirs_ * nph_ * nz_, 1.0f, stream_, &launches_), "scale init");
@@ -664,14 +743,14 @@ void SIM_Reconstructor::ingest()
 
 void SIM_Reconstructor::set_raw_float(const float* raw, int nx, int ny, int nz)
 {
-  if (nx != nx_ || ny != ny_ || nz != nimg_)
+  if (nx != nx_raw_ || ny != ny_ || nz != nimg_)
     throw std::runtime_error("setRaw: shape does not match the reconstructor");
   stage_raw(raw, false);
 }
 
 void SIM_Reconstructor::set_raw_u16(const uint16_t* raw, int nx, int ny, int nz)
 {
-  if (nx != nx_ || ny != ny_ || nz != nimg_)
+  if (nx != nx_raw_ || ny != ny_ || nz != nimg_)
     throw std::runtime_error("setRaw: shape does not match the reconstructor");
   stage_raw(raw, true);
 }
@@ -682,6 +761,7 @@ void SIM_Reconstructor::load_and_rescale(int it, int iw)
   TimerScope ts(this);
   (void)iw;
   if (!have_raw_) throw std::runtime_error("loadAndRescaleImage before setRaw/setFile");
+  if (opt.p.bBessel && opt.p.bNoRecon) return;  // cudaSirecon.cpp:1325
   if (!opt.p.do_rescale) return;
   cudaEvent_t a;
   long long l0;
@@ -718,7 +798,10 @@ void SIM_Reconstructor::build_overlaps(int d, int o1, int o2, float k0x, float k
   a.order2 = o2;
   // makeoverlaps scalars, gpuFunctionsImpl.cu:497-555 (float arithmetic)
   float order0_2_factor = 1.0f;
-  if (nz_ > 1) order0_2_factor = 5.0f;
+  if (nz_ > 1) {
+    order0_2_factor = 5.0f;
+    if (p.bBessel) order0_2_factor = 4.0f;
+  }
   float dxy = ip.dxy;
   float dkx = 1.0f / (nx_ * dxy);
   float dky = 1.0f / (ny_ * dxy);
@@ -731,9 +814,9 @@ void SIM_Reconstructor::build_overlaps(int d, int o1, int o2, float k0x, float k
   a.dkx = dkx;
   a.dky = dky;
   a.rdistcutoff = rdistcutoff;
-  a.otfcutoff = p.otfcutoff;
+  a.otfcutoff = p.bBessel ? 0.01f : p.otfcutoff;
   a.order0_2_factor = order0_2_factor;
-  a.zdc = zdc_ovl_;
+  a.zdc = p.bBessel ? overlap_zdc_bessel(o2, k0x, k0y) : zdc_ovl_;
   a.nokz0 = effective_nokz0(opt);
   const int dir_ = p.bOneOTFperAngle ? d : 0;
   for (int o = 0; o < norders_; ++o)
@@ -754,6 +837,25 @@ void SIM_Reconstructor::build_overlaps(int d, int o1, int o2, float k0x, float k
   cur_o2_ = o2;
   cache_.clear();
   sumx_ = sumy_ = -1;
+}
+
+// makeoverlaps' zdistcutoff in Bessel mode (gpuFunctionsImpl.cu:533-548): it
+// depends on the pattern's magnitude and the order built; clamped like the
+// widefield one to nz/2 - 1 (never more than the overlap buffers hold)
+int SIM_Reconstructor::overlap_zdc_bessel(int order2, float k0x, float k0y) const
+{
+  const ReconParams& p = opt.p;
+  const ImageParams& ip = opt.ip;
+  float dkz = ip.dz > 0.0f ? 1.0f / (nz_ * ip.dz) : p.dkzotf;
+  float k0mag = sqrt(k0x * k0x + k0y * k0y);
+  float lambdaem = (ip.wave[0] / p.nimm) / 1.0e3;
+  float alpha = asinf(p.na / p.nimm);
+  float kzExMax = 2.0 * p.BesselNA / p.BesselLambdaEx;
+  float halfangle = acosf(k0mag * order2 / (p.norders - 1) / kzExMax);
+  float zd = ceil((kzExMax * sinf(halfangle) + (1.0 - cosf(alpha)) / lambdaem) / dkz);
+  const int zmax = (nz_ / 2 - 1) > 0 ? (nz_ / 2 - 1) : 0;
+  if (!(zd <= nz_ / 2)) zd = zmax;  // also a NaN half angle
+  return std::min((int)zd, zdc_ovl_);
 }
 
 // XStarY for a batch of (angle, mag) candidates, cached as modamp1 = XStarY/sumX
@@ -838,7 +940,7 @@ float2v SIM_Reconstructor::findrealspacemodamp(int d, int o1, int o2, float k0x,
 // findk0 (gpuFunctionsImpl.cu:306-372)
 void SIM_Reconstructor::findk0(int d)
 {
-  const int fitorder2 = nz_ > 1 ? 2 : 1;
+  const int fitorder2 = nz_ > 1 && !opt.p.bBessel ? 2 : 1;
   float2v k0 = k0_[d];
   build_overlaps(d, 0, fitorder2, k0.x, k0.y);
   check_launch(launch_crosscorr_peak(d_pmap_, d_cc_, nx_, ny_, d_bval_, d_bidx_, d_peak_, stream_, &launches_),
@@ -869,7 +971,7 @@ void SIM_Reconstructor::fitk0andmodamps(int d)
 {
   ReconParams& p = opt.p;
   const int fitorder1 = 0;
-  const int fitorder2 = nz_ > 1 ? 2 : 1;
+  const int fitorder2 = nz_ > 1 && !opt.p.bBessel ? 2 : 1;
   float2v* k0 = &k0_[d];
   float k0mag = sqrt(k0->x * k0->x + k0->y * k0->y);
   float k0angle = atan2(k0->y, k0->x);
@@ -1142,10 +1244,21 @@ void SIM_Reconstructor::filter_zdc(int* zdc) const
   float lambdaexc = 0.88 * lambdaem;
   float alpha = asinf(p.na / p.nimm);
   for (int o = 0; o < kMaxOrders; ++o) zdc[o] = 0;
-  zdc[0] = (int)ceil(((1 - cosf(alpha)) / lambdaem) / dkz);
-  zdc[norders_ - 1] = 1.3 * zdc[0];
-  if (norders_ >= 3)
-    for (int order = 1; order < norders_ - 1; order++) zdc[order] = (1 + lambdaem / lambdaexc) * zdc[0];
+  if (p.bBessel) {  // gpuFunctionsImpl.cu:1260-1271
+    float k0mag = sqrt(k0_[0].x * k0_[0].x + k0_[0].y * k0_[0].y);
+    float kzExMax = 2 * p.BesselNA / p.BesselLambdaEx;
+    zdc[0] = (int)rint((kzExMax + (1 - cosf(alpha)) / lambdaem) / dkz);
+    for (int order = 1; order < norders_; order++) {
+      float halfangle = acosf(k0mag * order / (norders_ - 1) / kzExMax);
+      float zd = ceil((kzExMax * sinf(halfangle) + (1.0 - cosf(alpha)) / lambdaem) / dkz);
+      zdc[order] = zd == zd ? (int)zd : nz_;  // a NaN half angle: clamped below
+    }
+  } else {
+    zdc[0] = (int)ceil(((1 - cosf(alpha)) / lambdaem) / dkz);
+    zdc[norders_ - 1] = 1.3 * zdc[0];
+    if (norders_ >= 3)
+      for (int order = 1; order < norders_ - 1; order++) zdc[order] = (1 + lambdaem / lambdaexc) * zdc[0];
+  }
   for (int order = 0; order < norders_; order++)
     if (zdc[order] >= nz_ / 2) zdc[order] = ((nz_ / 2 - 1) > 0 ? (nz_ / 2 - 1) : 0);
 }
@@ -1217,7 +1330,7 @@ void SIM_Reconstructor::filter_and_assemble()
   (void)alpha;
   (void)lambdaexc;
   float apocutoff = rdistcutoff + k0mag * (norders_ - 1);
-  float zapocutoff = norders_ > 1 ? zdc[1] : 0;
+  float zapocutoff = p.bBessel ? zdc[0] : (norders_ > 1 ? zdc[1] : 0);
   fa.dkx = 1. / (nx_ * dxy);
   fa.dky = 1. / (ny_ * dxy);
   fa.rdistcutoff = rdistcutoff;
@@ -1236,7 +1349,7 @@ void SIM_Reconstructor::filter_and_assemble()
   fa.nokz0 = effective_nokz0(opt);
   fa.filteroverlaps = p.bFilteroverlaps;
   fa.apodizeoutput = p.apodizeoutput;
-  fa.bessel = 0;
+  fa.bessel = p.bBessel;
   fa.otf.nzotf = p.nzotf;
   fa.otf.nxotf = p.nxotf;
   fa.otf.dkrotf = p.dkrotf;
@@ -1301,9 +1414,9 @@ int SIM_Reconstructor::process_one_volume(bool sync)
     return last_result_;
   }
   last_result_ = 1;
-  prepare_asm_tables();
   separate();
   fit_all();
+  prepare_asm_tables();  // after the fit: in Bessel mode the in-band planes depend on k0
   filter_and_assemble();
   if (sync) check(cudaStreamSynchronize(stream_), "processOneVolume");
   have_raw_ = false;  // the bands are consumed (filtered in place)
@@ -1343,13 +1456,13 @@ bool SIM_Reconstructor::load_corr(std::string* err)
     *err = "File " + path + " does not exist";
     return false;
   }
-  if (f.hdr.nx != nx_ || f.hdr.ny != ny_ || f.hdr.nz < 2) {
+  if (f.hdr.nx != nx_raw_ || f.hdr.ny != ny_ || f.hdr.nz < 2) {
     *err = "calibration file " + path + " has different dimension than data file";
     return false;
   }
   std::vector<float> bg, sl;
   if (!mrc_read_section(f, 0, &bg, err) || !mrc_read_section(f, 1, &sl, err)) return false;
-  const size_t n = (size_t)nx_ * ny_;
+  const size_t n = (size_t)nx_raw_ * ny_;
   if (bg.size() != n || sl.size() != n) {
     *err = "calibration file " + path + ": sections are not real nx x ny images";
     return false;
@@ -1453,12 +1566,12 @@ void SIM_Reconstructor::process_series(const void* const* raws, bool u16, float*
 {
   if (n <= 0) return;
   if (!raws || !outs) throw std::runtime_error("processSeries: null buffer list");
-  const size_t raw_bytes = (size_t)nimg_ * nx_ * ny_ * (u16 ? 2 : 4);
+  const size_t raw_bytes = (size_t)nimg_ * nx_raw_ * ny_ * (u16 ? 2 : 4);
   const size_t out_bytes = out_elems() * sizeof(float);
   if (!d_raw_alt_) {
-    check(cudaMalloc(&d_raw_alt_, (size_t)nimg_ * nx_ * ny_ * sizeof(float)), "series raw buffer");
+    check(cudaMalloc(&d_raw_alt_, (size_t)nimg_ * nx_raw_ * ny_ * sizeof(float)), "series raw buffer");
     check(cudaMalloc((void**)&d_out_extra_, out_bytes), "series output buffer");
-    series_bytes_ = (size_t)nimg_ * nx_ * ny_ * sizeof(float) + out_bytes;
+    series_bytes_ = (size_t)nimg_ * nx_raw_ * ny_ * sizeof(float) + out_bytes;
     d_out_alt_ = d_out_extra_;
     check(cudaStreamCreateWithFlags(&h2d_stream_, cudaStreamNonBlocking), "series stream");
     check(cudaStreamCreateWithFlags(&d2h_stream_, cudaStreamNonBlocking), "series stream");
@@ -1573,6 +1686,20 @@ double SIM_Reconstructor::bench_device(int steps)
   cudaEventDestroy(b);
   have_raw_ = true;
   return total;
+}
+
+// The preconditioning buffers when the geometry did not need them at setup
+// (bBgInExtHdr alone): allocated on first use, zero backgrounds
+void SIM_Reconstructor::ensure_precondition_buffers()
+{
+  if (d_pre_ && d_bgx_) return;
+  const size_t npre = (size_t)nimg_ * nx_ * ny_;
+  check(cudaMalloc((void**)&pre_own_, npre * sizeof(float) + (size_t)nimg_ * sizeof(float) + 256),
+        "preconditioning buffers");
+  d_pre_ = pre_own_;
+  d_bgx_ = pre_own_ + npre;
+  check(cudaMemset(d_bgx_, 0, (size_t)nimg_ * sizeof(float)), "memset");
+  series_bytes_ += npre * sizeof(float) + (size_t)nimg_ * sizeof(float);
 }
 
 // ------------------------------------------------------------ debug dumps
@@ -1832,16 +1959,37 @@ void SIM_Reconstructor::set_file(int it, int iw)
     if (it < 0 || (size_t)it >= tiff_files_.size()) throw std::runtime_error("setFile: time index out of range");
     Stack s;
     if (!tiff_read(tiff_files_[it], &s, &err)) throw std::runtime_error(err);
-    if (s.width != nx_ || s.height != ny_ || s.depth != nimg_)
+    if (s.width != nx_raw_ || s.height != ny_ || s.depth != nimg_)
       throw std::runtime_error("setFile: TIFF size differs from the first file");
     stage_raw(s.data.data(), false);
   } else {
     // sections of time point it (single wave): nimg consecutive sections
-    std::vector<float> all((size_t)nimg_ * nx_ * ny_), sec;
+    std::vector<float> all((size_t)nimg_ * nx_raw_ * ny_), sec;
     for (int s = 0; s < nimg_; ++s) {
       int idx = it * nimg_ * opt.ip.nwaves + iw * nimg_ + s;
       if (!mrc_read_section(mrc_in_, idx, &sec, &err)) throw std::runtime_error(err);
-      memcpy(&all[(size_t)s * nx_ * ny_], sec.data(), (size_t)nx_ * ny_ * sizeof(float));
+      memcpy(&all[(size_t)s * nx_raw_ * ny_], sec.data(), (size_t)nx_raw_ * ny_ * sizeof(float));
+    }
+    if (opt.p.bBgInExtHdr) {
+      ensure_precondition_buffers();
+      // loadImageData (cudaSirecon.cpp:1386-1393): each section's extra
+      // background is the third float of its extended-header record
+      // (IMRtExHdrZWT: nint ints, then nreal floats per section)
+      const MrcHeader& h = mrc_in_.hdr;
+      const size_t rec = (size_t)(h.nint + h.nreal) * 4;
+      bgx_host_.assign(nimg_, 0.f);
+      for (int s = 0; s < nimg_; ++s) {
+        const size_t idx = (size_t)it * nimg_ * opt.ip.nwaves + (size_t)iw * nimg_ + s;
+        const size_t off = idx * rec + (size_t)h.nint * 4 + 8;
+        if (h.nreal >= 3 && off + 4 <= mrc_in_.ext.size()) {
+          uint32_t u;
+          memcpy(&u, mrc_in_.ext.data() + off, 4);
+          if (mrc_in_.swapped) u = __builtin_bswap32(u);
+          memcpy(&bgx_host_[s], &u, 4);
+        }
+      }
+      check(cudaMemcpy(d_bgx_, bgx_host_.data(), (size_t)nimg_ * sizeof(float), cudaMemcpyHostToDevice),
+            "section backgrounds");
     }
     stage_raw(all.data(), false);
   }

@@ -123,6 +123,7 @@ class SIM_Reconstructor {
 
   // fitting helpers (gpuFunctionsImpl.cu:306-1148 semantics)
   void build_overlaps(int d, int o1, int o2, float k0x, float k0y);
+  int overlap_zdc_bessel(int order2, float k0x, float k0y) const;
   // evaluate XStarY for candidate (angle, mag) pairs on the current overlaps
   void eval_candidates(int o1, int o2, const std::vector<std::pair<float, float>>& cands);
   float getmodamp(int d, float angle, float mag, int o1, int o2, int redo, float2v* modamp);
@@ -133,6 +134,14 @@ class SIM_Reconstructor {
 
   // geometry
   int nx_ = 0, ny_ = 0, nz_ = 0, nxh_ = 0, nimg_ = 0, norders_ = 0, nph_ = 0, ndirs_ = 0;
+  int nx_raw_ = 0;             // width of the raw planes (nx_ after deskew / cropXY)
+  float deskew_factor_ = 0.f;  // loadImageData's deskewFactor (0: no deskew)
+  bool precondition_ = false;  // deskew, crop or per-section backgrounds: a pass before ingest
+  float* d_pre_ = nullptr;     // the preconditioned planes [nimg][ny][nx]
+  float* d_bgx_ = nullptr;     // per-section extra background [nimg] (bBgInExtHdr)
+  std::vector<float> bgx_host_;
+  float* pre_own_ = nullptr;  // their allocation when not in the arena
+  void ensure_precondition_buffers();
   int X_ = 0, Y_ = 0, Z_ = 0;
   int ndirs_otf_ = 1;
   int zdc_ovl_ = 0;  // makeoverlaps zdistcutoff

@@ -16,6 +16,7 @@
 #include "cudaSireconImpl.h"
 #include "gpuFunctions.h"
 
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -90,6 +91,7 @@ struct Harness {
   // saveoverlaps dump point), when capturing is on
   bool capture_overlaps = false;
   std::vector<std::vector<float>> captured;  // [dir][2 * nx * ny * nz0 * 2 floats]
+  std::vector<float> section_bg;  // per raw section of a time point (bBgInExtHdr)
 };
 
 // SetDefaultParams, cudaSirecon.cpp:16-72, then the program_options defaults
@@ -227,11 +229,34 @@ void apply_config(Harness* h, const char* text)
     else if (k == "bessel") p.bBessel = parse_bool(v);
     else if (k == "besselExWave") p.BesselLambdaEx = f;
     else if (k == "besselNA") p.BesselNA = f;
+    else if (k == "deskew") p.deskewAngle = f;
+    else if (k == "deskewshift") p.extraShift = i;
+    else if (k == "noRecon") p.bNoRecon = parse_bool(v);
+    else if (k == "cropXY") p.cropXYto = (unsigned)i;
+    else if (k == "bgInExtHdr") p.bBgInExtHdr = i;
     else if (k == "xyres") ip.dxy = f;
     else if (k == "zres") ip.dz = f;
     else if (k == "zresPSF") p.dzPSF = f;
     else if (k == "wavelength") ip.wave[0] = (short)i;
   }
+}
+
+// notGoodDimension / findOptimalDimension, cudaSirecon.cpp:76-97
+bool not_good_dimension(unsigned num)
+{
+  if (num == 2 || num == 3 || num == 5 || num == 7) return false;
+  else if (num % 2 == 0) return not_good_dimension(num / 2);
+  else if (num % 3 == 0) return not_good_dimension(num / 3);
+  else if (num % 5 == 0) return not_good_dimension(num / 5);
+  else if (num % 7 == 0) return not_good_dimension(num / 7);
+  else return true;
+}
+
+unsigned find_optimal_dimension(unsigned inSize, int step = -1)
+{
+  unsigned outSize = inSize;
+  while (not_good_dimension(outSize)) outSize += step;
+  return outSize;
 }
 
 // makematrix default branch, cudaSirecon.cpp:591-617 (the LAPACK branch is
@@ -265,6 +290,17 @@ void setup(Harness* h, int nx, int ny, int nImages, const float* otf, int otf_w,
   ip.nz0 = ip.nz;
   h->zoffset = 0;
   ip.dz_raw = 0;
+  // setup_common's deskew and crop, cudaSirecon.cpp:1153-1170
+  if (fabs(p.deskewAngle) > 0.) {
+    if (p.deskewAngle < 0) p.deskewAngle += 180.;
+    ip.nx = find_optimal_dimension(ip.nx_raw + ip.nz0 * fabs(cos(p.deskewAngle * M_PI / 180.)) * ip.dz / ip.dxy);
+    ip.dz_raw = ip.dz;
+    ip.dz *= fabs(sin(p.deskewAngle * M_PI / 180.));
+  } else {
+    ip.nx = ip.nx_raw;
+    ip.dz_raw = 0;
+  }
+  if (p.cropXYto > 0 && p.cropXYto < (unsigned)ip.nx) ip.nx = p.cropXYto;
 
   p.norders = (p.norders_output != 0) ? p.norders_output : p.nphases / 2 + 1;
 
@@ -338,9 +374,12 @@ void setup(Harness* h, int nx, int ny, int nImages, const float* otf, int otf_w,
     d.amp[i][0].y = 0.0f;
   }
   // bgAndSlope, constant-background branch (cudaSirecon.cpp:139-161)
-  d.background.resize(sizeof(float) * ip.nx * ip.ny);
-  d.slope.resize(sizeof(float) * ip.nx * ip.ny);
-  for (int i = 0; i < ip.nx * ip.ny; i++) {
+  // sized for the raw planes: load_and_flatfield indexes them with the raw
+  // width (constant values, so the reference's nx-sized arrays read the same)
+  const int nbg = std::max(ip.nx, ip.nx_raw) * ip.ny;
+  d.background.resize(sizeof(float) * nbg);
+  d.slope.resize(sizeof(float) * nbg);
+  for (int i = 0; i < nbg; i++) {
     ((float*)d.background.getPtr())[i] = p.constbkgd;
     ((float*)d.slope.getPtr())[i] = 1.0;
   }
@@ -348,16 +387,20 @@ void setup(Harness* h, int nx, int ny, int nImages, const float* otf, int otf_w,
 }
 
 // loadImageData (cudaSirecon.cpp:1354-1435) with load_and_flatfield
-// (1715-1731) and the no-deskew copy of deskewOneSection (1733-1760):
-// one synchronous host->device copy per plane, like the reference.
+// (1715-1731) and deskewOneSection (1733-1760): one synchronous
+// host->device copy per plane, like the reference.  The per-section extra
+// background of the bBgInExtHdr branch (1386-1393) comes from
+// refh_set_section_backgrounds (the reference reads the MRC extended header).
 void load_image_data(Harness* h)
 {
   ReconParams& p = h->p;
   ImageParams& ip = h->ip;
   ReconData& d = h->d;
-  int nx = ip.nx, ny = ip.ny;
-  int xdim = (nx / 2 + 1) * 2;
-  std::vector<float> section((size_t)nx * ny);
+  const int nx_raw = ip.nx_raw, nx = ip.nx, ny = ip.ny;
+  const int xdim = (nx / 2 + 1) * 2;
+  float deskewFactor = 0;
+  if (fabs(p.deskewAngle) > 0.0) deskewFactor = cos(p.deskewAngle * M_PI / 180.) * ip.dz_raw / ip.dxy;
+  std::vector<float> section((size_t)nx_raw * ny + 1, 0.f);  // + 1: the reference's in[indin + 1] at the end
   std::vector<float> ext((size_t)xdim * ny);
   const float* bg = (const float*)d.background.getPtr();
   const float* sl = (const float*)d.slope.getPtr();
@@ -366,13 +409,27 @@ void load_image_data(Harness* h)
       int zsec = p.bFastSIM ? (z * p.ndirs * p.nphases + direction * p.nphases)
                             : (direction * ip.nz * p.nphases + z * p.nphases);
       for (int phase = 0; phase < p.nphases; ++phase) {
-        const float* buffer = h->raw.data() + (size_t)zsec * nx * ny;
+        if (p.bBgInExtHdr) d.backgroundExtra = zsec < (int)h->section_bg.size() ? h->section_bg[zsec] : 0.f;
+        const float* buffer = h->raw.data() + (size_t)zsec * nx_raw * ny;
         for (int l = 0; l < ny; l++)
-          for (int k = 0; k < nx; k++)
-            section[l * nx + k] = (buffer[l * nx + k] - bg[l * nx + k] - d.backgroundExtra) * sl[l * nx + k] * ip.inscale;
-        for (int y = 0; y < ny; y++)
-          for (int xo = 0; xo < xdim; xo++)
-            ext[(size_t)y * xdim + xo] = (xo < nx) ? section[(size_t)y * nx + xo] : 0.f;
+          for (int k = 0; k < nx_raw; k++)
+            section[l * nx_raw + k] =
+                (buffer[l * nx_raw + k] - bg[l * nx_raw + k] - d.backgroundExtra) * sl[l * nx_raw + k] * ip.inscale;
+        for (int xout = 0; xout < xdim; xout++) {
+          float xin = xout;
+          if (fabs(deskewFactor) > 0)
+            xin = xout - nx / 2. + p.extraShift - deskewFactor * (z - ip.nz / 2.) + nx_raw / 2.;
+          for (int y = 0; y < ny; y++) {
+            unsigned indout = y * xdim + xout;
+            if (xin >= 0 && xin < nx_raw) {
+              unsigned indin = y * nx_raw + (unsigned int)floor(xin);
+              float offset = xin - floor(xin);
+              ext[indout] = (1 - offset) * section[indin] + offset * section[indin + 1];
+            } else {
+              ext[indout] = 0.;
+            }
+          }
+        }
         cudaMemcpy((char*)d.savedBands[direction][phase].getPtr() +
                        (size_t)(z + h->zoffset) * xdim * ny * sizeof(float),
                    ext.data(), (size_t)xdim * ny * sizeof(float), cudaMemcpyHostToDevice);
@@ -576,15 +633,23 @@ void refh_set_cur_time(void* hv, int it) { ((Harness*)hv)->ip.curTimeIdx = (unsi
 void refh_set_raw(void* hv, const float* raw)
 {
   Harness* h = (Harness*)hv;
-  size_t n = (size_t)h->nImages * h->ip.nx * h->ip.ny;
+  size_t n = (size_t)h->nImages * h->ip.nx_raw * h->ip.ny;
   h->raw.assign(raw, raw + n);
   load_image_data(h);
 }
+
+void refh_set_section_backgrounds(void* hv, const float* v, int n)
+{
+  ((Harness*)hv)->section_bg.assign(v, v + n);
+}
+
+int refh_nx(void* hv) { return ((Harness*)hv)->ip.nx; }
 
 // SR_loadAndRescaleImage -> rescaleDriver (cudaSirecon.cpp:520-540)
 void refh_load_and_rescale(void* hv, int it)
 {
   Harness* h = (Harness*)hv;
+  if (h->p.bBessel && h->p.bNoRecon) return;  // cudaSirecon.cpp:1325
   for (int direction = 0; direction < h->p.ndirs; ++direction)
     for (int z = 0; z < h->ip.nz; ++z)
       if (h->p.do_rescale)

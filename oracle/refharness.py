@@ -47,6 +47,9 @@ def load(build: bool = True):
     lib.refh_norders.restype = ip
     lib.refh_nz.argtypes = [vp]
     lib.refh_nz.restype = ip
+    lib.refh_nx.argtypes = [vp]
+    lib.refh_nx.restype = ip
+    lib.refh_set_section_backgrounds.argtypes = [vp, fp, ip]
     lib.refh_fit_counts.argtypes = [vp, C.POINTER(C.c_longlong)]
     lib.refh_capture_overlaps.argtypes = [vp, ip]
     lib.refh_get_captured.argtypes = [vp, ip, fp]
@@ -68,10 +71,11 @@ class RefRecon:
         self.otf = np.ascontiguousarray(otf_pages, np.float32)
         d, h, w = self.otf.shape
         self.h = self.lib.refh_new(nx, ny, nimages, config.encode(), _fptr(self.otf), w, h, d)
-        self.nx, self.ny, self.nimages, self.ndirs = nx, ny, nimages, ndirs
+        self.nx_raw, self.ny, self.nimages, self.ndirs = nx, ny, nimages, ndirs
+        self.nx = self.lib.refh_nx(self.h)  # after deskew / cropXY
         self.nz = self.lib.refh_nz(self.h)
         self.norders = self.lib.refh_norders(self.h)
-        self.out_shape = (z_zoom * self.nz, int(round(zoom * ny)), int(round(zoom * nx)))
+        self.out_shape = (z_zoom * self.nz, int(round(zoom * ny)), int(round(zoom * self.nx)))
 
     def close(self):
         if self.h:
@@ -89,7 +93,14 @@ class RefRecon:
 
     def set_raw(self, raw: np.ndarray):
         r = np.ascontiguousarray(raw, np.float32)
+        assert r.shape == (self.nimages, self.ny, self.nx_raw), r.shape
         self.lib.refh_set_raw(self.h, _fptr(r))
+
+    def set_section_backgrounds(self, values):
+        """Per raw section extra background (the reference's bBgInExtHdr
+        values from the MRC extended header)."""
+        v = np.ascontiguousarray(values, np.float32)
+        self.lib.refh_set_section_backgrounds(self.h, _fptr(v), v.size)
 
     def load_and_rescale(self, it: int = 0):
         self.lib.refh_load_and_rescale(self.h, it)
