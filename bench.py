@@ -25,7 +25,9 @@ its SR_* flow on the same workload.
 --workload uneven: a 2D/3D batch of 560 acquisitions of 28 shapes through
 SRX_serverRunBatch vs the plain one-at-a-time flow.  --workload serving:
 Poisson arrivals of requests of four configurations through SRX_server*,
-p50/p95/p99 latency and throughput vs the plain flow.
+p50/p95/p99 latency and throughput vs the plain flow.  --workload makeotf:
+SRX_makeOTF on a 128 x 128 x 64 x 5 bead PSF vs the FP64 CPU restatement.
+The default line carries compact forms of all three.
 
 Prints one JSON line (rank 0).  N>1 runs independent replicas (one process
 per GPU, weak scaling: each rank reconstructs its own time points).
@@ -460,10 +462,11 @@ def run_reference(args, rank, world, dist, nx, ny, nz, vols, otf, cfg, outvox):
                 "api": "the reference's SR_setRaw (float32 stack) -> loadAndRescaleImage -> processOneVolume -> "
                        "getResult, host memory in and out"},
         "step_roofline": step_roofline(nx, ny, nz, fc0, fc1, args.steps, dt * 1e3 / args.steps, peak, peak_kind),
-        "cpu_baseline": {"value": round(value, 1), "unit": "Mvoxels/s", "cores": 1, "kind": "reference",
+        "cpu_baseline": {"value": round(value, 1), "unit": "Mvoxels/s", "cores": os.cpu_count(), "kind": "reference",
                          "sample": "the reference's own CUDA build (gpuFunctionsImpl.cu kernels + cuFFT, host "
-                                   "orchestration restated from cudaSirecon.cpp) through its SR_* flow on the full "
-                                   "workload; one host thread drives it"},
+                                   "orchestration restated from cudaSirecon.cpp, built with OpenMP like the "
+                                   "reference) through its SR_* flow on the full workload; deskewOneSection's "
+                                   "OpenMP loop uses every host thread, the rest runs on one"},
         "clocks": clk,
     }
 
@@ -726,6 +729,42 @@ def uneven_items(n2d=500, n3d=60):
     return [order[k] for k in perm], stacks, cfgs
 
 
+MAKEOTF_ARGS = ["-angle", "-0.8043", "-ls", "0.2035", "-xyres", "0.08", "-zres", "0.125", "-na", "1.42",
+                "-nimm", "1.515", "-wavelength", "528", "-fixorigin", "3", "20"]
+
+
+def run_makeotf(args, reps=20):
+    """makeotf on the 128 x 128 x 64 x 5 bead PSF the reconstruction's OTF
+    is made from: SRX_makeOTF (host PSF in, host OTF array out, everything
+    between them on the GPU) against the FP64 numpy restatement of
+    radialft.cpp on one host core.  The shipped program's FFTW path does not
+    build here (FFTW3f and libtiff are absent)."""
+    import cudasirecon_gb300 as sr
+    from cudasirecon_gb300.synthetic import Optics, bead_psf_stack
+    sr.load_library()
+    psf = bead_psf_stack(128, 128, 64, Optics())
+    for _ in range(3):
+        got = sr.make_otf(psf, MAKEOTF_ARGS)
+    times = []
+    for _ in range(reps):
+        t = time.perf_counter()
+        sr.make_otf(psf, MAKEOTF_ARGS)
+        times.append(time.perf_counter() - t)
+    gpu_ms = statistics.median(times) * 1e3
+    from oracle import makeotf_oracle as mo
+    t = time.perf_counter()
+    want = mo.makeotf(psf, mo.MakeOTFOptions.from_args(MAKEOTF_ARGS))
+    cpu_s = time.perf_counter() - t
+    g, w = got.astype(np.float64).ravel(), np.asarray(want, np.float64).ravel()
+    rel = float(np.linalg.norm(g - w) / max(np.linalg.norm(w), 1e-300))
+    return {"psf": "128x128x64x5 float32 bead stack (seeded synthetic), 3 orders, -fixorigin 3 20",
+            "ms_per_otf": round(gpu_ms, 3), "ms_per_otf_p95": round(float(np.percentile(times, 95)) * 1e3, 3),
+            "reps": reps, "timing": "wall clock around SRX_makeOTF: H2D of the PSF, all kernels, D2H of the OTF",
+            "cpu_baseline": {"value_ms_per_otf": round(cpu_s * 1e3, 1), "cores": 1, "kind": "port",
+                             "sample": "one full OTF by the FP64 numpy restatement of radialft.cpp"},
+            "speedup_vs_cpu": round(cpu_s * 1e3 / gpu_ms, 1), "rel_l2_vs_oracle": rel}
+
+
 def run_uneven(args, compact=False):
     """C4: the uneven 2D/3D batch, plain one-volume-at-a-time SR_* flow vs
     SRX_serverRunBatch (per-shape chunks, copies overlapped, shapes
@@ -813,7 +852,8 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=list(WORKLOADS) + ["serving", "uneven"], default="timeseries_512x512x48")
+    ap.add_argument("--workload", choices=list(WORKLOADS) + ["serving", "uneven", "makeotf"],
+                    default="timeseries_512x512x48")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="leave out the serving and uneven-batch summaries of the default line")
@@ -824,9 +864,10 @@ def main():
         return
     if args.impl == "reference":
         world, dist = 1, None
-    if args.workload in ("serving", "uneven"):
+    if args.workload in ("serving", "uneven", "makeotf"):
+        run = {"serving": run_serving, "uneven": run_uneven, "makeotf": run_makeotf}[args.workload]
         if rank == 0 and args.impl != "reference":
-            print(json.dumps(run_serving(args) if args.workload == "serving" else run_uneven(args)), flush=True)
+            print(json.dumps(run(args)), flush=True)
         elif rank == 0:
             print(json.dumps({"impl": "reference",
                               "unavailable": f"the {args.workload} workload has no reference arm"}))
@@ -845,6 +886,7 @@ def main():
             t0 = time.perf_counter()
             line["serving"] = run_serving(args, compact=True)
             line["uneven_batch"] = run_uneven(args, compact=True)
+            line["makeotf"] = run_makeotf(args)
             line["extras_wall_s"] = round(time.perf_counter() - t0, 1)
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -83,6 +83,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.SRX_fftPlanChoice.argtypes = [ip, ip, C.c_char_p, ip]
     lib.SRX_setFilterFusion.restype = None
     lib.SRX_setFilterFusion.argtypes = [vp, ip]
+    lib.SRX_setDeviceK0Search.restype = None
+    lib.SRX_setDeviceK0Search.argtypes = [vp, ip]
     lib.SRX_getProfile.restype = ip
     lib.SRX_getProfile.argtypes = [vp, C.c_char_p, ip]
     lib.SRX_resetProfile.argtypes = [vp]
@@ -361,6 +363,11 @@ class Reconstructor:
         """Wiener filter inside the assembly's band load (default) or as its
         own pass (SRX_setFilterFusion)."""
         self.lib.SRX_setFilterFusion(self.h, int(on))
+
+    def set_device_search(self, on: bool = True):
+        """k0 search on the device (default) or host-driven
+        (SRX_setDeviceK0Search)."""
+        self.lib.SRX_setDeviceK0Search(self.h, int(on))
 
     def profile(self) -> dict:
         import json

@@ -20,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcudasirecon.so")
 CLI = os.path.join(HERE, "bin", "cudasirecon")
 MAKEOTF = os.path.join(HERE, "bin", "makeotf")
-SOURCES = ["fft_plan.cu", "k_selftest.cu", "k_ingest.cu", "k_fit.cu", "k_assemble.cu", "reconstructor.cu",
+SOURCES = ["fft_plan.cu", "k_selftest.cu", "k_ingest.cu", "k_fit.cu", "k_search.cu", "k_assemble.cu", "reconstructor.cu",
            "makeotf.cu", "params.cpp", "image_io.cpp", "makeotf_io.cpp", "server.cpp", "capi.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -234,6 +234,11 @@ void SRX_setFilterFusion(SIM_Reconstructor* sr, int on)
   if (need(sr)) sr->set_filter_fusion(on != 0);
 }
 
+void SRX_setDeviceK0Search(SIM_Reconstructor* sr, int on)
+{
+  if (need(sr)) sr->set_device_search(on != 0);
+}
+
 long long SRX_kernelLaunches(SIM_Reconstructor* sr) { return need(sr) ? sr->launches() : -1; }
 
 int SRX_fftSelfTest(float* data, int n, int nlines, int inverse, int columns)

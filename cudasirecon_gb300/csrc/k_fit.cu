@@ -35,13 +35,22 @@ constexpr int kThreads = 256;
 constexpr int kMaxElems = kFftElems;
 
 // ---------------------------------------------------------------- overlaps
+// the shift k0 * (order2 - order1): from the arguments, or from device memory
+// (a k0 fitted on the device) times kfac
+__device__ __forceinline__ float2 ovl_shift(const OverlapArgs& a)
+{
+  if (a.kdev == nullptr) return make_float2(a.kx, a.ky);
+  const float2 k = *a.kdev;
+  return make_float2(__fmul_rn(k.x, a.kfac), __fmul_rn(k.y, a.kfac));
+}
+
 // Element (j) of overlap `ov` on row (zb, i) before the x transform:
 // makeOverlaps0Kernel (ov 0, gpuFunctionsImpl.cu:677-778) / makeOverlaps1Kernel
 // (ov 1, 780-872): the order-1/order-2 band value times the partner OTF over
 // sqrt(|OTF1|^2 + |OTF2|^2) inside both supports, merged re + i im.
 // kzi = otf_kz(a.otf, zb - a.zdc), rdk = 1 / a.otf.dkrotf (per row / thread)
-__device__ __forceinline__ float2 ovl_value(const OverlapArgs& a, int ov, int zb, int i, int j, const OtfKz& kzi,
-                                            float rdk)
+__device__ __forceinline__ float2 ovl_value(const OverlapArgs& a, float2 ks, int ov, int zb, int i, int j,
+                                            const OtfKz& kzi, float rdk)
 {
   const int nx = a.nx, ny = a.ny, nz = a.nz, nxh = nx / 2 + 1;
   const size_t bplane = (size_t)ny * nxh;
@@ -61,7 +70,7 @@ __device__ __forceinline__ float2 ovl_value(const OverlapArgs& a, int ov, int zb
   // every decision below is the reference's float test on a square root,
   // made on the squared value (thresholds from launch_overlaps)
   if (ov == 0 && r1sq <= a.r2_le) {  // rdist1 <= cut
-    float x12 = x1f - a.kx, y12 = y1f - a.ky;
+    float x12 = x1f - ks.x, y12 = y1f - ks.y;
     const float r12sq = x12 * x12 + y12 * y12;
     if (r12sq <= a.r2_le) {  // r12 <= cut
       float2 o1 = otf_lookup_rr(a.otf.otf[a.order1], a.otf, sqrtf(r1sq) * rdk, kzi);
@@ -84,7 +93,7 @@ __device__ __forceinline__ float2 ovl_value(const OverlapArgs& a, int ov, int zb
       }
     }
   } else if (ov == 1 && r1sq < a.r2_lt) {  // rdist1 < cut
-    float x21 = x1f + a.kx, y21 = y1f + a.ky;
+    float x21 = x1f + ks.x, y21 = y1f + ks.y;
     const float r21sq = x21 * x21 + y21 * y21;
     if (r21sq <= a.r2_le) {  // r21 <= cut
       float2 o2 = otf_lookup_rr(a.otf.otf[a.order2], a.otf, sqrtf(r1sq) * rdk, kzi);
@@ -117,6 +126,7 @@ __global__ void __launch_bounds__(kThreads) k_ovl_build_x(OverlapArgs a, FFTPlan
   const int nzb = 2 * a.zdc + 1;
   const int row0 = blockIdx.x * rows_per_cta;
   const int nrows = min(rows_per_cta, nzb * ny - row0);
+  const float2 ks = ovl_shift(a);
   for (int t = threadIdx.x; t < 2 * rows_per_cta * nx; t += blockDim.x) {
     int l = t / nx, j = t - l * nx;
     int r = l >> 1, ov = l & 1;
@@ -124,7 +134,7 @@ __global__ void __launch_bounds__(kThreads) k_ovl_build_x(OverlapArgs a, FFTPlan
     if (r < nrows) {
       int row = row0 + r;
       int zb = row / ny, i = row - zb * ny;
-      val = ovl_value(a, ov, zb, i, j, otf_kz(a.otf, zb - a.zdc), 1.f / a.otf.dkrotf);
+      val = ovl_value(a, ks, ov, zb, i, j, otf_kz(a.otf, zb - a.zdc), 1.f / a.otf.dkrotf);
     }
     sm[l * ldl + j] = val;
   }
@@ -166,6 +176,7 @@ __global__ void __launch_bounds__(kOvlWarps * 32, 5) k_ovl_build_xw(OverlapArgs 
   // build the warp's G lines (all 32 lanes, consecutive j); the kz part of
   // the OTF lookups is the same along a line
   const float rdk = 1.f / a.otf.dkrotf;
+  const float2 ks = ovl_shift(a);
 #pragma unroll
   for (int gl = 0; gl < G; ++gl) {
     const int L = l0 + gl;
@@ -176,7 +187,7 @@ __global__ void __launch_bounds__(kOvlWarps * 32, 5) k_ovl_build_xw(OverlapArgs 
     const int row = L >> 1, ov = L & 1;
     const int zb = row / ny, i = row - zb * ny;
     const OtfKz kzi = otf_kz(a.otf, zb - a.zdc);
-    for (int j = lane; j < N; j += 32) lines[warp][gl][j] = ovl_value(a, ov, zb, i, j, kzi, rdk);
+    for (int j = lane; j < N; j += 32) lines[warp][gl][j] = ovl_value(a, ks, ov, zb, i, j, kzi, rdk);
   }
   __syncwarp();
   float2 v[E];
@@ -507,15 +518,19 @@ constexpr int kCand = 8;  // candidates per pass (register accumulators)
 static_assert(2 * kCand == 16, "k_modamp_partial reduces 16 values per thread");
 
 // ex[c][x] = exp(i 2 pi (x - nx/2) kx_c dxy), ey[c][y] likewise
+// kdev: one candidate, kdev[0] * kfac (a k0 fitted on the device)
 __global__ void k_phase_tables(const __grid_constant__ CandList kc, int ncand, int nx, int ny, float dxy, float2* ex,
-                               float2* ey)
+                               float2* ey, const float2* kdev, float kfac)
 {
   int n = ncand * (nx + ny);
+  float2 kd = make_float2(0.f, 0.f);
+  if (kdev) kd = make_float2(__fmul_rn(kdev->x, kfac), __fmul_rn(kdev->y, kfac));
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     int c = t / (nx + ny), r = t - c * (nx + ny);
+    const float2 k = kdev ? kd : kc.k[c];
     double ang;
-    if (r < nx) ang = 2.0 * M_PI * ((double)r - 0.5 * nx) * (double)kc.k[c].x * (double)dxy;
-    else ang = 2.0 * M_PI * ((double)(r - nx) - 0.5 * ny) * (double)kc.k[c].y * (double)dxy;
+    if (r < nx) ang = 2.0 * M_PI * ((double)r - 0.5 * nx) * (double)k.x * (double)dxy;
+    else ang = 2.0 * M_PI * ((double)(r - nx) - 0.5 * ny) * (double)k.y * (double)dxy;
     double s, co;
     sincos(ang, &s, &co);
     float2 v = make_float2((float)co, (float)s);
@@ -827,8 +842,9 @@ int launch_copy_out(const void* src1, void* dst1, size_t n1, const void* src2, v
   return (int)cudaGetLastError();
 }
 
-int launch_modamp_candidates(const float2* pmap, int nx, int ny, float dxy, const CandList& kcand, int ncand,
-                             float2* tables, double* partial, double* xstary, cudaStream_t s, long long* launches)
+static int modamp_impl(const float2* pmap, int nx, int ny, float dxy, const CandList& kcand, int ncand,
+                       const float2* kdev, float kfac, float2* tables, double* partial, double* xstary, cudaStream_t s,
+                       long long* launches)
 {
   if (ncand < 1 || ncand > kMaxCand) return -1;
   float2* ex = tables;
@@ -836,7 +852,7 @@ int launch_modamp_candidates(const float2* pmap, int nx, int ny, float dxy, cons
   KernelTimer* kt = kernel_timer();
   if (kt) kt->begin(s);
   // double sincos: spread over all SMs (FP64 throughput is per SM)
-  k_phase_tables<<<(ncand * (nx + ny) + 63) / 64, 64, 0, s>>>(kcand, ncand, nx, ny, dxy, ex, ey);
+  k_phase_tables<<<(ncand * (nx + ny) + 63) / 64, 64, 0, s>>>(kcand, ncand, nx, ny, dxy, ex, ey, kdev, kfac);
   if (kt) kt->end("k_modamp_tables", s, (double)ncand * (nx + ny) * sizeof(float2));
   // about four elements per thread, at most kModampBlocks blocks
   const int nb = (int)std::min<long long>(kModampBlocks, std::max<long long>(1, ((long long)nx * ny + 1023) / 1024));
@@ -852,6 +868,19 @@ int launch_modamp_candidates(const float2* pmap, int nx, int ny, float dxy, cons
   if (kt) kt->end("k_modamp_final", s, (double)nb * ncand * 2 * sizeof(double));
   if (launches) *launches += 2;
   return (int)cudaGetLastError();
+}
+
+int launch_modamp_candidates(const float2* pmap, int nx, int ny, float dxy, const CandList& kcand, int ncand,
+                             float2* tables, double* partial, double* xstary, cudaStream_t s, long long* launches)
+{
+  return modamp_impl(pmap, nx, ny, dxy, kcand, ncand, nullptr, 0.f, tables, partial, xstary, s, launches);
+}
+
+int launch_modamp_device_k(const float2* pmap, int nx, int ny, float dxy, const float2* kdev, float kfac,
+                           float2* tables, double* partial, double* xstary, cudaStream_t s, long long* launches)
+{
+  if (kdev == nullptr) return -1;
+  return modamp_impl(pmap, nx, ny, dxy, CandList{}, 1, kdev, kfac, tables, partial, xstary, s, launches);
 }
 
 }  // namespace simrecon

@@ -110,6 +110,8 @@ struct OverlapArgs {
   int nx, ny, nz;
   int order1, order2;
   float kx, ky;         // k0 * (order2 - order1), 1/um
+  const float2* kdev;   // if set: k0 from device memory, times kfac (kx, ky unused)
+  float kfac;
   float dkx, dky;
   float rdistcutoff, otfcutoff, order0_2_factor;
   // exact squared forms of makeoverlaps' float decisions (set by
@@ -157,6 +159,34 @@ struct CandList {
 // XStarY[c] = sum_xy pmap(x,y) exp(i 2pi ((x - nx/2) kx_c + (y - ny/2) ky_c) dxy), c < ncand
 int launch_modamp_candidates(const float2* pmap, int nx, int ny, float dxy, const CandList& kcand, int ncand,
                              float2* tables, double* partial, double* xstary, cudaStream_t s, long long* launches);
+// one candidate read from device memory: kdev[0] * kfac
+int launch_modamp_device_k(const float2* pmap, int nx, int ny, float dxy, const float2* kdev, float kfac,
+                           float2* tables, double* partial, double* xstary, cudaStream_t s, long long* launches);
+
+// The pattern-vector search on the device (k_search.cu).
+// Upper bound on each line search's climb (the reference's loops have none):
+// 4096 steps is 4 rad of angle or 400 frequency pixels of magnitude.
+constexpr int kMaxClimbSteps = 4096;
+// findk0's peak refinement: peak = {ix, iy, a1x, a2, a3x, a1y, a3y} ->
+// k0out; k1out = k0 through (|k0|, atan2) and back (where the search's first
+// amplitude evaluation rebuilds the overlaps)
+int launch_findk0_finish(const float* peak, float2 guess, int nx, int ny, float dkx, float dky, int fitorder2,
+                         float2* k0out, float2* k1out, cudaStream_t s, long long* launches);
+struct K0SearchArgs {
+  const float2* pmap;    // [ny][nx] overlap map of orders (0, fitorder2), built at k1
+  const double* sumxy;   // [2] sum |X|^2, sum |Y|^2 of that build
+  const float2* k0find;  // findk0's k0 (the lines start at its angle and magnitude)
+  float2* k0fit;         // out: the fitted k0
+  double* slot;          // out: XStarY re, im, sum |X|^2, sum |Y|^2 at the fitted k0
+  int* info;             // [0] += candidates evaluated; [1] |= 1 line cache exceeded, 2 batch limit
+  int nx, ny, fitorder2;
+  float dxy, delta_angle, delta_mag;
+};
+// whether the search's phase tables fit a CTA's shared memory at this size
+bool k0_search_supported(int nx, int ny);
+// one thread-block cluster (8 CTAs): both line searches, their parabola fits
+// and the amplitude at the fitted k0 (fitk0andmodamps, gpuFunctionsImpl.cu:874-1020)
+int launch_k0_search(const K0SearchArgs& a, cudaStream_t s, long long* launches);
 
 // Modulation amplitudes of the last fit and the Wiener-filter weights derived
 // from them, in device memory: the filter reads them there, so a volume whose

@@ -504,6 +504,8 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
       {(void**)&d_xstary_, (size_t)kMaxCand * 2 * sizeof(double)},
       {(void**)&d_fit_, sizeof(FitDev)},
       {(void**)&d_fitslots_, (size_t)kMaxDirs * kMaxOrders * 4 * sizeof(double)},
+      {(void**)&d_kst_, (size_t)kMaxDirs * 3 * sizeof(float2)},
+      {(void**)&d_sinfo_, 2 * sizeof(int)},
       {(void**)&d_asmtab_, asm_table_bytes()},
       {(void**)&d_ex_, (size_t)ndirs_ * norders_ * X_ * sizeof(float2)},
       {(void**)&d_ey_, (size_t)ndirs_ * norders_ * Y_ * sizeof(float2)},
@@ -785,7 +787,7 @@ void SIM_Reconstructor::separate()
 }
 
 // ------------------------------------------------------------------ fitting
-void SIM_Reconstructor::build_overlaps(int d, int o1, int o2, float k0x, float k0y)
+void SIM_Reconstructor::build_overlaps(int d, int o1, int o2, float k0x, float k0y, const float2* kdev, float kfac)
 {
   const ReconParams& p = opt.p;
   const ImageParams& ip = opt.ip;
@@ -811,6 +813,8 @@ void SIM_Reconstructor::build_overlaps(int d, int o1, int o2, float k0x, float k
   if (rdistcutoff > 1. / (2. * dxy)) rdistcutoff = 1. / (2. * dxy);
   a.kx = k0x * (o2 - o1);
   a.ky = k0y * (o2 - o1);
+  a.kdev = kdev;  // a k0 fitted on the device (not in Bessel mode, whose zdc depends on |k0|)
+  a.kfac = kfac;
   a.dkx = dkx;
   a.dky = dky;
   a.rdistcutoff = rdistcutoff;
@@ -983,10 +987,8 @@ void SIM_Reconstructor::fitk0andmodamps(int d)
   float deltaangle = 0.001;
   float deltamag = 0.1 / (std::max(nx_, ny_) * opt.ip.dxy);
   const int K = 12;
-  // Upper bound on each climb (the reference's loops have none): 4096 steps
-  // is 4 rad of angle or 400 frequency pixels of magnitude, far past any
-  // physical maximum, so it only ends a climb whose amplitude never peaks.
-  constexpr int kMaxClimbSteps = 4096;
+  // each climb stops after kMaxClimbSteps (the reference's loops have no
+  // bound; it only ends a climb whose amplitude never peaks)
   // both directions of the angle search in one batch
   prefetch_line(fitorder1, fitorder2, true, k0mag, k0angle, deltaangle, K, +1);
   prefetch_line(fitorder1, fitorder2, true, k0mag, k0angle, deltaangle, K, -1);
@@ -1156,11 +1158,107 @@ void SIM_Reconstructor::fit_all()
   stage_begin("fit", &a, &l0);
   if (fit_without_search()) {
     fit_on_device();
-  } else {
+  } else if (!device_search_possible() || !fit_search_on_device()) {
     for (int d = 0; d < ndirs_; ++d) fit_direction(d);
     check_launch(upload_amps(), "fit results");
   }
   stage_end("fit", a, l0);
+}
+
+// The k0 search runs on the device unless a host decision is part of it:
+// Bessel mode (the overlaps' kz range depends on |k0|), a later time point
+// that may fall back to time 0's k0, the overlap debug dump after findk0.
+bool SIM_Reconstructor::device_search_possible() const
+{
+  const ReconParams& p = opt.p;
+  const ImageParams& ip = opt.ip;
+  if (!device_search_ || p.bBessel || debug_requested()) return false;
+  if (ip.ntimes > 1 && ip.curTimeIdx > 0) return false;
+  return k0_search_supported(nx_, ny_);
+}
+
+// findModulationVectorsAndPhasesForAllDirections with a k0 search
+// (cudaSirecon.cpp:296-408, 450-492) on the device: per direction findk0
+// (overlaps at the guess, cross-correlation peak, parabola refinement), the
+// overlaps rebuilt at the refined k0, the cluster search of fitk0andmodamps,
+// then the other orders' amplitudes at the fitted k0; the amplitudes are
+// finished like the no-search branch's.  One synchronisation at the end
+// brings the fitted k0 to the host (the filter's set-up needs it).  Returns
+// false, having changed nothing the host search depends on, when a climb
+// left the device's line cache; the host search then runs instead.
+bool SIM_Reconstructor::fit_search_on_device()
+{
+  ReconParams& p = opt.p;
+  const ImageParams& ip = opt.ip;
+  const int fo2 = nz_ > 1 ? 2 : 1;
+  const float dxy = ip.dxy;
+  const float dkx = 1 / (nx_ * dxy), dky = 1 / (ny_ * dxy);
+  check(cudaMemsetAsync(d_sinfo_, 0, 2 * sizeof(int), stream_), "fit");
+  long long builds = 0, reductions = 0;
+  for (int d = 0; d < ndirs_; ++d) {
+    k0_[d] = k0guess_[d];
+    float2* kfind = d_kst_ + 3 * d;
+    float2* k1 = kfind + 1;
+    float2* kfit = kfind + 2;
+    build_overlaps(d, 0, fo2, k0guess_[d].x, k0guess_[d].y);
+    check_launch(launch_crosscorr_peak(d_pmap_, d_cc_, nx_, ny_, d_bval_, d_bidx_, d_peak_, stream_, &launches_),
+                 "crosscorr");
+    check_launch(launch_findk0_finish(d_peak_, make_float2(k0guess_[d].x, k0guess_[d].y), nx_, ny_, dkx, dky, fo2,
+                                      kfind, k1, stream_, &launches_),
+                 "findk0");
+    // fitk0andmodamps' first getmodamp rebuilds the overlaps at k1
+    build_overlaps(d, 0, fo2, 0.f, 0.f, k1, (float)fo2);
+    K0SearchArgs sa{};
+    sa.pmap = d_pmap_;
+    sa.sumxy = d_sumxy_;
+    sa.k0find = kfind;
+    sa.k0fit = kfit;
+    sa.slot = d_fitslots_ + (size_t)(d * norders_ + fo2) * 4;
+    sa.info = d_sinfo_;
+    sa.nx = nx_;
+    sa.ny = ny_;
+    sa.fitorder2 = fo2;
+    sa.dxy = dxy;
+    sa.delta_angle = 0.001f;
+    sa.delta_mag = 0.1 / (std::max(nx_, ny_) * dxy);
+    check_launch(launch_k0_search(sa, stream_, &launches_), "k0 search");
+    builds += 2;
+    reductions += 1;  // the cross-correlation
+    // the other orders at the fitted k0 (overlaps rebuilt each time)
+    for (int order = 1; order < norders_; ++order) {
+      const int o1 = nz_ == 1 ? order - 1 : 0;
+      if (nz_ == 1 ? order < 2 : order == fo2) continue;
+      build_overlaps(d, o1, order, 0.f, 0.f, kfit, (float)(order - o1));
+      check_launch(launch_modamp_device_k(d_pmap_, nx_, ny_, dxy, kfit, (float)(order - o1), d_tables_, d_partial_,
+                                          d_xstary_, stream_, &launches_),
+                   "modamp");
+      double* slot = d_fitslots_ + (size_t)(d * norders_ + order) * 4;
+      check_launch(launch_copy_out(d_xstary_, slot, 4, d_sumxy_, slot + 2, 4, stream_, &launches_), "modamp");
+      ++builds;
+      ++reductions;
+    }
+  }
+  check_launch(launch_fit_finish(d_fitslots_, fit_finish_args(), d_fit_, stream_, &launches_), "fit results");
+  // the fitted k0s and the search's counters through mapped host memory
+  double* base = dh_pinned_ + 320;
+  check_launch(launch_copy_out(d_kst_, base, (size_t)ndirs_ * 6, d_sinfo_, base + 32, 2, stream_, &launches_),
+               "fit results");
+  check(cudaStreamSynchronize(stream_), "k0 search");
+  const float* kst = (const float*)(h_pinned_ + 320);
+  const int* info = (const int*)(h_pinned_ + 352);
+  fit_counts_[0] += builds;
+  fit_counts_[1] += reductions + info[0];
+  fit_counts_[2] += ndirs_;
+  cur_o1_ = cur_o2_ = -1;
+  cache_.clear();
+  if (info[1] != 0) return false;  // a climb left the line cache: the host search runs
+  for (int d = 0; d < ndirs_; ++d) {
+    k0_[d] = float2v{kst[6 * d + 4], kst[6 * d + 5]};
+    if (ip.curTimeIdx == 0) k0_time0_[d] = k0_[d];
+  }
+  p.recalcarrays = 1;  // fit_direction's setting, kept for callers that read it
+  amps_on_device_only_ = true;
+  return true;
 }
 
 FitFinishArgs SIM_Reconstructor::fit_finish_args() const

@@ -66,6 +66,9 @@ class SIM_Reconstructor {
   // Wiener filter inside the assembly's band load where supported (default),
   // or always as its own pass; both give the same volume within float rounding
   void set_filter_fusion(bool on) { filter_fusion_ = on; }
+  // k0 search on the device (default) or host-driven with batched candidate
+  // evaluations; both visit the same float32 angles and magnitudes
+  void set_device_search(bool on) { device_search_ = on; }
   // time both FFT paths at every site and length this handle's volume uses
   // (best of `reps`), record the faster in the plan cache; returns JSON
   std::string tune_fft(int reps);
@@ -100,6 +103,8 @@ class SIM_Reconstructor {
   void fit_direction(int d);
   bool fit_without_search() const;
   void fit_on_device();
+  bool device_search_possible() const;
+  bool fit_search_on_device();
   simrecon::FitFinishArgs fit_finish_args() const;
   int upload_amps();
   void sync_amps() const;
@@ -122,7 +127,7 @@ class SIM_Reconstructor {
   void check_launch(int rc, const char* what);
 
   // fitting helpers (gpuFunctionsImpl.cu:306-1148 semantics)
-  void build_overlaps(int d, int o1, int o2, float k0x, float k0y);
+  void build_overlaps(int d, int o1, int o2, float k0x, float k0y, const float2* kdev = nullptr, float kfac = 0.f);
   int overlap_zdc_bessel(int order2, float k0x, float k0y) const;
   // evaluate XStarY for candidate (angle, mag) pairs on the current overlaps
   void eval_candidates(int o1, int o2, const std::vector<std::pair<float, float>>& cands);
@@ -149,6 +154,7 @@ class SIM_Reconstructor {
   cudaStream_t stream_ = nullptr;
   int device_ = 0;
   bool filter_fusion_ = true;
+  bool device_search_ = true;
   bool dry_run_ = false;      // setup computes planned_bytes_ and allocates nothing
   size_t planned_bytes_ = 0;
 
@@ -178,6 +184,8 @@ class SIM_Reconstructor {
   double* d_xstary_ = nullptr;
   simrecon::FitDev* d_fit_ = nullptr;  // amplitudes + filter weights of the last fit
   double* d_fitslots_ = nullptr;       // [ndirs * norders][4]: XStarY re, im, sum |X|^2 per order
+  float2* d_kst_ = nullptr;            // device search, per direction: findk0's k0, k1, the fitted k0
+  int* d_sinfo_ = nullptr;             // device search: candidates evaluated, status
   void* d_asmtab_ = nullptr;           // assembly slot tables
   bool asm_tables_valid_ = false;
   int asm_tables_zdc_[simrecon::kMaxOrders] = {0};

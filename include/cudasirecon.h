@@ -241,6 +241,17 @@ int SRX_lastProcessResult(SIM_Reconstructor* sr);
  * (SRX_getBand) are unspecified. */
 void SRX_setFilterFusion(SIM_Reconstructor* sr, int on);
 
+/* k0 search placement (default on): on the device -- findk0's peak
+ * refinement and fitk0andmodamps' angle and magnitude line searches run as
+ * kernels (one thread-block cluster per direction), with one host
+ * synchronisation per volume instead of one per candidate batch -- or, with
+ * on = 0, driven from the host.  Both visit the same float32 angles and
+ * magnitudes (cudaSirecon.cpp:296-408, gpuFunctionsImpl.cu:306-372,
+ * 874-1044); the fitted k0 agree within float rounding of the start angle.
+ * Bessel mode, the overlap debug dump and later time points of a series
+ * (which may fall back to time 0's k0) use the host-driven search. */
+void SRX_setDeviceK0Search(SIM_Reconstructor* sr, int on);
+
 /* Number of this library's kernels launched since the handle was created. */
 long long SRX_kernelLaunches(SIM_Reconstructor* sr);
 

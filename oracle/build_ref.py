@@ -90,7 +90,7 @@ def build(force: bool = False, verbose: bool = False) -> str | None:
     flags = [
         "-std=c++17", "-O3", "-DNDEBUG", "-Dcimg_display=0", "-Dcimg_use_openmp=0",
         "-gencode", "arch=compute_103a,code=sm_103a",
-        "-Xcompiler", "-fPIC", "-w",
+        "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp", "-w",
         "-I", os.path.join(OUT, "shim"),
         "-I", os.path.join(STAGE, "src/cudaSirecon"),
         "-I", os.path.join(STAGE, "src/Buffers"),
@@ -112,7 +112,7 @@ def build(force: bool = False, verbose: bool = False) -> str | None:
             sys.stderr.write(out.decode(errors="replace"))
     if not ok:
         return None
-    link = [nvcc, "-shared", "-o", LIB] + objs + ["-lcufft", "-gencode", "arch=compute_103a,code=sm_103a",
+    link = [nvcc, "-shared", "-o", LIB] + objs + ["-lcufft", "-lgomp", "-gencode", "arch=compute_103a,code=sm_103a",
                                                    "-Xlinker", "--no-undefined"]
     r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode != 0:

@@ -388,7 +388,9 @@ void setup(Harness* h, int nx, int ny, int nImages, const float* otf, int otf_w,
 
 // loadImageData (cudaSirecon.cpp:1354-1435) with load_and_flatfield
 // (1715-1731) and deskewOneSection (1733-1760): one synchronous
-// host->device copy per plane, like the reference.  The per-section extra
+// host->device copy per plane, like the reference, which builds with OpenMP
+// (src/CMakeLists.txt:55-64) and runs deskewOneSection's column loop on every
+// host thread.  The per-section extra
 // background of the bBgInExtHdr branch (1386-1393) comes from
 // refh_set_section_backgrounds (the reference reads the MRC extended header).
 void load_image_data(Harness* h)
@@ -415,6 +417,8 @@ void load_image_data(Harness* h)
           for (int k = 0; k < nx_raw; k++)
             section[l * nx_raw + k] =
                 (buffer[l * nx_raw + k] - bg[l * nx_raw + k] - d.backgroundExtra) * sl[l * nx_raw + k] * ip.inscale;
+        // the reference's loop is an OpenMP parallel for over xout
+#pragma omp parallel for
         for (int xout = 0; xout < xdim; xout++) {
           float xin = xout;
           if (fabs(deskewFactor) > 0)
