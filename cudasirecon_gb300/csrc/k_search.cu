@@ -4,7 +4,8 @@
 //
 // k_findk0_finish   the cross-correlation peak's parabola fits and the
 //                   wrap-around choice -> k0 (one thread)
-// k_k0_search       one thread-block cluster per direction: the angle and
+// k_k0_search       one thread-block cluster per direction (all directions in
+//                   one launch, side by side on the GPU): the angle and
 //                   magnitude line searches with their parabola fits and the
 //                   final modulation amplitude.  The cluster's eight CTAs
 //                   evaluate batches of candidate k0s over the overlap map P
@@ -101,9 +102,12 @@ struct SearchLine {
 
 struct __align__(16) SearchCtl {
   int nbatch;                // candidates of the current batch; 0: finished
-  int pad[3];
-  float2 kc[kSB];            // candidate vectors, k1 * fitorder2
-  int j[kSB];                // line step of each candidate
+  int vary_angle;            // 1: pos[] are angles at magnitude `fixed`; 0: magnitudes at angle `fixed`
+  float fixed;
+  int pad;
+  float pos[kSB];            // the batch's positions along its line
+  int j[kSB];                // their line steps
+  float2 kc[kSB];            // candidate vectors k1 * fitorder2
   double red[kSC][kSB][2];   // every CTA's partial XStarY (leader only)
   double res[kSB][2];        // the batch's XStarY (leader only)
 };
@@ -176,14 +180,7 @@ struct Controller {
   float afit, mfit;    // fitted angle, magnitude
   float x1, amp1;      // carried between the lines
   float sx;            // sum |X|^2 as float
-  float fac;           // fitorder2 - fitorder1
 };
-
-__device__ float2 line_vector(const Controller& c, float pos)
-{
-  const float2 k1 = c.phase == kPhaseAngle ? polar_rn(c.k0mag, pos) : polar_rn(pos, c.afit);
-  return make_float2(__fmul_rn(k1.x, c.fac), __fmul_rn(k1.y, c.fac));
-}
 
 // position of step j from its neighbour towards the start (float-accumulated
 // like the reference's angle += deltaangle)
@@ -194,16 +191,18 @@ __device__ void set_pos(SearchLine& L, int j, float base, float delta)
   else L.pos[j + kSL] = __fsub_rn(L.pos[j + 1 + kSL], delta);
 }
 
-// queue steps j, j+s, ... (or the start batch) of the current line
-__device__ void request_line(Controller& c, SearchLine& L, SearchCtl& ctl, int j)
+// queue steps j, j+s, ... (or the start batch) of the current line; the
+// candidate vectors are formed by the leader's threads in parallel
+__device__ void request_line(const Controller& c, SearchLine& L, SearchCtl& ctl, int j)
 {
-  const float base = c.phase == kPhaseAngle ? c.k0angle : c.k0mag;
-  const float delta = c.phase == kPhaseAngle ? c.delta_angle : c.delta_mag;
+  const bool ang = c.phase == kPhaseAngle;
+  const float base = ang ? c.k0angle : c.k0mag;
+  const float delta = ang ? c.delta_angle : c.delta_mag;
   int n = 0;
   auto add = [&](int jj) {
     if (jj < -kSL || jj > kSL || L.have[jj + kSL]) return;
     set_pos(L, jj, base, delta);
-    ctl.kc[n] = line_vector(c, L.pos[jj + kSL]);
+    ctl.pos[n] = L.pos[jj + kSL];
     ctl.j[n] = jj;
     ++n;
   };
@@ -215,66 +214,65 @@ __device__ void request_line(Controller& c, SearchLine& L, SearchCtl& ctl, int j
     const int s = j > 0 ? 1 : -1;
     for (int i = 0; i < kSLineK; ++i) add(j + s * i);
   }
+  ctl.vary_angle = ang;
+  ctl.fixed = ang ? c.k0mag : c.afit;
   ctl.nbatch = n;
 }
 
-__device__ void reset_line(SearchLine& L)
-{
-  for (int i = 0; i < 2 * kSL + 1; ++i) L.have[i] = 0;
-}
-
 // Consume the finished batch, advance the search, queue the next batch (or
-// none).  Runs on one thread.
-__device__ void control(Controller& c, SearchLine& L, SearchCtl& ctl, const K0SearchArgs& a)
+// none).  Runs on one thread; lines[0] is the angle line, lines[1] the
+// magnitude line.
+__device__ void control(Controller& c, SearchLine* lines, SearchCtl& ctl, const K0SearchArgs& a, int dir)
 {
   const int nb = ctl.nbatch;
   if (c.phase == kPhaseFinal && nb > 0) {
     // getmodamp at the fitted (angle, magnitude): the amplitude of fitorder2
-    a.slot[0] = ctl.res[0][0];
-    a.slot[1] = ctl.res[0][1];
-    a.slot[2] = a.sumxy[0];
-    a.slot[3] = a.sumxy[1];
-    *a.k0fit = polar_rn(c.mfit, c.afit);
+    double* slot = a.slot[dir];
+    slot[0] = ctl.res[0][0];
+    slot[1] = ctl.res[0][1];
+    slot[2] = a.sumxy[dir][0];
+    slot[3] = a.sumxy[dir][1];
+    *a.k0fit[dir] = polar_rn(c.mfit, c.afit);
     c.phase = kPhaseDone;
     ctl.nbatch = 0;
     return;
   }
-  for (int i = 0; i < nb; ++i) {
-    const float mx = __fdiv_rn(__double2float_rn(ctl.res[i][0]), c.sx);
-    const float my = __fdiv_rn(__double2float_rn(ctl.res[i][1]), c.sx);
-    L.val[ctl.j[i] + kSL] = __fadd_rn(__fmul_rn(mx, mx), __fmul_rn(my, my));
-    L.have[ctl.j[i] + kSL] = 1;
+  if (nb > 0) {
+    SearchLine& L = lines[c.phase == kPhaseAngle ? 0 : 1];
+    for (int i = 0; i < nb; ++i) {
+      const float mx = __fdiv_rn(__double2float_rn(ctl.res[i][0]), c.sx);
+      const float my = __fdiv_rn(__double2float_rn(ctl.res[i][1]), c.sx);
+      L.val[ctl.j[i] + kSL] = __fadd_rn(__fmul_rn(mx, mx), __fmul_rn(my, my));
+      L.have[ctl.j[i] + kSL] = 1;
+    }
   }
   ctl.nbatch = 0;
-  for (;;) {
-    if (c.phase == kPhaseAngle || c.phase == kPhaseMag) {
-      const ClimbResult r = run_climb(L, c.x1, c.amp1);
-      if (r.need) {
-        if (r.j < -kSL || r.j > kSL) {  // beyond the line cache: the host search takes over
-          c.status = 1;
-          c.phase = kPhaseDone;
-          return;
-        }
-        request_line(c, L, ctl, r.j);
+  while (c.phase == kPhaseAngle || c.phase == kPhaseMag) {
+    SearchLine& L = lines[c.phase == kPhaseAngle ? 0 : 1];
+    const ClimbResult r = run_climb(L, c.x1, c.amp1);
+    if (r.need) {
+      if (r.j < -kSL || r.j > kSL) {  // beyond the line cache: the host search takes over
+        c.status = 1;
+        c.phase = kPhaseDone;
         return;
       }
-      c.x1 = r.x1;
-      c.amp1 = r.amp1;
-      if (c.phase == kPhaseAngle) {
-        c.afit = r.fit;
-        c.phase = kPhaseMag;
-        reset_line(L);
-        continue;
-      }
-      c.mfit = r.fit;
-      c.phase = kPhaseFinal;
-      const float2 k1 = polar_rn(c.mfit, c.afit);
-      ctl.kc[0] = make_float2(__fmul_rn(k1.x, c.fac), __fmul_rn(k1.y, c.fac));
-      ctl.j[0] = 0;
-      ctl.nbatch = 1;
+      request_line(c, L, ctl, r.j);
       return;
     }
-    return;
+    c.x1 = r.x1;
+    c.amp1 = r.amp1;
+    if (c.phase == kPhaseAngle) {
+      c.afit = r.fit;
+      c.phase = kPhaseMag;
+      continue;
+    }
+    c.mfit = r.fit;
+    c.phase = kPhaseFinal;
+    ctl.pos[0] = c.mfit;
+    ctl.j[0] = 0;
+    ctl.vary_angle = 0;
+    ctl.fixed = c.afit;
+    ctl.nbatch = 1;
   }
 }
 
@@ -294,50 +292,135 @@ __device__ __forceinline__ float2 phase_factor(int x, int n, float hi, float lo)
   return make_float2(c, s);
 }
 
+// XStarY partial sums of CC candidates over this CTA's tile: per row the x
+// sum with the x phase factors, times the row's y factor; two rows per pass
+// share the x factors.  acc: per-thread sums.
+template <int CC>
+__device__ __forceinline__ void tile_sums(const float2* __restrict__ pmap, int nx, const float2* ex, const float2* ey,
+                                          int tw, int th, int x0, int y0, int warp, int lane, float2 (&acc)[CC])
+{
+#pragma unroll
+  for (int k = 0; k < CC; ++k) acc[k] = make_float2(0.f, 0.f);
+  const int y1 = y0 + th, x1 = x0 + tw;
+  for (int y = y0 + 2 * warp; y < y1; y += 2 * kSW) {
+    const bool two = y + 1 < y1;
+    float2 r0[CC], r1[CC];
+#pragma unroll
+    for (int k = 0; k < CC; ++k) r0[k] = r1[k] = make_float2(0.f, 0.f);
+    for (int x = x0 + lane; x < x1; x += 32) {
+      const float2 p0 = __ldg(pmap + (size_t)y * nx + x);
+      const float2 p1 = two ? __ldg(pmap + (size_t)(y + 1) * nx + x) : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int k = 0; k < CC; ++k) {
+        const float2 e = ex[k * tw + (x - x0)];
+        r0[k].x = fmaf(p0.x, e.x, fmaf(-p0.y, e.y, r0[k].x));
+        r0[k].y = fmaf(p0.x, e.y, fmaf(p0.y, e.x, r0[k].y));
+        r1[k].x = fmaf(p1.x, e.x, fmaf(-p1.y, e.y, r1[k].x));
+        r1[k].y = fmaf(p1.x, e.y, fmaf(p1.y, e.x, r1[k].y));
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < CC; ++k) {
+      const float2 e0 = ey[k * th + (y - y0)];
+      acc[k].x += r0[k].x * e0.x - r0[k].y * e0.y;
+      acc[k].y += r0[k].x * e0.y + r0[k].y * e0.x;
+      if (two) {
+        const float2 e1 = ey[k * th + (y + 1 - y0)];
+        acc[k].x += r1[k].x * e1.x - r1[k].y * e1.y;
+        acc[k].y += r1[k].x * e1.y + r1[k].y * e1.x;
+      }
+    }
+  }
+}
+
+// the CTA's sums of CC candidates in double (warps by shuffles, then the
+// warps in order) into the leader's partial-sum table at candidate c0
+template <int CC>
+__device__ __forceinline__ void tile_reduce(const float2 (&acc)[CC], double (*wsum)[2 * 16], SearchCtl* lead,
+                                            int rank, int c0, int tid, int warp, int lane)
+{
+#pragma unroll
+  for (int k = 0; k < CC; ++k) {
+    double sr = acc[k].x, si = acc[k].y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      sr += __shfl_xor_sync(0xffffffffu, sr, o);
+      si += __shfl_xor_sync(0xffffffffu, si, o);
+    }
+    if (lane == 0) {
+      wsum[warp][2 * k] = sr;
+      wsum[warp][2 * k + 1] = si;
+    }
+  }
+  __syncthreads();
+  if (tid < 2 * CC) {
+    double s = 0.0;
+    for (int w = 0; w < kSW; ++w) s += wsum[w][tid];
+    lead->red[rank][c0 + (tid >> 1)][tid & 1] = s;
+  }
+}
+
+template <int CC>
+__device__ void chunk(const float2* __restrict__ pmap, int nx, const float2* ex, const float2* ey, int tw, int th,
+                      int x0, int y0, double (*wsum)[2 * 16], SearchCtl* lead, int rank, int c0)
+{
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  float2 acc[CC];
+  tile_sums<CC>(pmap, nx, ex, ey, tw, th, x0, y0, warp, lane, acc);
+  tile_reduce<CC>(acc, wsum, lead, rank, c0, tid, warp, lane);
+}
+
+// C: the most candidates one pass holds (phase tables in shared memory)
 template <int C>
 __global__ void __cluster_dims__(kSC, 1, 1) __launch_bounds__(kST, 1) k_k0_search(const __grid_constant__ K0SearchArgs a)
 {
   cg::cluster_group cluster = cg::this_cluster();
   const unsigned rank = cluster.block_rank();
+  const int dir = blockIdx.x / kSC;  // one cluster per direction
+  const float2* __restrict__ pmap = a.pmap[dir];
   __shared__ SearchCtl ctl;
-  __shared__ SearchLine line;
-  __shared__ double wsum[kSW][2 * C];
+  __shared__ SearchLine lines[2];
+  __shared__ double wsum[kSW][2 * 16];
   __shared__ float2 kloc[kSB];
   __shared__ int nloc;
   extern __shared__ float2 tab[];
   SearchCtl* lead = cluster.map_shared_rank(&ctl, 0);
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x;
   const int nx = a.nx, ny = a.ny;
   // tile of P: 2 column halves x 4 row quarters
   const int tx = rank & 1, ty = rank >> 1;
   const int x0 = tx * nx / 2, x1 = (tx + 1) * nx / 2;
   const int y0 = ty * ny / 4, y1 = (ty + 1) * ny / 4;
   const int tw = x1 - x0, th = y1 - y0;
-  float2* ex = tab;                  // [C][tw]
-  float2* ey = tab + (size_t)C * tw; // [C][th]
 
   Controller c{};
   if (rank == 0) {
-    for (int i = tid; i < 2 * kSL + 1; i += kST) line.have[i] = 0;
+    for (int i = tid; i < 2 * kSL + 1; i += kST) lines[0].have[i] = lines[1].have[i] = 0;
     if (tid == 0) {
-      const float2 k0 = *a.k0find;
+      const float2 k0 = *a.k0find[dir];
       c.phase = kPhaseAngle;
       c.k0mag = __fsqrt_rn(__fadd_rn(__fmul_rn(k0.x, k0.x), __fmul_rn(k0.y, k0.y)));
       c.k0angle = atan2f(k0.y, k0.x);
       c.delta_angle = a.delta_angle;
       c.delta_mag = a.delta_mag;
-      c.sx = __double2float_rn(a.sumxy[0]);
-      c.fac = (float)a.fitorder2;
+      c.sx = __double2float_rn(a.sumxy[dir][0]);
       ctl.nbatch = 0;
     }
   }
+  const float fac = (float)a.fitorder2;
   int it = 0;
   for (; it < kSMaxBatches; ++it) {
     if (rank == 0) {
-      __syncthreads();  // the previous batch's sums are in ctl.res
+      __syncthreads();  // the previous batch's sums are in ctl.res; the line caches are clear
       if (tid == 0) {
-        control(c, line, ctl, a);
+        control(c, lines, ctl, a, dir);
         c.ncand += ctl.nbatch;
+      }
+      __syncthreads();
+      // the candidate vectors (getmodamp: k1 = mag (cosf, sinf)(angle), times fitorder2 - fitorder1)
+      if (tid < ctl.nbatch) {
+        const float2 k1 = ctl.vary_angle ? polar_rn(ctl.fixed, ctl.pos[tid]) : polar_rn(ctl.pos[tid], ctl.fixed);
+        ctl.kc[tid] = make_float2(__fmul_rn(k1.x, fac), __fmul_rn(k1.y, fac));
       }
     }
     cluster.sync();  // the batch (or the end) is visible to every CTA
@@ -346,77 +429,28 @@ __global__ void __cluster_dims__(kSC, 1, 1) __launch_bounds__(kST, 1) k_k0_searc
     __syncthreads();
     const int nb = nloc;
     if (nb == 0) break;
-    for (int c0 = 0; c0 < nb; c0 += C) {
-      const int nc = min(C, nb - c0);
-      // phase tables of this tile
-      for (int e = tid; e < nc * (tw + th); e += kST) {
-        const int cc = e / (tw + th), r = e - cc * (tw + th);
-        const float2 kk = kloc[c0 + cc];
+    for (int c0 = 0; c0 < nb;) {
+      const int rem = nb - c0;
+      const int cc = rem >= 16 && C >= 16 ? 16 : rem >= 8 && C >= 8 ? 8 : rem >= 4 ? 4 : rem >= 2 ? 2 : 1;
+      float2* ex = tab;                    // [cc][tw]
+      float2* ey = tab + (size_t)cc * tw;  // [cc][th]
+      for (int e = tid; e < cc * (tw + th); e += kST) {
+        const int k = e / (tw + th), r = e - k * (tw + th);
+        const float2 kk = kloc[c0 + k];
         const bool isx = r < tw;
         const double kd = (double)(isx ? kk.x : kk.y) * (double)a.dxy;
         const float hi = (float)kd, lo = (float)(kd - (double)hi);
-        if (isx) ex[cc * tw + r] = phase_factor(x0 + r, nx, hi, lo);
-        else ey[cc * th + (r - tw)] = phase_factor(y0 + (r - tw), ny, hi, lo);
+        if (isx) ex[k * tw + r] = phase_factor(x0 + r, nx, hi, lo);
+        else ey[k * th + (r - tw)] = phase_factor(y0 + (r - tw), ny, hi, lo);
       }
       __syncthreads();
-      float2 acc[C];
-#pragma unroll
-      for (int k = 0; k < C; ++k) acc[k] = make_float2(0.f, 0.f);
-      // two rows per pass share the x phase factors
-      for (int y = y0 + 2 * warp; y < y1; y += 2 * kSW) {
-        const bool two = y + 1 < y1;
-        float2 r0[C], r1[C];
-#pragma unroll
-        for (int k = 0; k < C; ++k) r0[k] = r1[k] = make_float2(0.f, 0.f);
-        for (int x = x0 + lane; x < x1; x += 32) {
-          const float2 p0 = __ldg(a.pmap + (size_t)y * nx + x);
-          const float2 p1 = two ? __ldg(a.pmap + (size_t)(y + 1) * nx + x) : make_float2(0.f, 0.f);
-#pragma unroll
-          for (int k = 0; k < C; ++k) {
-            if (k < nc) {
-              const float2 e = ex[k * tw + (x - x0)];
-              r0[k].x = fmaf(p0.x, e.x, fmaf(-p0.y, e.y, r0[k].x));
-              r0[k].y = fmaf(p0.x, e.y, fmaf(p0.y, e.x, r0[k].y));
-              r1[k].x = fmaf(p1.x, e.x, fmaf(-p1.y, e.y, r1[k].x));
-              r1[k].y = fmaf(p1.x, e.y, fmaf(p1.y, e.x, r1[k].y));
-            }
-          }
-        }
-#pragma unroll
-        for (int k = 0; k < C; ++k) {
-          if (k < nc) {
-            const float2 e0 = ey[k * th + (y - y0)];
-            acc[k].x += r0[k].x * e0.x - r0[k].y * e0.y;
-            acc[k].y += r0[k].x * e0.y + r0[k].y * e0.x;
-            if (two) {
-              const float2 e1 = ey[k * th + (y + 1 - y0)];
-              acc[k].x += r1[k].x * e1.x - r1[k].y * e1.y;
-              acc[k].y += r1[k].x * e1.y + r1[k].y * e1.x;
-            }
-          }
-        }
-      }
-      // CTA sum in double: warps by shuffles, then the warps in order
-#pragma unroll
-      for (int k = 0; k < C; ++k) {
-        double sr = acc[k].x, si = acc[k].y;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          sr += __shfl_xor_sync(0xffffffffu, sr, o);
-          si += __shfl_xor_sync(0xffffffffu, si, o);
-        }
-        if (lane == 0) {
-          wsum[warp][2 * k] = sr;
-          wsum[warp][2 * k + 1] = si;
-        }
-      }
-      __syncthreads();
-      if (tid < 2 * nc) {
-        double s = 0.0;
-        for (int w = 0; w < kSW; ++w) s += wsum[w][tid];
-        lead->red[rank][c0 + (tid >> 1)][tid & 1] = s;
-      }
+      if (cc == 16) chunk<16>(pmap, nx, ex, ey, tw, th, x0, y0, wsum, lead, rank, c0);
+      else if (cc == 8) chunk<8>(pmap, nx, ex, ey, tw, th, x0, y0, wsum, lead, rank, c0);
+      else if (cc == 4) chunk<4>(pmap, nx, ex, ey, tw, th, x0, y0, wsum, lead, rank, c0);
+      else if (cc == 2) chunk<2>(pmap, nx, ex, ey, tw, th, x0, y0, wsum, lead, rank, c0);
+      else chunk<1>(pmap, nx, ex, ey, tw, th, x0, y0, wsum, lead, rank, c0);
       __syncthreads();  // tables and wsum are reused by the next chunk
+      c0 += cc;
     }
     cluster.sync();  // every CTA's partial sums are in the leader
     if (rank == 0 && tid < 2 * nb) {
@@ -459,20 +493,20 @@ bool k0_search_supported(int nx, int ny) { return nx >= 64 && ny >= 8 && search_
 int launch_k0_search(const K0SearchArgs& a, cudaStream_t s, long long* launches)
 {
   const int C = search_chunk(a.nx, a.ny);
-  if (C == 0 || a.nx < 64 || a.ny < 8) return -1;
+  if (C == 0 || a.nx < 64 || a.ny < 8 || a.ndirs < 1 || a.ndirs > kMaxDirs) return -1;
   const size_t tw = (size_t)(a.nx + 1) / 2, th = (size_t)(a.ny + 3) / 4;
   const size_t smem = (size_t)C * (tw + th) * sizeof(float2);
   auto go = [&](auto kern) {
     // raised only (under a lock): handles of other shapes launch concurrently
     allow_dynamic_smem((const void*)kern, smem);
-    kern<<<kSC, kST, smem, s>>>(a);
+    kern<<<kSC * a.ndirs, kST, smem, s>>>(a);
   };
   KernelTimer* kt = kernel_timer();
   if (kt) kt->begin(s);
   if (C == 16) go(k_k0_search<16>);
   else if (C == 8) go(k_k0_search<8>);
   else go(k_k0_search<4>);
-  if (kt) kt->end("k_k0_search", s, (double)a.nx * a.ny * sizeof(float2));
+  if (kt) kt->end("k_k0_search", s, (double)a.ndirs * a.nx * a.ny * sizeof(float2));
   if (launches) *launches += 1;
   return (int)cudaGetLastError();
 }

@@ -173,19 +173,21 @@ constexpr int kMaxClimbSteps = 4096;
 int launch_findk0_finish(const float* peak, float2 guess, int nx, int ny, float dkx, float dky, int fitorder2,
                          float2* k0out, float2* k1out, cudaStream_t s, long long* launches);
 struct K0SearchArgs {
-  const float2* pmap;    // [ny][nx] overlap map of orders (0, fitorder2), built at k1
-  const double* sumxy;   // [2] sum |X|^2, sum |Y|^2 of that build
-  const float2* k0find;  // findk0's k0 (the lines start at its angle and magnitude)
-  float2* k0fit;         // out: the fitted k0
-  double* slot;          // out: XStarY re, im, sum |X|^2, sum |Y|^2 at the fitted k0
-  int* info;             // [0] += candidates evaluated; [1] |= 1 line cache exceeded, 2 batch limit
-  int nx, ny, fitorder2;
+  // per direction:
+  const float2* pmap[kMaxDirs];    // [ny][nx] overlap map of orders (0, fitorder2), built at k1
+  const double* sumxy[kMaxDirs];   // [2] sum |X|^2, sum |Y|^2 of that build
+  const float2* k0find[kMaxDirs];  // findk0's k0 (the lines start at its angle and magnitude)
+  float2* k0fit[kMaxDirs];         // out: the fitted k0
+  double* slot[kMaxDirs];          // out: XStarY re, im, sum |X|^2, sum |Y|^2 at the fitted k0
+  int* info;                       // [0] += candidates evaluated; [1] |= 1 line cache exceeded, 2 batch limit
+  int ndirs, nx, ny, fitorder2;
   float dxy, delta_angle, delta_mag;
 };
 // whether the search's phase tables fit a CTA's shared memory at this size
 bool k0_search_supported(int nx, int ny);
-// one thread-block cluster (8 CTAs): both line searches, their parabola fits
-// and the amplitude at the fitted k0 (fitk0andmodamps, gpuFunctionsImpl.cu:874-1020)
+// one thread-block cluster (8 CTAs) per direction, all directions at once:
+// both line searches, their parabola fits and the amplitude at the fitted k0
+// (fitk0andmodamps, gpuFunctionsImpl.cu:874-1020)
 int launch_k0_search(const K0SearchArgs& a, cudaStream_t s, long long* launches);
 
 // Modulation amplitudes of the last fit and the Wiener-filter weights derived

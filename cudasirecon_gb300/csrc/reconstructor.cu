@@ -505,6 +505,8 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
       {(void**)&d_fit_, sizeof(FitDev)},
       {(void**)&d_fitslots_, (size_t)kMaxDirs * kMaxOrders * 4 * sizeof(double)},
       {(void**)&d_kst_, (size_t)kMaxDirs * 3 * sizeof(float2)},
+      {(void**)&d_pmapd_, (size_t)ndirs_ * nxy * sizeof(float2)},
+      {(void**)&d_sumxyd_, (size_t)ndirs_ * 2 * sizeof(double)},
       {(void**)&d_sinfo_, 2 * sizeof(int)},
       {(void**)&d_asmtab_, asm_table_bytes()},
       {(void**)&d_ex_, (size_t)ndirs_ * norders_ * X_ * sizeof(float2)},
@@ -787,7 +789,8 @@ void SIM_Reconstructor::separate()
 }
 
 // ------------------------------------------------------------------ fitting
-void SIM_Reconstructor::build_overlaps(int d, int o1, int o2, float k0x, float k0y, const float2* kdev, float kfac)
+void SIM_Reconstructor::build_overlaps(int d, int o1, int o2, float k0x, float k0y, const float2* kdev, float kfac,
+                                       float2* pmap, double* sumxy)
 {
   const ReconParams& p = opt.p;
   const ImageParams& ip = opt.ip;
@@ -832,8 +835,8 @@ void SIM_Reconstructor::build_overlaps(int d, int o1, int o2, float k0x, float k
   a.ovl = d_ovl_;
   a.ppart = d_ppart_;
   a.sums = d_sums_;
-  a.pmap = d_pmap_;
-  a.sumxy = d_sumxy_;
+  a.pmap = pmap ? pmap : d_pmap_;
+  a.sumxy = sumxy ? sumxy : d_sumxy_;
   check_launch(launch_overlaps(a, stream_, &launches_), "makeoverlaps");
   ++fit_counts_[0];
   last_ovl_ = a;
@@ -1195,35 +1198,40 @@ bool SIM_Reconstructor::fit_search_on_device()
   const float dkx = 1 / (nx_ * dxy), dky = 1 / (ny_ * dxy);
   check(cudaMemsetAsync(d_sinfo_, 0, 2 * sizeof(int), stream_), "fit");
   long long builds = 0, reductions = 0;
+  K0SearchArgs sa{};
+  const size_t nxy = (size_t)nx_ * ny_;
   for (int d = 0; d < ndirs_; ++d) {
     k0_[d] = k0guess_[d];
     float2* kfind = d_kst_ + 3 * d;
     float2* k1 = kfind + 1;
-    float2* kfit = kfind + 2;
     build_overlaps(d, 0, fo2, k0guess_[d].x, k0guess_[d].y);
     check_launch(launch_crosscorr_peak(d_pmap_, d_cc_, nx_, ny_, d_bval_, d_bidx_, d_peak_, stream_, &launches_),
                  "crosscorr");
     check_launch(launch_findk0_finish(d_peak_, make_float2(k0guess_[d].x, k0guess_[d].y), nx_, ny_, dkx, dky, fo2,
                                       kfind, k1, stream_, &launches_),
                  "findk0");
-    // fitk0andmodamps' first getmodamp rebuilds the overlaps at k1
-    build_overlaps(d, 0, fo2, 0.f, 0.f, k1, (float)fo2);
-    K0SearchArgs sa{};
-    sa.pmap = d_pmap_;
-    sa.sumxy = d_sumxy_;
-    sa.k0find = kfind;
-    sa.k0fit = kfit;
-    sa.slot = d_fitslots_ + (size_t)(d * norders_ + fo2) * 4;
-    sa.info = d_sinfo_;
-    sa.nx = nx_;
-    sa.ny = ny_;
-    sa.fitorder2 = fo2;
-    sa.dxy = dxy;
-    sa.delta_angle = 0.001f;
-    sa.delta_mag = 0.1 / (std::max(nx_, ny_) * dxy);
-    check_launch(launch_k0_search(sa, stream_, &launches_), "k0 search");
+    // fitk0andmodamps' first getmodamp rebuilds the overlaps at k1; every
+    // direction keeps its map for the searches, which run side by side
+    build_overlaps(d, 0, fo2, 0.f, 0.f, k1, (float)fo2, d_pmapd_ + d * nxy, d_sumxyd_ + 2 * d);
+    sa.pmap[d] = d_pmapd_ + d * nxy;
+    sa.sumxy[d] = d_sumxyd_ + 2 * d;
+    sa.k0find[d] = kfind;
+    sa.k0fit[d] = kfind + 2;
+    sa.slot[d] = d_fitslots_ + (size_t)(d * norders_ + fo2) * 4;
     builds += 2;
     reductions += 1;  // the cross-correlation
+  }
+  sa.info = d_sinfo_;
+  sa.ndirs = ndirs_;
+  sa.nx = nx_;
+  sa.ny = ny_;
+  sa.fitorder2 = fo2;
+  sa.dxy = dxy;
+  sa.delta_angle = 0.001f;
+  sa.delta_mag = 0.1 / (std::max(nx_, ny_) * dxy);
+  check_launch(launch_k0_search(sa, stream_, &launches_), "k0 search");
+  for (int d = 0; d < ndirs_; ++d) {
+    float2* kfit = d_kst_ + 3 * d + 2;
     // the other orders at the fitted k0 (overlaps rebuilt each time)
     for (int order = 1; order < norders_; ++order) {
       const int o1 = nz_ == 1 ? order - 1 : 0;

@@ -127,7 +127,10 @@ class SIM_Reconstructor {
   void check_launch(int rc, const char* what);
 
   // fitting helpers (gpuFunctionsImpl.cu:306-1148 semantics)
-  void build_overlaps(int d, int o1, int o2, float k0x, float k0y, const float2* kdev = nullptr, float kfac = 0.f);
+  // kdev: the shift from device memory (times kfac); pmap / sumxy: outputs
+  // other than the handle's single overlap map
+  void build_overlaps(int d, int o1, int o2, float k0x, float k0y, const float2* kdev = nullptr, float kfac = 0.f,
+                      float2* pmap = nullptr, double* sumxy = nullptr);
   int overlap_zdc_bessel(int order2, float k0x, float k0y) const;
   // evaluate XStarY for candidate (angle, mag) pairs on the current overlaps
   void eval_candidates(int o1, int o2, const std::vector<std::pair<float, float>>& cands);
@@ -186,6 +189,8 @@ class SIM_Reconstructor {
   double* d_fitslots_ = nullptr;       // [ndirs * norders][4]: XStarY re, im, sum |X|^2 per order
   float2* d_kst_ = nullptr;            // device search, per direction: findk0's k0, k1, the fitted k0
   int* d_sinfo_ = nullptr;             // device search: candidates evaluated, status
+  float2* d_pmapd_ = nullptr;          // device search: each direction's overlap map [ndirs][ny][nx]
+  double* d_sumxyd_ = nullptr;         // and its sum |X|^2, sum |Y|^2 [ndirs][2]
   void* d_asmtab_ = nullptr;           // assembly slot tables
   bool asm_tables_valid_ = false;
   int asm_tables_zdc_[simrecon::kMaxOrders] = {0};
