@@ -382,6 +382,7 @@ __global__ void __cluster_dims__(kSC, 1, 1) __launch_bounds__(kST, 1) k_k0_searc
   __shared__ SearchLine lines[2];
   __shared__ double wsum[kSW][2 * 16];
   __shared__ float2 kloc[kSB];
+  __shared__ float2 khl[kSB][2];  // k dxy of each candidate and axis as hi + lo floats
   __shared__ int nloc;
   extern __shared__ float2 tab[];
   SearchCtl* lead = cluster.map_shared_rank(&ctl, 0);
@@ -429,6 +430,13 @@ __global__ void __cluster_dims__(kSC, 1, 1) __launch_bounds__(kST, 1) k_k0_searc
     __syncthreads();
     const int nb = nloc;
     if (nb == 0) break;
+    if (tid < 2 * nb) {  // the double products once per candidate and axis (FP64 is slow on this GPU)
+      const float2 kk = kloc[tid >> 1];
+      const double kd = (double)((tid & 1) ? kk.y : kk.x) * (double)a.dxy;
+      const float hi = (float)kd;
+      khl[tid >> 1][tid & 1] = make_float2(hi, (float)(kd - (double)hi));
+    }
+    __syncthreads();
     for (int c0 = 0; c0 < nb;) {
       const int rem = nb - c0;
       const int cc = rem >= 16 && C >= 16 ? 16 : rem >= 8 && C >= 8 ? 8 : rem >= 4 ? 4 : rem >= 2 ? 2 : 1;
@@ -436,12 +444,10 @@ __global__ void __cluster_dims__(kSC, 1, 1) __launch_bounds__(kST, 1) k_k0_searc
       float2* ey = tab + (size_t)cc * tw;  // [cc][th]
       for (int e = tid; e < cc * (tw + th); e += kST) {
         const int k = e / (tw + th), r = e - k * (tw + th);
-        const float2 kk = kloc[c0 + k];
         const bool isx = r < tw;
-        const double kd = (double)(isx ? kk.x : kk.y) * (double)a.dxy;
-        const float hi = (float)kd, lo = (float)(kd - (double)hi);
-        if (isx) ex[k * tw + r] = phase_factor(x0 + r, nx, hi, lo);
-        else ey[k * th + (r - tw)] = phase_factor(y0 + (r - tw), ny, hi, lo);
+        const float2 hl = khl[c0 + k][isx ? 0 : 1];
+        if (isx) ex[k * tw + r] = phase_factor(x0 + r, nx, hl.x, hl.y);
+        else ey[k * th + (r - tw)] = phase_factor(y0 + (r - tw), ny, hl.x, hl.y);
       }
       __syncthreads();
       if (cc == 16) chunk<16>(pmap, nx, ex, ey, tw, th, x0, y0, wsum, lead, rank, c0);
@@ -488,7 +494,14 @@ static int search_chunk(int nx, int ny)
   return 0;
 }
 
-bool k0_search_supported(int nx, int ny) { return nx >= 64 && ny >= 8 && search_chunk(nx, ny) > 0; }
+// Up to 1024^2 maps (a tile of at most 512 x 256 per CTA).  Larger maps
+// take the host-driven search, whose candidate batches run on every SM: one
+// cluster per direction would spend milliseconds per batch on a 1024 x 512
+// tile.
+bool k0_search_supported(int nx, int ny)
+{
+  return nx >= 64 && ny >= 8 && (long long)nx * ny <= 1024LL * 1024 && search_chunk(nx, ny) > 0;
+}
 
 int launch_k0_search(const K0SearchArgs& a, cudaStream_t s, long long* launches)
 {

@@ -248,8 +248,10 @@ void SRX_setFilterFusion(SIM_Reconstructor* sr, int on);
  * on = 0, driven from the host.  Both visit the same float32 angles and
  * magnitudes (cudaSirecon.cpp:296-408, gpuFunctionsImpl.cu:306-372,
  * 874-1044); the fitted k0 agree within float rounding of the start angle.
- * Bessel mode, the overlap debug dump and later time points of a series
- * (which may fall back to time 0's k0) use the host-driven search. */
+ * Bessel mode, the overlap debug dump, later time points of a series
+ * (which may fall back to time 0's k0) and images larger than 1024 x 1024
+ * (whose candidate batches are better spread over the whole GPU) use the
+ * host-driven search. */
 void SRX_setDeviceK0Search(SIM_Reconstructor* sr, int on);
 
 /* Number of this library's kernels launched since the handle was created. */
