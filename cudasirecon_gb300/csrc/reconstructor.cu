@@ -468,6 +468,7 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
   const size_t nspec = (size_t)ndirs_ * nph_ * nz_ * ny_ * nxh_;
   const int nzb = 2 * zdc_ovl_ + 1;
   const size_t nxy = (size_t)nx_ * ny_;
+  fit_lanes_ = std::max(1, std::min(ndirs_, (int)kFitLanes));
   // assembly scratch: every slot of the volume (at most nz planes of
   // 1 + ndirs*(norders-1) slots) when that fits in 2 GiB, else as many as do
   // (at least one plane's worth); the slots are processed in plane groups
@@ -490,18 +491,19 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
       {(void**)&d_sepmat_, sepmat_.size() * sizeof(float)},
       {(void**)&d_apofact_, (size_t)kMaxApo * sizeof(float)},
       {(void**)&d_otf_, hotf.size() * sizeof(float2)},
-      {(void**)&d_ovl_, 2 * (size_t)nzb * nxy * sizeof(float2)},
-      {(void**)&d_ppart_, (size_t)nzb * nxy * sizeof(float2)},
-      {(void**)&d_sums_, 2 * (size_t)(nx_ + 1) * nzb * sizeof(double)},
-      {(void**)&d_pmap_, nxy * sizeof(float2)},
-      {(void**)&d_sumxy_, 2 * sizeof(double)},
+      // the fit's working buffers, one set per fit lane (directions fitted side by side)
+      {(void**)&d_ovl_, fit_lanes_ * ovl_lane_elems() * sizeof(float2)},
+      {(void**)&d_ppart_, fit_lanes_ * ppart_lane_elems() * sizeof(float2)},
+      {(void**)&d_sums_, fit_lanes_ * sums_lane_elems() * sizeof(double)},
+      {(void**)&d_pmap_, fit_lanes_ * nxy * sizeof(float2)},
+      {(void**)&d_sumxy_, fit_lanes_ * 2 * sizeof(double)},
       {(void**)&d_cc_, nxy * sizeof(float2)},
       {(void**)&d_bval_, 256 * sizeof(float)},
       {(void**)&d_bidx_, 256 * sizeof(int)},
       {(void**)&d_peak_, 8 * sizeof(float)},
-      {(void**)&d_tables_, (size_t)kMaxCand * (nx_ + ny_) * sizeof(float2)},
-      {(void**)&d_partial_, (size_t)kModampBlocks * kMaxCand * 2 * sizeof(double)},
-      {(void**)&d_xstary_, (size_t)kMaxCand * 2 * sizeof(double)},
+      {(void**)&d_tables_, fit_lanes_ * tables_lane_elems() * sizeof(float2)},
+      {(void**)&d_partial_, fit_lanes_ * partial_lane_elems() * sizeof(double)},
+      {(void**)&d_xstary_, fit_lanes_ * (size_t)kMaxCand * 2 * sizeof(double)},
       {(void**)&d_fit_, sizeof(FitDev)},
       {(void**)&d_fitslots_, (size_t)kMaxDirs * kMaxOrders * 4 * sizeof(double)},
       {(void**)&d_kst_, (size_t)kMaxDirs * 3 * sizeof(float2)},
@@ -526,6 +528,11 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
   }
   check(cudaGetDevice(&device_), "cudaGetDevice");
   check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  for (int l = 1; l < fit_lanes_; ++l) {
+    check(cudaStreamCreateWithFlags(&fit_stream_[l], cudaStreamNonBlocking), "cudaStreamCreate");
+    check(cudaEventCreateWithFlags(&fit_join_[l], cudaEventDisableTiming), "cudaEventCreate");
+  }
+  check(cudaEventCreateWithFlags(&fit_fork_, cudaEventDisableTiming), "cudaEventCreate");
   cudaError_t e = cudaMalloc((void**)&arena_, total);
   if (e != cudaSuccess) {
     *err = std::string("device allocation of ") + std::to_string(total >> 20) + " MiB failed: " +
@@ -578,6 +585,11 @@ SIM_Reconstructor::~SIM_Reconstructor()
   if (d_bgslope_) cudaFree(d_bgslope_);
   if (pre_own_) cudaFree(pre_own_);
   if (h_pinned_) cudaFreeHost(h_pinned_);
+  for (int l = 1; l < kFitLanes; ++l) {
+    if (fit_stream_[l]) cudaStreamDestroy(fit_stream_[l]);
+    if (fit_join_[l]) cudaEventDestroy(fit_join_[l]);
+  }
+  if (fit_fork_) cudaEventDestroy(fit_fork_);
   if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -790,8 +802,9 @@ void SIM_Reconstructor::separate()
 
 // ------------------------------------------------------------------ fitting
 void SIM_Reconstructor::build_overlaps(int d, int o1, int o2, float k0x, float k0y, const float2* kdev, float kfac,
-                                       float2* pmap, double* sumxy)
+                                       float2* pmap, double* sumxy, int lane)
 {
+  cudaStream_t s = lane_stream(lane);
   const ReconParams& p = opt.p;
   const ImageParams& ip = opt.ip;
   OverlapArgs a{};
@@ -832,12 +845,12 @@ void SIM_Reconstructor::build_overlaps(int d, int o1, int o2, float k0x, float k
   a.otf.nxotf = p.nxotf;
   a.otf.dkrotf = p.dkrotf;
   a.otf.kzscale = kzscale;
-  a.ovl = d_ovl_;
-  a.ppart = d_ppart_;
-  a.sums = d_sums_;
-  a.pmap = pmap ? pmap : d_pmap_;
-  a.sumxy = sumxy ? sumxy : d_sumxy_;
-  check_launch(launch_overlaps(a, stream_, &launches_), "makeoverlaps");
+  a.ovl = d_ovl_ + lane * ovl_lane_elems();
+  a.ppart = d_ppart_ + lane * ppart_lane_elems();
+  a.sums = d_sums_ + lane * sums_lane_elems();
+  a.pmap = pmap ? pmap : lane_pmap(lane);
+  a.sumxy = sumxy ? sumxy : d_sumxy_ + 2 * lane;
+  check_launch(launch_overlaps(a, s, &launches_), "makeoverlaps");
   ++fit_counts_[0];
   last_ovl_ = a;
   cur_o1_ = o1;
@@ -1230,22 +1243,27 @@ bool SIM_Reconstructor::fit_search_on_device()
   sa.delta_angle = 0.001f;
   sa.delta_mag = 0.1 / (std::max(nx_, ny_) * dxy);
   check_launch(launch_k0_search(sa, stream_, &launches_), "k0 search");
+  const int nl = lanes_begin();
   for (int d = 0; d < ndirs_; ++d) {
     float2* kfit = d_kst_ + 3 * d + 2;
+    const int lane = d % nl;
+    cudaStream_t ls = lane_stream(lane);
     // the other orders at the fitted k0 (overlaps rebuilt each time)
     for (int order = 1; order < norders_; ++order) {
       const int o1 = nz_ == 1 ? order - 1 : 0;
       if (nz_ == 1 ? order < 2 : order == fo2) continue;
-      build_overlaps(d, o1, order, 0.f, 0.f, kfit, (float)(order - o1));
-      check_launch(launch_modamp_device_k(d_pmap_, nx_, ny_, dxy, kfit, (float)(order - o1), d_tables_, d_partial_,
-                                          d_xstary_, stream_, &launches_),
+      build_overlaps(d, o1, order, 0.f, 0.f, kfit, (float)(order - o1), nullptr, nullptr, lane);
+      check_launch(launch_modamp_device_k(lane_pmap(lane), nx_, ny_, dxy, kfit, (float)(order - o1),
+                                          lane_tables(lane), lane_partial(lane), lane_xstary(lane), ls, &launches_),
                    "modamp");
       double* slot = d_fitslots_ + (size_t)(d * norders_ + order) * 4;
-      check_launch(launch_copy_out(d_xstary_, slot, 4, d_sumxy_, slot + 2, 4, stream_, &launches_), "modamp");
+      check_launch(launch_copy_out(lane_xstary(lane), slot, 4, d_sumxy_ + 2 * lane, slot + 2, 4, ls, &launches_),
+                   "modamp");
       ++builds;
       ++reductions;
     }
   }
+  lanes_end(nl);
   check_launch(launch_fit_finish(d_fitslots_, fit_finish_args(), d_fit_, stream_, &launches_), "fit results");
   // the fitted k0s and the search's counters through mapped host memory
   double* base = dh_pinned_ + 320;
@@ -1306,24 +1324,64 @@ void SIM_Reconstructor::fit_on_device()
   const ReconParams& p = opt.p;
   const ImageParams& ip = opt.ip;
   const bool reuse = ip.ntimes > 1 && ip.curTimeIdx > 0 && p.bUseTime0k0;
+  // the directions are independent: each runs on its own fit lane (stream
+  // and working buffers), joined before the amplitudes are finished
+  const int nl = lanes_begin();
   for (int d = 0; d < ndirs_; ++d) {
     if (!reuse) k0_[d] = k0guess_[d];
     const float2v k = k0_[d];
+    const int lane = d % nl;
     for (int order = 1; order < norders_; ++order) {
-      build_overlaps(d, 0, order, k.x, k.y);
+      build_overlaps(d, 0, order, k.x, k.y, nullptr, 0.f, nullptr, nullptr, lane);
       CandList kc{};
       kc.k[0] = make_float2(k.x * order, k.y * order);
-      check_launch(launch_modamp_candidates(d_pmap_, nx_, ny_, ip.dxy, kc, 1, d_tables_, d_partial_, d_xstary_,
-                                            stream_, &launches_),
+      check_launch(launch_modamp_candidates(lane_pmap(lane), nx_, ny_, ip.dxy, kc, 1, lane_tables(lane),
+                                            lane_partial(lane), lane_xstary(lane), lane_stream(lane), &launches_),
                    "modamp");
       ++fit_counts_[1];
       double* slot = d_fitslots_ + (size_t)(d * norders_ + order) * 4;
-      check_launch(launch_copy_out(d_xstary_, slot, 4, d_sumxy_, slot + 2, 2, stream_, &launches_), "modamp");
+      check_launch(launch_copy_out(lane_xstary(lane), slot, 4, d_sumxy_ + 2 * lane, slot + 2, 2, lane_stream(lane),
+                                   &launches_),
+                   "modamp");
     }
   }
+  lanes_end(nl);
   check_launch(launch_fit_finish(d_fitslots_, fit_finish_args(), d_fit_, stream_, &launches_), "modamp");
   cur_o1_ = cur_o2_ = -1;
   amps_on_device_only_ = true;
+}
+
+// Fit lanes: per-lane working buffers of the overlap builds and amplitude
+// evaluations, and the lane's stream (lane 0: the handle's stream)
+size_t SIM_Reconstructor::ovl_lane_elems() const { return 2 * (size_t)(2 * zdc_ovl_ + 1) * nx_ * ny_; }
+size_t SIM_Reconstructor::ppart_lane_elems() const { return (size_t)(2 * zdc_ovl_ + 1) * nx_ * ny_; }
+size_t SIM_Reconstructor::sums_lane_elems() const { return 2 * (size_t)(nx_ + 1) * (2 * zdc_ovl_ + 1); }
+size_t SIM_Reconstructor::tables_lane_elems() const { return (size_t)kMaxCand * (nx_ + ny_); }
+size_t SIM_Reconstructor::partial_lane_elems() const { return (size_t)kModampBlocks * kMaxCand * 2; }
+float2* SIM_Reconstructor::lane_pmap(int l) const { return d_pmap_ + (size_t)l * nx_ * ny_; }
+float2* SIM_Reconstructor::lane_tables(int l) const { return d_tables_ + l * tables_lane_elems(); }
+double* SIM_Reconstructor::lane_partial(int l) const { return d_partial_ + l * partial_lane_elems(); }
+double* SIM_Reconstructor::lane_xstary(int l) const { return d_xstary_ + (size_t)l * kMaxCand * 2; }
+cudaStream_t SIM_Reconstructor::lane_stream(int l) const { return l == 0 ? stream_ : fit_stream_[l]; }
+
+// fork the fit lanes off the handle's stream; returns how many are used (one
+// while profiling, so that every kernel's CUDA-event time is its own)
+int SIM_Reconstructor::lanes_begin()
+{
+  const int nl = profiling_ ? 1 : std::min(fit_lanes_, ndirs_);
+  if (nl > 1) {
+    check(cudaEventRecord(fit_fork_, stream_), "fit fork");
+    for (int l = 1; l < nl; ++l) check(cudaStreamWaitEvent(fit_stream_[l], fit_fork_, 0), "fit fork");
+  }
+  return nl;
+}
+
+void SIM_Reconstructor::lanes_end(int nl)
+{
+  for (int l = 1; l < nl; ++l) {
+    check(cudaEventRecord(fit_join_[l], fit_stream_[l]), "fit join");
+    check(cudaStreamWaitEvent(stream_, fit_join_[l], 0), "fit join");
+  }
 }
 
 // the device's amplitudes into amp_ (waits for the stream)

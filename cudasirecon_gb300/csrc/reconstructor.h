@@ -130,7 +130,21 @@ class SIM_Reconstructor {
   // kdev: the shift from device memory (times kfac); pmap / sumxy: outputs
   // other than the handle's single overlap map
   void build_overlaps(int d, int o1, int o2, float k0x, float k0y, const float2* kdev = nullptr, float kfac = 0.f,
-                      float2* pmap = nullptr, double* sumxy = nullptr);
+                      float2* pmap = nullptr, double* sumxy = nullptr, int lane = 0);
+  // fit lanes (directions fitted side by side on their own streams)
+  static constexpr int kFitLanes = 3;
+  size_t ovl_lane_elems() const;
+  size_t ppart_lane_elems() const;
+  size_t sums_lane_elems() const;
+  size_t tables_lane_elems() const;
+  size_t partial_lane_elems() const;
+  float2* lane_pmap(int l) const;
+  float2* lane_tables(int l) const;
+  double* lane_partial(int l) const;
+  double* lane_xstary(int l) const;
+  cudaStream_t lane_stream(int l) const;
+  int lanes_begin();
+  void lanes_end(int nl);
   int overlap_zdc_bessel(int order2, float k0x, float k0y) const;
   // evaluate XStarY for candidate (angle, mag) pairs on the current overlaps
   void eval_candidates(int o1, int o2, const std::vector<std::pair<float, float>>& cands);
@@ -155,6 +169,10 @@ class SIM_Reconstructor {
   int zdc_ovl_ = 0;  // makeoverlaps zdistcutoff
   bool otf_dk_from_header_ = false;  // MRC OTF: dkr / dkz taken from its header
   cudaStream_t stream_ = nullptr;
+  int fit_lanes_ = 1;  // set at setup: min(ndirs, kFitLanes)
+  cudaStream_t fit_stream_[kFitLanes] = {nullptr, nullptr, nullptr};
+  cudaEvent_t fit_join_[kFitLanes] = {nullptr, nullptr, nullptr};
+  cudaEvent_t fit_fork_ = nullptr;
   int device_ = 0;
   bool filter_fusion_ = true;
   bool device_search_ = true;
