@@ -468,7 +468,7 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
   const size_t nspec = (size_t)ndirs_ * nph_ * nz_ * ny_ * nxh_;
   const int nzb = 2 * zdc_ovl_ + 1;
   const size_t nxy = (size_t)nx_ * ny_;
-  fit_lanes_ = std::max(1, std::min(ndirs_, (int)kFitLanes));
+  fit_lanes_ = std::max(1, std::min(ndirs_ * std::max(1, norders_ - 1), (int)kFitLanes));
   // assembly scratch: every slot of the volume (at most nz planes of
   // 1 + ndirs*(norders-1) slots) when that fits in 2 GiB, else as many as do
   // (at least one plane's worth); the slots are processed in plane groups
@@ -1246,12 +1246,12 @@ bool SIM_Reconstructor::fit_search_on_device()
   const int nl = lanes_begin();
   for (int d = 0; d < ndirs_; ++d) {
     float2* kfit = d_kst_ + 3 * d + 2;
-    const int lane = d % nl;
-    cudaStream_t ls = lane_stream(lane);
     // the other orders at the fitted k0 (overlaps rebuilt each time)
     for (int order = 1; order < norders_; ++order) {
       const int o1 = nz_ == 1 ? order - 1 : 0;
       if (nz_ == 1 ? order < 2 : order == fo2) continue;
+      const int lane = (d * (norders_ - 1) + order - 1) % nl;
+      cudaStream_t ls = lane_stream(lane);
       build_overlaps(d, o1, order, 0.f, 0.f, kfit, (float)(order - o1), nullptr, nullptr, lane);
       check_launch(launch_modamp_device_k(lane_pmap(lane), nx_, ny_, dxy, kfit, (float)(order - o1),
                                           lane_tables(lane), lane_partial(lane), lane_xstary(lane), ls, &launches_),
@@ -1324,14 +1324,15 @@ void SIM_Reconstructor::fit_on_device()
   const ReconParams& p = opt.p;
   const ImageParams& ip = opt.ip;
   const bool reuse = ip.ntimes > 1 && ip.curTimeIdx > 0 && p.bUseTime0k0;
-  // the directions are independent: each runs on its own fit lane (stream
-  // and working buffers), joined before the amplitudes are finished
+  // the (direction, order) overlap pairs are independent: each runs on its
+  // own fit lane (stream and working buffers), joined before the amplitudes
+  // are finished
   const int nl = lanes_begin();
   for (int d = 0; d < ndirs_; ++d) {
     if (!reuse) k0_[d] = k0guess_[d];
     const float2v k = k0_[d];
-    const int lane = d % nl;
     for (int order = 1; order < norders_; ++order) {
+      const int lane = (d * (norders_ - 1) + order - 1) % nl;
       build_overlaps(d, 0, order, k.x, k.y, nullptr, 0.f, nullptr, nullptr, lane);
       CandList kc{};
       kc.k[0] = make_float2(k.x * order, k.y * order);
@@ -1368,7 +1369,7 @@ cudaStream_t SIM_Reconstructor::lane_stream(int l) const { return l == 0 ? strea
 // while profiling, so that every kernel's CUDA-event time is its own)
 int SIM_Reconstructor::lanes_begin()
 {
-  const int nl = profiling_ ? 1 : std::min(fit_lanes_, ndirs_);
+  const int nl = profiling_ ? 1 : fit_lanes_;
   if (nl > 1) {
     check(cudaEventRecord(fit_fork_, stream_), "fit fork");
     for (int l = 1; l < nl; ++l) check(cudaStreamWaitEvent(fit_stream_[l], fit_fork_, 0), "fit fork");

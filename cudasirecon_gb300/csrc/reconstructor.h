@@ -131,8 +131,9 @@ class SIM_Reconstructor {
   // other than the handle's single overlap map
   void build_overlaps(int d, int o1, int o2, float k0x, float k0y, const float2* kdev = nullptr, float kfac = 0.f,
                       float2* pmap = nullptr, double* sumxy = nullptr, int lane = 0);
-  // fit lanes (directions fitted side by side on their own streams)
-  static constexpr int kFitLanes = 3;
+  // fit lanes (the overlap pairs of the fit built side by side on their own
+  // streams)
+  static constexpr int kFitLanes = 3;  // six lanes measured 1 % faster for twice the buffers
   size_t ovl_lane_elems() const;
   size_t ppart_lane_elems() const;
   size_t sums_lane_elems() const;
@@ -169,9 +170,9 @@ class SIM_Reconstructor {
   int zdc_ovl_ = 0;  // makeoverlaps zdistcutoff
   bool otf_dk_from_header_ = false;  // MRC OTF: dkr / dkz taken from its header
   cudaStream_t stream_ = nullptr;
-  int fit_lanes_ = 1;  // set at setup: min(ndirs, kFitLanes)
-  cudaStream_t fit_stream_[kFitLanes] = {nullptr, nullptr, nullptr};
-  cudaEvent_t fit_join_[kFitLanes] = {nullptr, nullptr, nullptr};
+  int fit_lanes_ = 1;  // set at setup: min(ndirs * (norders - 1), kFitLanes)
+  cudaStream_t fit_stream_[kFitLanes] = {};
+  cudaEvent_t fit_join_[kFitLanes] = {};
   cudaEvent_t fit_fork_ = nullptr;
   int device_ = 0;
   bool filter_fusion_ = true;
