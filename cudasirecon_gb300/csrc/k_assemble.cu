@@ -690,7 +690,9 @@ __global__ void __launch_bounds__(kXwWarps * 32, 3) k_asm_xw(AssembleArgs a, con
   const int g = lane / P, p = lane - g * P;
   const int yr = (blockIdx.x * kXwWarps + warp) * G + g;
   const bool act = yr < a.Y;
-  const int pidx = blockIdx.y;
+  // output planes in the reverse of the order the y pass wrote their slots:
+  // the last slots written are still in L2 when the first CTAs read them
+  const int pidx = gridDim.y - 1 - blockIdx.y;
   const int s0 = plane_slot0[pidx], ns = plane_nslot[pidx], zout = plane_zout[pidx];
   const int nx = a.nx, Y = a.Y, xlo = nx / 2 - 1;
   float2* xb = xs + (warp * G + g) * XB;

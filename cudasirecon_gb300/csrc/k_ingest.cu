@@ -325,7 +325,10 @@ __global__ void __launch_bounds__(kThreads) k_fft_cols_4s(float2* data, int ncol
   constexpr int R1 = colfft_r1(N), W = 8;
   extern __shared__ float2 sm[];  // ColFft<N, R1, W>::kSmemElems
   const int c0 = blockIdx.x * W;
-  float2* base = data + (size_t)blockIdx.y * N * ncol + c0;
+  // planes in the reverse of the order the x pass wrote them: the last ones
+  // written are still in L2 when the first CTAs read them
+  const int plane = gridDim.y - 1 - blockIdx.y;
+  float2* base = data + (size_t)plane * N * ncol + c0;
   const int nc = min(W, ncol - c0);
   colfft_stage1<N, R1, W, -1>(sm, tw, [&](int row, int c) {
     return c < nc ? base[(size_t)row * ncol + c] : make_float2(0.f, 0.f);
