@@ -497,10 +497,10 @@ bool SIM_Reconstructor::setup(int nx, int ny, int nimages, int nwaves, const Sta
       {(void**)&d_sums_, fit_lanes_ * sums_lane_elems() * sizeof(double)},
       {(void**)&d_pmap_, fit_lanes_ * nxy * sizeof(float2)},
       {(void**)&d_sumxy_, fit_lanes_ * 2 * sizeof(double)},
-      {(void**)&d_cc_, nxy * sizeof(float2)},
-      {(void**)&d_bval_, 256 * sizeof(float)},
-      {(void**)&d_bidx_, 256 * sizeof(int)},
-      {(void**)&d_peak_, 8 * sizeof(float)},
+      {(void**)&d_cc_, fit_lanes_ * nxy * sizeof(float2)},
+      {(void**)&d_bval_, fit_lanes_ * 256 * sizeof(float)},
+      {(void**)&d_bidx_, fit_lanes_ * 256 * sizeof(int)},
+      {(void**)&d_peak_, fit_lanes_ * 8 * sizeof(float)},
       {(void**)&d_tables_, fit_lanes_ * tables_lane_elems() * sizeof(float2)},
       {(void**)&d_partial_, fit_lanes_ * partial_lane_elems() * sizeof(double)},
       {(void**)&d_xstary_, fit_lanes_ * (size_t)kMaxCand * 2 * sizeof(double)},
@@ -1213,19 +1213,25 @@ bool SIM_Reconstructor::fit_search_on_device()
   long long builds = 0, reductions = 0;
   K0SearchArgs sa{};
   const size_t nxy = (size_t)nx_ * ny_;
+  // each direction's findk0 and first overlap rebuild on its fit lane
+  const int nl0 = lanes_begin();
   for (int d = 0; d < ndirs_; ++d) {
     k0_[d] = k0guess_[d];
     float2* kfind = d_kst_ + 3 * d;
     float2* k1 = kfind + 1;
-    build_overlaps(d, 0, fo2, k0guess_[d].x, k0guess_[d].y);
-    check_launch(launch_crosscorr_peak(d_pmap_, d_cc_, nx_, ny_, d_bval_, d_bidx_, d_peak_, stream_, &launches_),
+    const int lane = d % nl0;
+    cudaStream_t ls = lane_stream(lane);
+    float* peak = d_peak_ + 8 * lane;
+    build_overlaps(d, 0, fo2, k0guess_[d].x, k0guess_[d].y, nullptr, 0.f, nullptr, nullptr, lane);
+    check_launch(launch_crosscorr_peak(lane_pmap(lane), d_cc_ + lane * nxy, nx_, ny_, d_bval_ + 256 * lane,
+                                       d_bidx_ + 256 * lane, peak, ls, &launches_),
                  "crosscorr");
-    check_launch(launch_findk0_finish(d_peak_, make_float2(k0guess_[d].x, k0guess_[d].y), nx_, ny_, dkx, dky, fo2,
-                                      kfind, k1, stream_, &launches_),
+    check_launch(launch_findk0_finish(peak, make_float2(k0guess_[d].x, k0guess_[d].y), nx_, ny_, dkx, dky, fo2,
+                                      kfind, k1, ls, &launches_),
                  "findk0");
     // fitk0andmodamps' first getmodamp rebuilds the overlaps at k1; every
     // direction keeps its map for the searches, which run side by side
-    build_overlaps(d, 0, fo2, 0.f, 0.f, k1, (float)fo2, d_pmapd_ + d * nxy, d_sumxyd_ + 2 * d);
+    build_overlaps(d, 0, fo2, 0.f, 0.f, k1, (float)fo2, d_pmapd_ + d * nxy, d_sumxyd_ + 2 * d, lane);
     sa.pmap[d] = d_pmapd_ + d * nxy;
     sa.sumxy[d] = d_sumxyd_ + 2 * d;
     sa.k0find[d] = kfind;
@@ -1234,6 +1240,7 @@ bool SIM_Reconstructor::fit_search_on_device()
     builds += 2;
     reductions += 1;  // the cross-correlation
   }
+  lanes_end(nl0);
   sa.info = d_sinfo_;
   sa.ndirs = ndirs_;
   sa.nx = nx_;
