@@ -18,8 +18,9 @@
 // and parabola fits with separately rounded float operations, as the
 // reference's host code does.  The candidate values themselves come from the
 // device's cosf/sinf/atan2f, which may differ from a host libm in the last
-// bit, so the fitted k0 matches the host-driven search to within float
-// rounding of the start angle (about 1e-5 pixel), not bit for bit.
+// bit, and the phase factors from float sincospi of an exactly reduced
+// argument (the host-driven evaluation uses double sincos), so the fitted k0
+// matches the host-driven search to a few 1e-5 pixel, not bit for bit.
 #include <cooperative_groups.h>
 
 #include "kernels.h"
@@ -119,8 +120,8 @@ struct ClimbResult {
   float x1, amp1;
 };
 
-// One line search of fitk0andmodamps (gpuFunctionsImpl.cu:905-975 for the
-// angle, 979-1010 for the magnitude), replayed from the line's cached values;
+// One line search of fitk0andmodamps (gpuFunctionsImpl.cu:902-942 for the
+// angle, 944-985 for the magnitude), replayed from the line's cached values;
 // x1 / amp1 carry over from the previous line as in the reference (declared
 // once, not reset between the two searches).
 __device__ ClimbResult run_climb(const SearchLine& L, float x1, float amp1)
